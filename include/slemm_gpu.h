@@ -1,0 +1,175 @@
+/*
+ * slemm_gpu.h — C ABI of the GB300 engine for SLEMM's packed-genotype path.
+ *
+ * Every entry point returns an int status (SLEMM_OK = 0, negative on error) and never throws
+ * across the ABI.  slemm_gpu_last_error() returns a thread-local message for the last failure.
+ * Pointers are plain host or device pointers as stated per call; matrices are column-major
+ * FP32 with an explicit leading dimension, like the Eigen MatrixXf the reference passes around.
+ *
+ * Threading: one host thread per handle; all work is ordered on the handle's CUDA stream.
+ * The library starts no host threads of its own.
+ *
+ * Reference interfaces replaced (paths inside jiang18/slemm):
+ *   - the genotype store `std::vector<std::vector<bool>> kmat`      src/option.cpp:347
+ *     filled by the .bed decoder                                    src/input.cpp:343-386
+ *   - the operator family H0_quadform_mv / H0_ldet_mv / lnr_op_select,
+ *     weighted_rmatvec / rmatvec / matvec                          src/reml.cpp:8-233
+ *   - L_Seed / L_Solve / SLQ_LDet                                  src/reml.cpp:246-451
+ *   - SLDF_REML (DF-REML, --reml --lrt)                            src/reml.cpp:549-690
+ *   - LMC_REML  (MC-REML, --reml)                                  src/reml.cpp:730-883
+ *   - computeTotalGeneticValuePLINK (--pred GEBV)                  src/pred.cpp:4-141
+ *   - the per-variant GRAMMAR-Gamma loop of slemm_gamma            bin/slemm_gamma.py:302-325
+ */
+#ifndef SLEMM_GPU_H_
+#define SLEMM_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define SLEMM_OK               0
+#define SLEMM_ERR_ARG         -1   /* invalid argument (null pointer, bad size, bad enum)     */
+#define SLEMM_ERR_CUDA        -2   /* a CUDA runtime call failed                               */
+#define SLEMM_ERR_NOMEM       -3   /* device or host allocation failed                         */
+#define SLEMM_ERR_STATE       -4   /* call out of order (e.g. op before set_weights)           */
+#define SLEMM_ERR_RANK        -5   /* fixed-effect design matrix not of full rank              */
+#define SLEMM_ERR_NUMERIC     -6   /* non-finite value where a finite one is required          */
+#define SLEMM_ERR_UNSUPPORTED -7   /* no sm_103a device, or a size beyond a kernel's limit      */
+
+/* ---- operator kinds (src/reml.cpp:8-233) ------------------------------------------------ */
+#define SLEMM_OP_QUADFORM  0  /* out = rr∘ΣZ W Zᵀ(rr∘(v−QQᵀv)) + τ0 v − QQᵀ(·)  H0_quadform_mv :8   */
+#define SLEMM_OP_LDET      1  /* out = rr∘Z W Zᵀ(rr∘v) + τ0 v                    H0_ldet_mv     :52  */
+#define SLEMM_OP_MATVEC    2  /* out(n×k) = Z_c v,      v is m×k                 matvec         :198 */
+#define SLEMM_OP_RMATVEC   3  /* out(m×k) = Z_cᵀ v,     v is n×k                 rmatvec        :160 */
+#define SLEMM_OP_WRMATVEC  4  /* out(m×k) = W Z_cᵀ v                              weighted_rmatvec :121 */
+
+/* ---- precision of the packed products --------------------------------------------------- */
+#define SLEMM_PREC_FP32    0  /* CUDA-core FP32 FMA on exact integer counts                      */
+#define SLEMM_PREC_BF16X2  1  /* tcgen05 BF16 MMA, dense side split hi+lo, FP32 accumulation     */
+#define SLEMM_PREC_BF16X3  2  /* tcgen05 BF16 MMA, dense side split hi+mid+lo (≈FP32 mantissa)   */
+
+/* ---- memory location flags ---------------------------------------------------------------- */
+#define SLEMM_MEM_HOST     0
+#define SLEMM_MEM_DEVICE   1
+
+typedef struct slemm_geno  slemm_geno;   /* packed genotypes resident in HBM + weights         */
+typedef struct slemm_lseed slemm_lseed;  /* Lanczos seed system (basis, Jacobi coefficients)  */
+
+/* ---- library / device ------------------------------------------------------------------------ */
+const char* slemm_gpu_last_error(void);
+int slemm_gpu_version(void);                       /* 10000*major + 100*minor + patch */
+/* Selects the device, checks it is sm_103 class. */
+int slemm_gpu_init(int device);
+/* Number of GPU kernel launches issued by this library since load (all handles). */
+int64_t slemm_gpu_launch_count(void);
+
+/* ---- genotype handle ------------------------------------------------------------------------- */
+/* Replaces kmat + read_plink_bin_geno_file_and_generate_pxvb_data's decode (src/input.cpp:343-386).
+ * bed_rows: host pointer to m SNP-major .bed rows (magic bytes already skipped), row j at
+ *   bed_rows + j*row_stride, each row ceil(n_fam/4) bytes, selected SNPs in analysis order.
+ * keep_idx: host pointer to n indices into [0, n_fam) of the individuals kept, in order
+ *   (NULL = all n_fam individuals; then n must equal n_fam).
+ * Codes follow PLINK: 00→0, 10(het)→1, 11→2, 01(missing)→1 allele-2 copies, exactly like the
+ * reference's bit decode (missing counts as one copy).  The handle keeps two packed 2-bit
+ * copies (SNP-major and individual-major) in HBM.  flags: reserved, pass 0. */
+int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
+                              int64_t row_stride, const int64_t* keep_idx, int64_t n,
+                              int flags, slemm_geno** out);
+int slemm_gpu_genotype_destroy(slemm_geno* g);
+int slemm_gpu_genotype_dims(const slemm_geno* g, int64_t* n, int64_t* m);
+/* Binds the handle's work to a caller stream (cudaStream_t passed as void*; NULL = own stream). */
+int slemm_gpu_set_stream(slemm_geno* g, void* stream);
+int slemm_gpu_get_stream(const slemm_geno* g, void** stream);
+
+/* Bit-exact integer side outputs (host pointers, length m each, may be NULL):
+ * popcnt = Σ_i count_ji (src/reml.cpp:613-621 nz_bits); n0/n1/n2 = genotype classes with
+ * missing counted as a heterozygote (src/input.cpp:10-22). */
+int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32_t* n1,
+                              int32_t* n2);
+
+/* gm (m), w (m), rr (n) — host pointers.  gm is the per-SNP mean count, w the per-SNP
+ * weight (gw in the reference, src/reml.cpp:622), rr = R^{-1/2} (NULL = all ones). */
+int slemm_gpu_set_weights(slemm_geno* g, const float* gm, const float* w, const float* rr);
+/* Q: host n×c column-major orthonormal basis of R^{-1/2}X (src/reml.cpp:583-585). c may be 0. */
+int slemm_gpu_set_projection(slemm_geno* g, const float* Q, int64_t ldq, int c);
+int slemm_gpu_set_precision(slemm_geno* g, int prec);
+/* per_vector != 0 makes every operator run one column at a time (the plain per-vector path). */
+int slemm_gpu_set_per_vector(slemm_geno* g, int per_vector);
+
+/* One operator application (src/reml.cpp:8-233).  `in` is n×k (QUADFORM, LDET, RMATVEC,
+ * WRMATVEC) or m×k (MATVEC); `out` is n×k or m×k accordingly.  mem = SLEMM_MEM_HOST or
+ * SLEMM_MEM_DEVICE for both pointers.  Host calls copy in, run, copy out and synchronise. */
+int slemm_gpu_op(slemm_geno* g, int op_kind, float tau0, const float* in, int64_t ld_in, int k,
+                 float* out, int64_t ld_out, int mem);
+
+/* ---- Lanczos seed / shifted solves (src/reml.cpp:246-431) ------------------------------- */
+/* Runs the per-column Lanczos/CG recurrence on B (n×t) with operator op_kind (QUADFORM or LDET)
+ * at shift tau0 until max_col |ρ|·‖u‖/‖b‖ ≤ tol or maxit, storing the basis in HBM.  The
+ * recurrence scalars are accumulated in FP64.  *iters receives the number of steps j. */
+int slemm_gpu_lanczos_seed(slemm_geno* g, int op_kind, float tau0, const float* B, int64_t ldb,
+                           int t, float tol, int maxit, int mem, slemm_lseed** out, int* iters);
+int slemm_gpu_lseed_destroy(slemm_lseed* s);
+/* Jacobi coefficients: beta is t×(iters+1), delta is t×iters, column-major, host FP64. */
+int slemm_gpu_lseed_coeffs(const slemm_lseed* s, double* beta, double* delta);
+/* X = (A + sigma I)^{-1} B via the stored basis (L_Solve, src/reml.cpp:369-431), CG stopped at
+ * relative residual tol.  B must be the seed's right-hand side block. */
+int slemm_gpu_lanczos_solve(slemm_lseed* s, float sigma, float tol, float* X, int64_t ldx,
+                            int mem);
+
+/* ---- batched tridiagonal eigensolve + SLQ (src/reml.cpp:440-451, 638-646) -------------- */
+/* For t Jacobi matrices (diag delta t×nld, off-diag beta t×(nld+1) with beta[:,1:nld] used),
+ * returns eigenvalues D (t×nld) and squared first eigenvector components W2 (t×nld), FP64,
+ * computed on the GPU (one implicit-QL solve per probe). Host pointers, column-major. */
+int slemm_gpu_tridiag_eig(const double* delta, const double* beta, int t, int nld, double* D,
+                          double* W2);
+
+/* ---- REML drivers ----------------------------------------------------------------------------- */
+typedef struct {
+  int   n_V;        /* Rademacher probes (SLDF) or MC samples n_MC (LMC)                 */
+  int   seed;       /* --seed                                                             */
+  float tol_L;      /* --rel_tol (Lanczos relative tolerance)                              */
+  float s2max;      /* --max_heritability                                                  */
+  float s2min;      /* 1e-4 in the reference                                               */
+  float tol_VC;     /* 1e-4 in the reference (golden-section tolerance on h2)              */
+  int   maxit;      /* 600 in the reference                                                */
+  int   verbose;    /* print the reference's progress lines to stdout                      */
+} slemm_reml_opts;
+
+typedef struct {
+  float vg, ve, h2, lrt;  /* variance components, h2 = vg/(vg+ve), LRT (SLDF only, else 0) */
+  int   iters_y, iters_Q, iters_V;   /* Lanczos steps per seed system                     */
+  int   n_criterion;      /* REML criterion (or first-order function) evaluations          */
+  double seconds;         /* wall time inside the call                                     */
+} slemm_reml_result;
+
+/* DF-REML with Rademacher probes + golden-section search (src/reml.cpp:549-690).
+ * Host pointers: rvec (n; NULL = ones), X (n×c col-major, ldx), y (n), persnp (m, already
+ * normalised to mean 1 by the caller as option.cpp:424 does).  Outputs (host): Py (n),
+ * snp_blup (m), blue (c), var_blue (c×c, may be NULL). */
+int slemm_gpu_reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
+                        const float* y, const float* persnp, const slemm_reml_opts* opts,
+                        float* Py, float* snp_blup, float* blue, float* var_blue,
+                        slemm_reml_result* res);
+/* MC-REML with secant iterations (src/reml.cpp:730-883), same argument conventions. */
+int slemm_gpu_reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
+                       const float* y, const float* persnp, const slemm_reml_opts* opts,
+                       float* Py, float* snp_blup, float* blue, slemm_reml_result* res);
+
+/* ---- prediction and GWAS score statistics ------------------------------------------------- */
+/* GEBV: tgv_i = Σ_j (flip_j ? 2−count_ij : count_ij)·alpha_j, FP64 accumulation of exact
+ * integer counts (src/pred.cpp:112-130).  Uses the handle's genotypes (no centring). flip: m
+ * bytes or NULL.  Host pointers. */
+int slemm_gpu_gebv(slemm_geno* g, const double* alpha, const uint8_t* flip, double* tgv);
+/* GRAMMAR-Gamma per-SNP terms (bin/slemm_gamma.py:302-325), counting allele 1 like pgenlib:
+ * x = 2 − count.  For every SNP j: s_j = Σx; if s_j ≤ mac or 2n − s_j ≤ mac → NaN; else
+ * xy_j = (x − s/n)·y and xx_j = ‖(I−QQᵀ)(rr∘(x − s/n))‖².  y is n (host).  Projection and rr
+ * come from the handle.  Outputs xy, xx (m, host). */
+int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, float* xx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLEMM_GPU_H_ */

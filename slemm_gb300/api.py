@@ -1,0 +1,258 @@
+"""Host-side mirror of the reference's operator interface over the C ABI.
+
+Names follow the reference (src/reml.cpp): ``H0_quadform_mv``, ``H0_ldet_mv``, ``matvec``,
+``rmatvec``, ``weighted_rmatvec``, ``L_Seed``, ``L_Solve``, ``SLDF_REML``, ``LMC_REML``.
+Matrices are NumPy arrays (host; copied through the library) or CUDA tensors (device;
+column-major n×k stored as a contiguous (k, n) tensor).  Errors raise ``SlemmError`` carrying
+the library's status code — the reference instead exits or throws a C string.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (MEM_DEVICE, MEM_HOST, OP_LDET, OP_MATVEC, OP_QUADFORM, OP_RMATVEC,
+                   OP_WRMATVEC, RemlOpts, RemlResult, check)
+
+_OP_OF_NAME = {"quadform": OP_QUADFORM, "ldet": OP_LDET}
+
+
+def _f32c(a, rows=None):
+    """Column-major FP32 copy (Fortran order) of a host matrix/vector; returns (array, k)."""
+    a = np.asarray(a, dtype=np.float32)
+    if a.ndim == 1:
+        a = a[:, None]
+    return np.asfortranarray(a), a.shape[1]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def init(device: int = 0):
+    check(_lib.load().slemm_gpu_init(device))
+
+
+def launch_count() -> int:
+    return int(_lib.load().slemm_gpu_launch_count())
+
+
+class Genotypes:
+    """Packed genotypes resident in HBM (replaces the reference's kmat, src/option.cpp:347).
+
+    bed_rows: m×ceil(n_fam/4) uint8 .bed rows (SNP-major, magic skipped) of the analysed SNPs in
+    analysis order; keep_idx: indices of kept individuals in .fam order (None = all)."""
+
+    def __init__(self, bed_rows, n_fam: int, keep_idx=None):
+        self._lib = _lib.load()
+        rows = np.ascontiguousarray(bed_rows, dtype=np.uint8)
+        m, rb = rows.shape
+        keep = None if keep_idx is None else np.ascontiguousarray(keep_idx, dtype=np.int64)
+        n = n_fam if keep is None else keep.size
+        h = ctypes.c_void_p()
+        check(self._lib.slemm_gpu_genotype_create(_ptr(rows), n_fam, m, rb, _ptr(keep), n, 0,
+                                                  ctypes.byref(h)))
+        self.h = h
+        self.n, self.m = int(n), int(m)
+
+    def close(self):
+        if getattr(self, "h", None):
+            check(self._lib.slemm_gpu_genotype_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- integer side outputs -------------------------------------------------------------
+    def counts(self):
+        """(popcnt int64, n0, n1, n2 int32) per SNP — bit-exact integer work."""
+        pc = np.zeros(self.m, np.int64)
+        n0 = np.zeros(self.m, np.int32)
+        n1 = np.zeros(self.m, np.int32)
+        n2 = np.zeros(self.m, np.int32)
+        check(self._lib.slemm_gpu_genotype_counts(self.h, _ptr(pc), _ptr(n0), _ptr(n1), _ptr(n2)))
+        return pc, n0, n1, n2
+
+    # ---- configuration -----------------------------------------------------------------------
+    def set_weights(self, gm, w, rr=None):
+        gm = np.ascontiguousarray(gm, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        rr = None if rr is None else np.ascontiguousarray(rr, np.float32)
+        check(self._lib.slemm_gpu_set_weights(self.h, _ptr(gm), _ptr(w), _ptr(rr)))
+
+    def set_projection(self, Q):
+        if Q is None or np.asarray(Q).size == 0:
+            check(self._lib.slemm_gpu_set_projection(self.h, None, self.n, 0))
+            return
+        Qf, c = _f32c(Q)
+        check(self._lib.slemm_gpu_set_projection(self.h, _ptr(Qf), self.n, c))
+
+    def set_precision(self, prec: int):
+        check(self._lib.slemm_gpu_set_precision(self.h, prec))
+
+    def set_per_vector(self, flag: bool):
+        check(self._lib.slemm_gpu_set_per_vector(self.h, 1 if flag else 0))
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self._lib.slemm_gpu_set_stream(self.h, stream_ptr))
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        check(self._lib.slemm_gpu_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    # ---- operators (src/reml.cpp:8-233) -----------------------------------------------------------
+    def op(self, kind: int, v, tau0: float = 0.0):
+        """Host call: NumPy in, NumPy out (column-major semantics, shape rows×k)."""
+        vin, k = _f32c(v)
+        rows_out = self.m if kind in (OP_RMATVEC, OP_WRMATVEC) else self.n
+        out = np.zeros((rows_out, k), np.float32, order="F")
+        check(self._lib.slemm_gpu_op(self.h, kind, float(tau0), _ptr(vin), vin.shape[0], k,
+                                     _ptr(out), rows_out, MEM_HOST))
+        return out
+
+    def op_device(self, kind: int, v_t, out_t, tau0: float = 0.0):
+        """Device call on CUDA tensors stored as (k, rows) contiguous (column-major rows×k)."""
+        k, rows_in = v_t.shape
+        rows_out = out_t.shape[1]
+        check(self._lib.slemm_gpu_op(self.h, kind, float(tau0), ctypes.c_void_p(v_t.data_ptr()),
+                                     rows_in, k, ctypes.c_void_p(out_t.data_ptr()), rows_out,
+                                     MEM_DEVICE))
+
+    def H0_quadform_mv(self, tau0, v):
+        return self.op(OP_QUADFORM, v, tau0)
+
+    def H0_ldet_mv(self, tau0, v):
+        return self.op(OP_LDET, v, tau0)
+
+    def lnr_op_select(self, lnr: str, tau0, v):
+        if lnr not in _OP_OF_NAME:
+            raise ValueError("Unknown linear operator in lnr_op_select()")
+        return self.op(_OP_OF_NAME[lnr], v, tau0)
+
+    def matvec(self, v):
+        return self.op(OP_MATVEC, v)
+
+    def rmatvec(self, v):
+        return self.op(OP_RMATVEC, v)
+
+    def weighted_rmatvec(self, v):
+        return self.op(OP_WRMATVEC, v)
+
+    # ---- Lanczos (src/reml.cpp:246-431) ------------------------------------------------------------
+    def L_Seed(self, lnr: str, tau0, B, tol=5e-4, maxit=600):
+        Bf, t = _f32c(B)
+        s = ctypes.c_void_p()
+        it = ctypes.c_int()
+        check(self._lib.slemm_gpu_lanczos_seed(self.h, _OP_OF_NAME[lnr], float(tau0), _ptr(Bf),
+                                               Bf.shape[0], t, float(tol), int(maxit), MEM_HOST,
+                                               ctypes.byref(s), ctypes.byref(it)))
+        return LSeed(self, s, t, it.value)
+
+    # ---- drivers ------------------------------------------------------------------------------------
+    def _reml_args(self, rvec, X, y, persnp):
+        n = self.n
+        rv = None if rvec is None else np.ascontiguousarray(rvec, np.float32)
+        Xf, c = _f32c(X)
+        yv = np.ascontiguousarray(y, np.float32)
+        ps = np.ascontiguousarray(persnp, np.float32)
+        assert yv.size == n and Xf.shape[0] == n and ps.size == self.m
+        return rv, Xf, c, yv, ps
+
+    def SLDF_REML(self, rvec, X, y, persnp, seed=0, n_V=30, tol_L=5e-4, s2max=0.7, s2min=1e-4,
+                  tol_VC=1e-4, maxit=600, verbose=False):
+        rv, Xf, c, yv, ps = self._reml_args(rvec, X, y, persnp)
+        o = RemlOpts(n_V, seed, tol_L, s2max, s2min, tol_VC, maxit, int(verbose))
+        Py = np.zeros(self.n, np.float32)
+        b = np.zeros(self.m, np.float32)
+        blue = np.zeros(c, np.float32)
+        vb = np.zeros((c, c), np.float32, order="F")
+        r = RemlResult()
+        check(self._lib.slemm_gpu_reml_sldf(self.h, _ptr(rv), _ptr(Xf), self.n, c, _ptr(yv),
+                                            _ptr(ps), ctypes.byref(o), _ptr(Py), _ptr(b),
+                                            _ptr(blue), _ptr(vb), ctypes.byref(r)))
+        return dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue,
+                    var_blue=vb, iters=(r.iters_y, r.iters_Q, r.iters_V),
+                    n_criterion=r.n_criterion, seconds=r.seconds)
+
+    def LMC_REML(self, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, s2min=1e-4,
+                 maxit=600, verbose=False):
+        rv, Xf, c, yv, ps = self._reml_args(rvec, X, y, persnp)
+        o = RemlOpts(n_MC, seed, tol_L, s2max, s2min, 1e-4, maxit, int(verbose))
+        Py = np.zeros(self.n, np.float32)
+        b = np.zeros(self.m, np.float32)
+        blue = np.zeros(c, np.float32)
+        r = RemlResult()
+        check(self._lib.slemm_gpu_reml_lmc(self.h, _ptr(rv), _ptr(Xf), self.n, c, _ptr(yv),
+                                           _ptr(ps), ctypes.byref(o), _ptr(Py), _ptr(b),
+                                           _ptr(blue), ctypes.byref(r)))
+        return dict(vg=r.vg, ve=r.ve, h2=r.h2, Py=Py, snp_blup=b, blue=blue, iters=r.iters_V,
+                    n_criterion=r.n_criterion, seconds=r.seconds)
+
+    def gebv(self, alpha, flip=None):
+        """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""
+        a = np.ascontiguousarray(alpha, np.float64)
+        f = None if flip is None else np.ascontiguousarray(flip, np.uint8)
+        out = np.zeros(self.n, np.float64)
+        check(self._lib.slemm_gpu_gebv(self.h, _ptr(a), _ptr(f), _ptr(out)))
+        return out
+
+    def score_terms(self, y, mac: int):
+        """slemm_gamma per-variant xy and xx (bin/slemm_gamma.py:302-319)."""
+        yv = np.ascontiguousarray(y, np.float32)
+        xy = np.zeros(self.m, np.float32)
+        xx = np.zeros(self.m, np.float32)
+        check(self._lib.slemm_gpu_score_terms(self.h, _ptr(yv), int(mac), _ptr(xy), _ptr(xx)))
+        return xy, xx
+
+
+class LSeed:
+    """A seed system resident on the GPU (basis + Jacobi coefficients)."""
+
+    def __init__(self, geno: Genotypes, handle, t: int, iters: int):
+        self.g, self.s, self.t, self.iters = geno, handle, t, iters
+
+    def coeffs(self):
+        beta = np.zeros((self.t, self.iters + 1), np.float64, order="F")
+        delta = np.zeros((self.t, max(self.iters, 1)), np.float64, order="F")
+        check(self.g._lib.slemm_gpu_lseed_coeffs(self.s, _ptr(beta), _ptr(delta)))
+        return beta, delta[:, : self.iters]
+
+    def L_Solve(self, sigma, tol=1e-6):
+        X = np.zeros((self.g.n, self.t), np.float32, order="F")
+        check(self.g._lib.slemm_gpu_lanczos_solve(self.s, float(sigma), float(tol), _ptr(X),
+                                                  self.g.n, MEM_HOST))
+        return X
+
+    def close(self):
+        if getattr(self, "s", None):
+            check(self.g._lib.slemm_gpu_lseed_destroy(self.s))
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tridiag_eig(delta, beta):
+    """Batched FP64 eigenvalues D and squared first components W² (src/reml.cpp:638-646)."""
+    delta = np.asfortranarray(delta, np.float64)
+    beta = np.asfortranarray(beta, np.float64)
+    t, nld = delta.shape
+    D = np.zeros((t, nld), np.float64, order="F")
+    W2 = np.zeros((t, nld), np.float64, order="F")
+    check(_lib.load().slemm_gpu_tridiag_eig(_ptr(delta), _ptr(beta), t, nld, _ptr(D), _ptr(W2)))
+    return D, W2

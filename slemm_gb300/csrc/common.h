@@ -1,0 +1,135 @@
+// common.h — shared internals of libslemm_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <atomic>
+
+#include "../../include/slemm_gpu.h"
+
+namespace slemm {
+
+// ---- errors --------------------------------------------------------------------------------
+void set_error(const std::string& msg);
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define SLEMM_THROW(code_, msg_)                                      \
+  do {                                                                \
+    throw ::slemm::Error{(code_), std::string(__func__) + ": " + (msg_)}; \
+  } while (0)
+
+#define CUDA_TRY(expr)                                                              \
+  do {                                                                              \
+    cudaError_t e__ = (expr);                                                       \
+    if (e__ != cudaSuccess)                                                         \
+      throw ::slemm::Error{SLEMM_ERR_CUDA, std::string(#expr) + " -> " +            \
+                                               cudaGetErrorString(e__)};           \
+  } while (0)
+
+#define CHECK_ARG(cond, msg_) \
+  do {                        \
+    if (!(cond)) SLEMM_THROW(SLEMM_ERR_ARG, msg_); \
+  } while (0)
+
+// Wraps a C-ABI body: maps exceptions to status codes and the thread-local message.
+template <class F>
+int guarded(F&& f)
+{
+  try {
+    f();
+    return SLEMM_OK;
+  } catch (const Error& e) {
+    set_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return SLEMM_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return SLEMM_ERR_STATE;
+  }
+}
+
+// ---- launch accounting -----------------------------------------------------------------------
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+// Checks the launch just issued.
+#define LAUNCH_CHECK()                                   \
+  do {                                                   \
+    ::slemm::count_launch();                             \
+    CUDA_TRY(cudaGetLastError());                        \
+  } while (0)
+
+// ---- sizes -----------------------------------------------------------------------------------
+constexpr int kTileM = 128;          // rows of one packed tile (M of one MMA)
+constexpr int kTileK = 64;           // K elements of one packed tile (one 128-B bf16 row)
+constexpr int kTileBytes = kTileM * kTileK / 4;   // 2048 packed bytes per tile
+__host__ __device__ inline int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+__host__ __device__ inline int64_t ceil_div(int64_t x, int64_t a) { return (x + a - 1) / a; }
+
+// ---- device buffer -----------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release()
+  {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // Grows (never shrinks); contents are not preserved.
+  void* ensure(size_t nbytes)
+  {
+    if (nbytes <= bytes) return p;
+    release();
+    if (nbytes == 0) return nullptr;
+    cudaError_t e = cudaMalloc(&p, nbytes);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error{SLEMM_ERR_NOMEM, "cudaMalloc(" + std::to_string(nbytes) + ") -> " +
+                                       cudaGetErrorString(e)};
+    }
+    bytes = nbytes;
+    return p;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// ---- packed product plan ------------------------------------------------------------------------
+// D[M_pad × N] = Cnt[M_pad × K_pad] · B where the count matrix is a tiled 2-bit packed array
+// (tiles of kTileM rows × kTileK K-elements, 2048 contiguous bytes each, see geno.cu) and B is
+// either FP32 [k][K_pad] (SIMT) or BF16 [N][K_pad] (tensor cores).  The raw product goes to
+// partials [splits][N][M_pad] (FP32), reduced by the finalize kernels of ops.cu.
+struct GemmArgs {
+  const uint8_t* A;     // tiled packed counts
+  int64_t M_pad;        // rows (multiple of 128)
+  int64_t K_pad;        // K elements (multiple of 128)
+  const void* B;        // dense side
+  int N;                // columns of D (k for SIMT, padded pieces*k for TC)
+  float* D;             // partials
+  int splits;           // split-K factor
+  int* err;             // device error word (bounded waits that gave up set bits here)
+};
+
+void gemm_simt(const GemmArgs& a, cudaStream_t st);
+// Tensor-core path (tcgen05); N must be a multiple of 16 in [16, 256].
+void gemm_tc(const GemmArgs& a, cudaStream_t st);
+int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int num_sms);
+int num_sms();
+
+}  // namespace slemm

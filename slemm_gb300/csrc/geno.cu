@@ -1,0 +1,404 @@
+// geno.cu — library state, the packed genotype handle and its bit-exact integer kernels.
+//
+// Device layout of the counts.  The reference keeps genotypes as m rows of 2n bits
+// (std::vector<std::vector<bool>>, src/option.cpp:347) decoded byte by byte from the .bed
+// (src/input.cpp:343-386).  Here each allele-2 count x ∈ {0,1,2} is stored as two bits
+// (nz = [x≠0], hi = [x==2]) in a tiled layout:
+//   tile (mt, kt) = 128 rows × 64 K-elements = 2048 contiguous bytes at
+//   ((mt·K_tiles + kt)·128 + r)·16; the 16 bytes of row r hold K-elements kt·64 … kt·64+63 as
+//   four 32-bit words, word w covering elements 16w … 16w+15 with
+//     bits  0-7 : nz of the even elements 16w+2q (bit q)
+//     bits  8-15: hi of the even elements        (bit 8+q)
+//     bits 16-23: nz of the odd elements 16w+2q+1 (bit 16+q)
+//     bits 24-31: hi of the odd elements          (bit 24+q)
+// so that (word >> q) puts element pair q where one integer multiply-add turns it into a
+// BF16 pair (see decode.cuh).  Two copies are kept: G (rows = SNPs, K = individuals) and GT
+// (rows = individuals, K = SNPs), so both products read K-contiguous tiles with one 2048-byte
+// bulk copy per tile.  Padding rows/columns hold count 0.
+#include "internal.h"
+
+#include <cstring>
+#include <mutex>
+
+namespace slemm {
+
+std::atomic<int64_t> g_launches{0};
+static thread_local std::string t_last_error;
+void set_error(const std::string& msg) { t_last_error = msg; }
+
+int num_sms()
+{
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+// Picks the split-K factor so that M_tiles·splits CTAs fill whole waves, keeping at least
+// 16 K-tiles per split.
+int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int sms)
+{
+  const int64_t slots = (int64_t)ctas_per_sm * sms;
+  int best = 1;
+  double best_eff = -1.0;
+  for (int s = 1; s <= 16; ++s) {
+    if (s > 1 && K_tiles / s < 16) break;
+    const int64_t ctas = M_tiles * s;
+    const double waves = (double)ctas / slots;
+    const double eff = waves / std::ceil(waves) - 0.015 * (s - 1);   // partials cost per split
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = s;
+    }
+  }
+  return best;
+}
+
+// ---- pack kernels ------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned count_of(const uint8_t* __restrict__ row, int64_t f)
+{
+  const unsigned code = (row[f >> 2] >> (2 * (f & 3))) & 3u;
+  return (code & 1u) + (code >> 1);   // missing (01) → 1, exactly as the reference's b[k]+b[k+1]
+}
+
+__device__ __forceinline__ unsigned plane_bits(unsigned x, int e)
+{
+  // element e (0..15) of a word; x = count
+  const unsigned nz = x != 0u, hi = x == 2u;
+  const int q = e >> 1;
+  return (e & 1) ? ((nz << (16 + q)) | (hi << (24 + q))) : ((nz << q) | (hi << (8 + q)));
+}
+
+// G words: thread → (SNP row j, word wi along individuals).
+__global__ void pack_G_kernel(const uint8_t* __restrict__ raw, int64_t row_bytes, int64_t j0,
+                              int64_t rows_in_chunk, const int64_t* __restrict__ keep, int64_t n,
+                              int64_t K_tiles, uint32_t* __restrict__ G)
+{
+  const int64_t words_per_row = K_tiles * 4;   // 64 elements per tile row = 4 words
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t jl = gid / words_per_row;
+  const int64_t wi = gid % words_per_row;
+  if (jl >= rows_in_chunk) return;
+  const int64_t j = j0 + jl;
+  const uint8_t* row = raw + jl * row_bytes;
+  unsigned word = 0;
+#pragma unroll 4
+  for (int e = 0; e < 16; ++e) {
+    const int64_t i = wi * 16 + e;
+    if (i < n) word |= plane_bits(count_of(row, keep ? keep[i] : i), e);
+  }
+  const int64_t mt = j / 128, r = j % 128, kt = wi / 4, wr = wi % 4;
+  G[((mt * K_tiles + kt) * 128 + r) * 4 + wr] = word;
+}
+
+// GT words: thread → (individual row i, word wj along SNPs of this chunk).
+__global__ void pack_GT_kernel(const uint8_t* __restrict__ raw, int64_t row_bytes, int64_t j0,
+                               int64_t rows_in_chunk, int64_t m, const int64_t* __restrict__ keep,
+                               int64_t n, int64_t n_pad, int64_t K_tiles_T,
+                               uint32_t* __restrict__ GT)
+{
+  // chunk covers SNPs j0 .. j0+rows_in_chunk (j0 multiple of 128); words of 16 SNPs
+  const int64_t words_in_chunk = ceil_div(rows_in_chunk, 16);
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = gid % n_pad;
+  const int64_t wl = gid / n_pad;
+  if (wl >= words_in_chunk) return;
+  unsigned word = 0;
+  if (i < n) {
+    const int64_t f = keep ? keep[i] : i;
+#pragma unroll 4
+    for (int e = 0; e < 16; ++e) {
+      const int64_t jl = wl * 16 + e;
+      if (jl < rows_in_chunk && j0 + jl < m) word |= plane_bits(count_of(raw + jl * row_bytes, f), e);
+    }
+  }
+  const int64_t wj = j0 / 16 + wl;   // global word index along SNPs
+  const int64_t mt = i / 128, r = i % 128, kt = wj / 4, wr = wj % 4;
+  GT[((mt * K_tiles_T + kt) * 128 + r) * 4 + wr] = word;
+}
+
+// Per-row integer counts over the G copy: allele count, n1 (one nz bit, no hi), n2 (hi bits).
+__global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int64_t K_tiles,
+                                  int64_t* __restrict__ pc, int32_t* __restrict__ c1,
+                                  int32_t* __restrict__ c2)
+{
+  // one warp per SNP row
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= m) return;
+  const int64_t mt = warp / 128, r = warp % 128;
+  long long nz = 0, hi = 0;
+  for (int64_t wi = lane; wi < K_tiles * 4; wi += 32) {
+    const int64_t kt = wi / 4, wr = wi % 4;
+    const uint32_t w = G[((mt * K_tiles + kt) * 128 + r) * 4 + wr];
+    nz += __popc(w & 0x00FF00FFu);
+    hi += __popc(w & 0xFF00FF00u);
+  }
+  for (int o = 16; o; o >>= 1) {
+    nz += __shfl_xor_sync(0xffffffffu, nz, o);
+    hi += __shfl_xor_sync(0xffffffffu, hi, o);
+  }
+  if (lane == 0) {
+    pc[warp] = nz + hi;
+    c1[warp] = (int32_t)(nz - hi);
+    c2[warp] = (int32_t)hi;
+  }
+}
+
+}  // namespace slemm
+
+using namespace slemm;
+
+// =================================================================================================
+// C ABI
+// =================================================================================================
+extern "C" {
+
+const char* slemm_gpu_last_error(void) { return t_last_error.c_str(); }
+int slemm_gpu_version(void) { return 100; }   // 0.1.0
+int64_t slemm_gpu_launch_count(void) { return g_launches.load(); }
+
+int slemm_gpu_init(int device)
+{
+  return guarded([&] {
+    int cnt = 0;
+    CUDA_TRY(cudaGetDeviceCount(&cnt));
+    CHECK_ARG(device >= 0 && device < cnt, "device index out of range");
+    CUDA_TRY(cudaSetDevice(device));
+    cudaDeviceProp p;
+    CUDA_TRY(cudaGetDeviceProperties(&p, device));
+    if (!(p.major == 10 && p.minor == 3))
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "this build targets sm_103a; device is sm_" +
+                                             std::to_string(p.major) + std::to_string(p.minor));
+  });
+}
+
+int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
+                              int64_t row_stride, const int64_t* keep_idx, int64_t n, int flags,
+                              slemm_geno** out)
+{
+  return guarded([&] {
+    CHECK_ARG(out != nullptr, "out is null");
+    *out = nullptr;
+    CHECK_ARG(bed_rows != nullptr, "bed_rows is null");
+    CHECK_ARG(n_fam > 0 && m > 0 && n > 0, "empty genotype matrix");
+    const int64_t row_bytes = ceil_div(n_fam, 4);
+    CHECK_ARG(row_stride >= row_bytes, "row_stride < ceil(n_fam/4)");
+    if (!keep_idx) CHECK_ARG(n == n_fam, "keep_idx is null but n != n_fam");
+    CHECK_ARG(n <= n_fam, "n > n_fam");
+    CHECK_ARG(n < (int64_t)INT32_MAX && m < (int64_t)INT32_MAX, "dimension exceeds 2^31");
+    if (keep_idx)
+      for (int64_t i = 0; i < n; ++i)
+        CHECK_ARG(keep_idx[i] >= 0 && keep_idx[i] < n_fam, "keep_idx entry out of range");
+    (void)flags;
+
+    auto* g = new slemm_geno();
+    try {
+      CUDA_TRY(cudaGetDevice(&g->device));
+      CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      g->own_stream = true;
+      g->n = n;
+      g->m = m;
+      g->n_pad = round_up(n, kTileM);
+      g->m_pad = round_up(m, kTileM);
+      const int64_t Kt_G = g->n_pad / kTileK, Kt_GT = g->m_pad / kTileK;
+      const size_t bytes_G = (size_t)(g->m_pad / kTileM) * Kt_G * kTileBytes;
+      const size_t bytes_GT = (size_t)(g->n_pad / kTileM) * Kt_GT * kTileBytes;
+      g->G.ensure(bytes_G);
+      g->GT.ensure(bytes_GT);
+      g->err.ensure(sizeof(int));
+      CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));
+      CUDA_TRY(cudaMemsetAsync(g->G.p, 0, bytes_G, g->stream));
+      CUDA_TRY(cudaMemsetAsync(g->GT.p, 0, bytes_GT, g->stream));
+
+      DevBuf d_keep;
+      if (keep_idx) {
+        d_keep.ensure(n * sizeof(int64_t));
+        CUDA_TRY(cudaMemcpyAsync(d_keep.p, keep_idx, n * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                 g->stream));
+      }
+      // stream SNP chunks of 4096 rows (multiple of 128) through a device staging buffer
+      const int64_t chunk = 4096;
+      DevBuf d_raw;
+      d_raw.ensure((size_t)chunk * row_bytes);
+      for (int64_t j0 = 0; j0 < m; j0 += chunk) {
+        const int64_t rows = std::min(chunk, m - j0);
+        if (row_stride == row_bytes) {
+          CUDA_TRY(cudaMemcpyAsync(d_raw.p, bed_rows + j0 * row_stride, rows * row_bytes,
+                                   cudaMemcpyHostToDevice, g->stream));
+        } else {
+          CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride,
+                                     row_bytes, rows, cudaMemcpyHostToDevice, g->stream));
+        }
+        {
+          const int64_t total = rows * (Kt_G * 4);
+          const int th = 256;
+          pack_G_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
+              d_raw.as<uint8_t>(), row_bytes, j0, rows, d_keep.as<int64_t>(), n, Kt_G,
+              g->G.as<uint32_t>());
+          LAUNCH_CHECK();
+        }
+        {
+          const int64_t total = ceil_div(rows, 16) * g->n_pad;
+          const int th = 256;
+          pack_GT_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
+              d_raw.as<uint8_t>(), row_bytes, j0, rows, m, d_keep.as<int64_t>(), n, g->n_pad,
+              Kt_GT, g->GT.as<uint32_t>());
+          LAUNCH_CHECK();
+        }
+      }
+      CUDA_TRY(cudaStreamSynchronize(g->stream));
+    } catch (...) {
+      if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+      delete g;
+      throw;
+    }
+    *out = g;
+  });
+}
+
+int slemm_gpu_genotype_destroy(slemm_geno* g)
+{
+  return guarded([&] {
+    if (!g) return;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+  });
+}
+
+int slemm_gpu_genotype_dims(const slemm_geno* g, int64_t* n, int64_t* m)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+  });
+}
+
+int slemm_gpu_set_stream(slemm_geno* g, void* stream)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    if (g->own_stream) cudaStreamDestroy(g->stream);
+    if (stream) {
+      g->stream = (cudaStream_t)stream;
+      g->own_stream = false;
+    } else {
+      CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      g->own_stream = true;
+    }
+  });
+}
+
+int slemm_gpu_get_stream(const slemm_geno* g, void** stream)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr && stream != nullptr, "null argument");
+    *stream = (void*)g->stream;
+  });
+}
+
+int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32_t* n1,
+                              int32_t* n2)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    DevBuf d_pc, d_c1, d_c2;
+    d_pc.ensure(g->m * sizeof(int64_t));
+    d_c1.ensure(g->m * sizeof(int32_t));
+    d_c2.ensure(g->m * sizeof(int32_t));
+    const int th = 256;
+    const int64_t warps = g->m;
+    row_counts_kernel<<<(unsigned)ceil_div(warps * 32, th), th, 0, g->stream>>>(
+        g->G.as<uint32_t>(), g->m, g->n_pad / kTileK, d_pc.as<int64_t>(), d_c1.as<int32_t>(),
+        d_c2.as<int32_t>());
+    LAUNCH_CHECK();
+    std::vector<int64_t> pc(g->m);
+    std::vector<int32_t> c1(g->m), c2(g->m);
+    CUDA_TRY(cudaMemcpyAsync(pc.data(), d_pc.p, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                             g->stream));
+    CUDA_TRY(cudaMemcpyAsync(c1.data(), d_c1.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             g->stream));
+    CUDA_TRY(cudaMemcpyAsync(c2.data(), d_c2.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    for (int64_t j = 0; j < g->m; ++j) {
+      if (popcnt) popcnt[j] = pc[j];
+      if (n1) n1[j] = c1[j];
+      if (n2) n2[j] = c2[j];
+      if (n0) n0[j] = (int32_t)(g->n - c1[j] - c2[j]);
+    }
+  });
+}
+
+int slemm_gpu_set_weights(slemm_geno* g, const float* gm, const float* w, const float* rr)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr && gm != nullptr && w != nullptr, "null argument");
+    std::vector<float> hgm(g->m_pad, 0.f), hw(g->m_pad, 0.f), hrr(g->n_pad, 0.f);
+    for (int64_t j = 0; j < g->m; ++j) {
+      CHECK_ARG(std::isfinite(gm[j]) && std::isfinite(w[j]), "non-finite gm or w");
+      hgm[j] = gm[j];
+      hw[j] = w[j];
+    }
+    for (int64_t i = 0; i < g->n; ++i) {
+      hrr[i] = rr ? rr[i] : 1.0f;
+      CHECK_ARG(std::isfinite(hrr[i]), "non-finite rr");
+    }
+    g->gm.ensure(g->m_pad * sizeof(float));
+    g->w.ensure(g->m_pad * sizeof(float));
+    g->rr.ensure(g->n_pad * sizeof(float));
+    CUDA_TRY(cudaMemcpyAsync(g->gm.p, hgm.data(), g->m_pad * sizeof(float), cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaMemcpyAsync(g->w.p, hw.data(), g->m_pad * sizeof(float), cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaMemcpyAsync(g->rr.p, hrr.data(), g->n_pad * sizeof(float), cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    g->weights_set = true;
+  });
+}
+
+int slemm_gpu_set_projection(slemm_geno* g, const float* Q, int64_t ldq, int c)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    CHECK_ARG(c >= 0 && c <= 64, "projection rank must be in [0, 64]");
+    g->c = c;
+    if (c == 0) return;
+    CHECK_ARG(Q != nullptr && ldq >= g->n, "bad Q");
+    std::vector<float> hq((size_t)g->n_pad * c, 0.f);
+    for (int l = 0; l < c; ++l)
+      for (int64_t i = 0; i < g->n; ++i) hq[(size_t)l * g->n_pad + i] = Q[(size_t)l * ldq + i];
+    g->Q.ensure(hq.size() * sizeof(float));
+    CUDA_TRY(cudaMemcpyAsync(g->Q.p, hq.data(), hq.size() * sizeof(float), cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+  });
+}
+
+int slemm_gpu_set_precision(slemm_geno* g, int prec)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    CHECK_ARG(prec == SLEMM_PREC_FP32 || prec == SLEMM_PREC_BF16X2 || prec == SLEMM_PREC_BF16X3,
+              "unknown precision");
+    g->prec = prec;
+  });
+}
+
+int slemm_gpu_set_per_vector(slemm_geno* g, int per_vector)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    g->per_vector = per_vector ? 1 : 0;
+  });
+}
+
+}  // extern "C"

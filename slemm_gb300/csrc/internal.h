@@ -1,0 +1,61 @@
+// internal.h — handle layout and internal entry points shared by the translation units.
+#pragma once
+
+#include "common.h"
+
+struct slemm_geno {
+  int device = 0;
+  int64_t n = 0, m = 0;           // kept individuals, SNPs
+  int64_t n_pad = 0, m_pad = 0;   // padded to kTileM
+  // Two tiled 2-bit copies of the count matrix (layout in geno.cu):
+  //   G : M = SNPs (m_pad rows),        K = individuals (n_pad)  → Z_cᵀU direction
+  //   GT: M = individuals (n_pad rows), K = SNPs (m_pad)         → Z_c V direction
+  slemm::DevBuf G, GT;
+  slemm::DevBuf gm, w, rr;        // FP32, padded with zeros (rr padded with 0)
+  slemm::DevBuf Q;                // n_pad × c column-major, zero padded rows
+  int c = 0;
+  bool weights_set = false;
+  int prec = SLEMM_PREC_BF16X2;
+  int per_vector = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // work buffers
+  slemm::DevBuf ws_B, ws_D, ws_red, ws_small, ws_T, ws_in, ws_out;
+  slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
+};
+
+namespace slemm {
+
+// ops.cu — one operator application on device buffers (column-major, ld given).
+void op_device(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
+               float* out, int64_t ld_out);
+
+// Column reductions with FP64 accumulation, deterministic two-stage (ops.cu).
+// dots[c] = Σ_i a[i,c]·b[i,c] over i < n for c < k (b == nullptr → Σ a²).  Result on device.
+void col_dots(slemm_geno* g, const float* a, int64_t lda, const float* b, int64_t ldb,
+              int64_t n, int k, double* d_out);
+// QtX[l,c] = Σ_i Q[i,l]·X[i,c], double c×k on device.
+void proj_coeffs(slemm_geno* g, const float* X, int64_t ldx, int k, double* d_QtX);
+// X[:,c] -= Σ_l Q[:,l] QtX[l,c].
+void proj_apply(slemm_geno* g, float* X, int64_t ldx, int k, const double* d_QtX);
+
+// lanczos.cu — seed on a device RHS block (n×t, ld = n); `groups` splits the columns into
+// groups with their own stopping rule (empty = one group).
+slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const float* dB, int t,
+                                 float tol, int maxit, bool verbose, std::vector<int> groups,
+                                 int p_freq);
+// Solve for the columns of group `grp`; X has that group's columns (ld = ldx) on device.
+int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp);
+void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2);
+// Accessors of the seed object (defined in lanczos.cu).
+int lseed_iters(const slemm_lseed* S, int grp);
+const double* lseed_delta(const slemm_lseed* S);   // iters × t (row j = step j)
+const double* lseed_beta(const slemm_lseed* S);    // (iters+1) × t
+int lseed_t(const slemm_lseed* S);
+void lseed_free(slemm_lseed* S);
+
+int64_t workspace_bytes(const slemm_geno* g);
+// Reads (and clears) the device error word; throws if a kernel gave up a bounded wait.
+void check_device_error(slemm_geno* g);
+
+}  // namespace slemm

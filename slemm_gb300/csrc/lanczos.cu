@@ -1,0 +1,547 @@
+// lanczos.cu — Lanczos seed systems, shifted solves and the batched tridiagonal eigensolve.
+//
+// L_Seed (src/reml.cpp:246-339): per-column Lanczos on a block B (n×t) with the operator of
+// ops.cu.  The basis vectors are FP32 in HBM like the reference's std::vector<MatrixXf>; every
+// scalar of the three-term recurrence (δ = uᵀAu, β = ‖·‖, the CG coefficients γ, ω, ρ and the
+// residual test) is accumulated and kept in FP64.
+//
+// L_Solve (src/reml.cpp:369-431): the reference rebuilds CG on (A + σI) from the stored basis
+// step by step.  Unrolling its recurrences (P_0 = B, P_j = ρ_j U_j + ω_{j−1} P_{j−1},
+// X = Σ_j γ_j P_j) gives X = S_0·B + Σ_{i≥1} ρ_i S_i U_i with S_i = γ_i + ω_i S_{i+1}; the
+// host evaluates those FP64 coefficients with the reference's stopping rule and one kernel
+// forms the weighted sum over the stored basis — one pass instead of one pass per step.
+//
+// Tridiagonal eigensolve (src/reml.cpp:638-646): per probe, implicit QL with Wilkinson shifts in
+// FP64, one thread per probe, tracking only the first row of the eigenvector matrix (all the
+// quadrature needs).
+#include "internal.h"
+
+#include <chrono>
+
+struct slemm_lseed {
+  slemm_geno* g = nullptr;
+  int kind = 0;
+  float tau0 = 0.f;
+  int t = 0;
+  int iters = 0;   // j: basis holds U_0 … U_j
+  int64_t n = 0;
+  static constexpr int kChunk = 16;          // basis blocks per allocation
+  std::vector<slemm::DevBuf*> chunks;        // each holds kChunk blocks of n×t FP32
+  slemm::DevBuf B;                           // right-hand side block (n×t)
+  std::vector<double> beta;                  // (iters+1) × t, row j = step j
+  std::vector<double> delta;                 // iters × t
+  std::vector<double> unorm;                 // (iters+1) × t, ‖U_j‖ of the stored FP32 vectors
+  std::vector<double> bnorm;                 // t
+  // Column groups that share one stopping rule (the reference runs each group as its own
+  // L_Seed call); group_iters[g] is the step at which group g met the tolerance.
+  std::vector<int> group_start, group_iters;
+  ~slemm_lseed()
+  {
+    for (auto* c : chunks) delete c;
+  }
+  float* block(int j)
+  {
+    const int c = j / kChunk;
+    while ((int)chunks.size() <= c) {
+      auto* b = new slemm::DevBuf();
+      b->ensure((size_t)kChunk * n * t * sizeof(float));
+      chunks.push_back(b);
+    }
+    return chunks[c]->as<float>() + (size_t)(j % kChunk) * n * t;
+  }
+};
+
+namespace slemm {
+
+constexpr int kLzRows = 4096;
+
+__device__ __forceinline__ double lz_block_sum(double v, double* sh)
+{
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+  return r;
+}
+
+// tmp ← tmp − U_prev·β (β = nullptr at j = 0); red[c][blk] = Σ U_cur·tmp
+__global__ void lz_dot_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur,
+                              const float* __restrict__ Uprev, const double* __restrict__ beta,
+                              int64_t n, double* __restrict__ red, int nblk)
+{
+  __shared__ double sh[32];
+  const int c = blockIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
+  const double b = beta ? beta[c] : 0.0;
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const int64_t o = (int64_t)c * n + i;
+    double x = tmp[o];
+    if (Uprev) {
+      x -= (double)Uprev[o] * b;
+      tmp[o] = (float)x;
+      x = (double)(float)x;
+    }
+    acc += (double)Ucur[o] * x;
+  }
+  const double s = lz_block_sum(acc, sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
+// tmp ← tmp − U_cur·δ; red[c][blk] = Σ tmp²
+__global__ void lz_orth_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur,
+                               const double* __restrict__ delta, int64_t n,
+                               double* __restrict__ red, int nblk)
+{
+  __shared__ double sh[32];
+  const int c = blockIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
+  const double d = delta[c];
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const int64_t o = (int64_t)c * n + i;
+    const float x = (float)((double)tmp[o] - (double)Ucur[o] * d);
+    tmp[o] = x;
+    acc += (double)x * (double)x;
+  }
+  const double s = lz_block_sum(acc, sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
+// U_next ← src / scale (scale = sqrt(nrm2)); red[c][blk] = Σ U_next²
+__global__ void lz_scale_kernel(float* __restrict__ Unext, const float* __restrict__ src,
+                                const double* __restrict__ nrm2, int64_t n,
+                                double* __restrict__ red, int nblk)
+{
+  __shared__ double sh[32];
+  const int c = blockIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
+  const double inv = 1.0 / sqrt(nrm2[c]);
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const int64_t o = (int64_t)c * n + i;
+    const float x = (float)((double)src[o] * inv);
+    Unext[o] = x;
+    acc += (double)x * (double)x;
+  }
+  const double s = lz_block_sum(acc, sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
+__global__ void lz_reduce_kernel(const double* __restrict__ red, int nblk, int t,
+                                 double* __restrict__ out)
+{
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= t) return;
+  double s = 0.0;
+  for (int b = lane; b < nblk; b += 32) s += red[(int64_t)c * nblk + b];
+  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[c] = s;
+}
+
+// X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]   (FP64 accumulation)
+// (columns c0 … c0+tc−1 of the block; coef is steps × tc, X has tc columns)
+__global__ void lz_combine_kernel(float* __restrict__ X, int64_t ldx, const float* __restrict__ B,
+                                  const float* const* __restrict__ blocks, int J,
+                                  const double* __restrict__ coef, int64_t n, int c0, int tc)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i >= n) return;
+  const int64_t o = (int64_t)(c0 + c) * n + i;
+  double acc = coef[c] * (double)B[o];
+  for (int j = 1; j <= J; ++j) acc += coef[(int64_t)j * tc + c] * (double)blocks[j][o];
+  X[(int64_t)c * ldx + i] = (float)acc;
+}
+
+// Batched implicit QL on symmetric tridiagonal matrices, first eigenvector row only.
+// d: t×nld diagonals (column-major in t), e: t×nld off-diagonals e[0..nld−2] (e[nld−1] = 0).
+__global__ void tridiag_ql_kernel(double* __restrict__ d, double* __restrict__ e,
+                                  double* __restrict__ z, int t, int nld, int* __restrict__ fail)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= t) return;
+  auto D = [&](int i) -> double& { return d[(int64_t)i * t + p]; };
+  auto E = [&](int i) -> double& { return e[(int64_t)i * t + p]; };
+  auto Z = [&](int i) -> double& { return z[(int64_t)i * t + p]; };
+  for (int i = 0; i < nld; ++i) Z(i) = (i == 0) ? 1.0 : 0.0;
+  if (nld > 0) E(nld - 1) = 0.0;
+  const double eps = 2.220446049250313e-16;
+  for (int l = 0; l < nld; ++l) {
+    for (int iter = 0;; ++iter) {
+      int mm = l;
+      for (; mm < nld - 1; ++mm) {
+        const double dd = fabs(D(mm)) + fabs(D(mm + 1));
+        if (fabs(E(mm)) <= eps * dd) break;
+      }
+      if (mm == l) break;
+      if (iter >= 64) {
+        atomicOr(fail, 1);
+        break;
+      }
+      // Wilkinson-type shift from the leading 2×2 block
+      double g = (D(l + 1) - D(l)) / (2.0 * E(l));
+      double r = hypot(g, 1.0);
+      g = D(mm) - D(l) + E(l) / (g + (g >= 0 ? r : -r));
+      double s = 1.0, c = 1.0, pp = 0.0;
+      int i = mm - 1;
+      bool deflated = false;
+      for (; i >= l; --i) {
+        const double f = s * E(i), b = c * E(i);
+        r = hypot(f, g);
+        E(i + 1) = r;
+        if (r == 0.0) {
+          D(i + 1) -= pp;
+          E(mm) = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = D(i + 1) - pp;
+        r = (D(i) - g) * s + 2.0 * c * b;
+        pp = s * r;
+        D(i + 1) = g + pp;
+        g = c * r - b;
+        const double zf = Z(i + 1);
+        Z(i + 1) = s * Z(i) + c * zf;
+        Z(i) = c * Z(i) - s * zf;
+      }
+      if (deflated) continue;
+      D(l) -= pp;
+      E(l) = g;
+      E(mm) = 0.0;
+    }
+  }
+}
+
+static void lz_reduce(const double* red, int nblk, int t, double* out, cudaStream_t st)
+{
+  lz_reduce_kernel<<<(unsigned)ceil_div(t, 8), 256, 0, st>>>(red, nblk, t, out);
+  LAUNCH_CHECK();
+}
+
+}  // namespace slemm
+
+using namespace slemm;
+
+namespace slemm {
+
+// Runs L_Seed on a device RHS block B (n×t, ld = n).  Returns the seed object.
+slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const float* dB, int t,
+                                 float tol, int maxit, bool verbose, std::vector<int> groups,
+                                 int p_freq)
+{
+  if (groups.empty()) groups.push_back(t);
+  {
+    int tot = 0;
+    for (int x : groups) {
+      CHECK_ARG(x >= 1, "empty column group");
+      tot += x;
+    }
+    CHECK_ARG(tot == t, "column groups do not add up to t");
+  }
+  CHECK_ARG(kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET, "seed operator must be QUADFORM or LDET");
+  CHECK_ARG(t >= 1 && maxit >= 2, "bad t or maxit");
+  const int64_t n = g->n;
+  cudaStream_t st = g->stream;
+  auto* S = new slemm_lseed();
+  try {
+    S->g = g;
+    S->kind = kind;
+    S->tau0 = tau0;
+    S->t = t;
+    S->n = n;
+    {
+      int c0 = 0;
+      for (int x : groups) {
+        S->group_start.push_back(c0);
+        c0 += x;
+      }
+      S->group_start.push_back(c0);
+      S->group_iters.assign(groups.size(), -1);
+    }
+    S->B.ensure((size_t)n * t * sizeof(float));
+    CUDA_TRY(cudaMemcpyAsync(S->B.p, dB, (size_t)n * t * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    const int nblk = (int)ceil_div(n, kLzRows);
+    DevBuf red, scal, tmpb;
+    red.ensure((size_t)nblk * t * sizeof(double));
+    scal.ensure((size_t)4 * t * sizeof(double));   // [0]=dots [1]=nrm2 [2]=unorm2 [3]=beta(device)
+    tmpb.ensure((size_t)n * t * sizeof(float));
+    double* d_dot = scal.as<double>();
+    double* d_nrm = d_dot + t;
+    double* d_un = d_nrm + t;
+    double* d_beta = d_un + t;
+    float* tmp = tmpb.as<float>();
+    std::vector<double> h(3 * t);
+
+    // B_norm, U_0 = B / β_0
+    col_dots(g, S->B.as<float>(), n, nullptr, 0, n, t, d_nrm);
+    dim3 gr(nblk, t);
+    lz_scale_kernel<<<gr, 256, 0, st>>>(S->block(0), S->B.as<float>(), d_nrm, n, red.as<double>(), nblk);
+    LAUNCH_CHECK();
+    lz_reduce(red.as<double>(), nblk, t, d_un, st);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), d_nrm, 2 * t * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    S->bnorm.resize(t);
+    S->beta.assign(t, 0.0);
+    S->unorm.assign(t, 0.0);
+    for (int c = 0; c < t; ++c) {
+      S->bnorm[c] = std::sqrt(h[c]);
+      S->beta[c] = S->bnorm[c];
+      S->unorm[c] = std::sqrt(h[t + c]);
+      if (!(S->bnorm[c] > 0.0) || !std::isfinite(S->bnorm[c]))
+        SLEMM_THROW(SLEMM_ERR_NUMERIC, "right-hand side column " + std::to_string(c) + " has zero or non-finite norm");
+    }
+    std::vector<double> rho(t), gamma(t, 1.0), omega(t, 0.0), gamma_prev(t), omega_prev(t);
+    for (int c = 0; c < t; ++c) rho[c] = S->bnorm[c];
+    int j = 0;
+    bool cnvg = false;
+    const int ngroups = (int)groups.size();
+    std::vector<double> col_res(t, 0.0);
+    while (j < maxit - 1) {
+      float* Uj = S->block(j);
+      float* Uprev = j > 0 ? S->block(j - 1) : nullptr;
+      op_device(g, kind, tau0, Uj, n, t, tmp, n);
+      if (j > 0)
+        CUDA_TRY(cudaMemcpyAsync(d_beta, S->beta.data() + (size_t)j * t, t * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+      lz_dot_kernel<<<gr, 256, 0, st>>>(tmp, Uj, Uprev, j > 0 ? d_beta : nullptr, n, red.as<double>(), nblk);
+      LAUNCH_CHECK();
+      lz_reduce(red.as<double>(), nblk, t, d_dot, st);
+      lz_orth_kernel<<<gr, 256, 0, st>>>(tmp, Uj, d_dot, n, red.as<double>(), nblk);
+      LAUNCH_CHECK();
+      lz_reduce(red.as<double>(), nblk, t, d_nrm, st);
+      float* Un = S->block(j + 1);
+      lz_scale_kernel<<<gr, 256, 0, st>>>(Un, tmp, d_nrm, n, red.as<double>(), nblk);
+      LAUNCH_CHECK();
+      lz_reduce(red.as<double>(), nblk, t, d_un, st);
+      CUDA_TRY(cudaMemcpyAsync(h.data(), d_dot, 3 * t * sizeof(double), cudaMemcpyDeviceToHost, st));
+      check_device_error(g);   // synchronises
+      double res = 0.0;
+      for (int c = 0; c < t; ++c) {
+        const double dl = h[c], bt = std::sqrt(h[t + c]), un = std::sqrt(h[2 * t + c]);
+        S->delta.push_back(dl);
+        S->beta.push_back(bt);
+        S->unorm.push_back(un);
+        // CG coefficients (src/reml.cpp:304-307)
+        const double gm = (j == 0) ? 1.0 / dl : 1.0 / (dl - omega[c] / gamma[c]);
+        const double om = (bt * gm) * (bt * gm);
+        rho[c] = -bt * gm * rho[c];
+        gamma[c] = gm;
+        omega[c] = om;
+        col_res[c] = std::fabs(rho[c]) * un / S->bnorm[c];
+        if (!std::isfinite(dl) || !std::isfinite(bt))
+          SLEMM_THROW(SLEMM_ERR_NUMERIC, "non-finite Lanczos coefficient at step " + std::to_string(j));
+      }
+      ++j;
+      bool all = true;
+      for (int q = 0; q < ngroups; ++q) {
+        if (S->group_iters[q] >= 0) continue;
+        double rg = 0.0;
+        for (int c = S->group_start[q]; c < S->group_start[q + 1]; ++c) rg = std::max(rg, col_res[c]);
+        if (rg <= tol) S->group_iters[q] = j;
+        else all = false;
+        res = std::max(res, rg);
+      }
+      if (verbose && j % p_freq == 0) printf("Relative error at step %d is %g\n", j, res);
+      if (all) {
+        cnvg = true;
+        break;
+      }
+    }
+    for (int q = 0; q < ngroups; ++q)
+      if (S->group_iters[q] < 0) S->group_iters[q] = j;
+    if (verbose) {
+      if (cnvg) printf("Converged after %d iterations.\n", j);
+      else printf("Failed to converge after %d iterations.\n", maxit);
+      fflush(stdout);
+    }
+    S->iters = j;
+  } catch (...) {
+    delete S;
+    throw;
+  }
+  return S;
+}
+
+// X = (A + σI)^{-1}B for the columns of group `grp` (all columns when the seed has one group),
+// using at most that group's basis; X on device (tc columns, ld = ldx).  Returns the CG steps.
+int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp)
+{
+  const int t = S->t;
+  const int c0 = S->group_start[grp], tc = S->group_start[grp + 1] - c0;
+  const int J = S->group_iters[grp];
+  cudaStream_t st = S->g->stream;
+  // forward pass: γ, ω, ρ with the reference's stopping rule (src/reml.cpp:404-426)
+  std::vector<double> gam((size_t)(J + 1) * tc, 0.0), om((size_t)(J + 1) * tc, 0.0), rho((size_t)(J + 1) * tc, 0.0);
+  for (int c = 0; c < tc; ++c) rho[c] = S->bnorm[c0 + c];
+  int steps = 0;
+  for (int j = 0; j < J; ++j) {
+    double res = 0.0;
+    for (int c = 0; c < tc; ++c) {
+      const int cc = c0 + c;
+      const double dl = S->delta[(size_t)j * t + cc] + sigma;
+      const double bt = S->beta[(size_t)(j + 1) * t + cc];
+      const double g = (j == 0) ? 1.0 / dl : 1.0 / (dl - om[(size_t)(j - 1) * tc + c] / gam[(size_t)(j - 1) * tc + c]);
+      gam[(size_t)j * tc + c] = g;
+      om[(size_t)j * tc + c] = (bt * g) * (bt * g);
+      rho[(size_t)(j + 1) * tc + c] = -bt * g * rho[(size_t)j * tc + c];
+      res = std::max(res, std::fabs(rho[(size_t)(j + 1) * tc + c]) * S->unorm[(size_t)(j + 1) * t + cc] / S->bnorm[cc]);
+    }
+    steps = j + 1;
+    if (res <= tol) break;
+  }
+  // backward pass: S_i = γ_i + ω_i S_{i+1}; X = S_0 B + Σ_{i=1}^{steps-1} ρ_i S_i U_i
+  // (the R and P of the last step are not folded into X: X is updated before R).
+  std::vector<double> coef((size_t)steps * tc, 0.0);
+  std::vector<double> Sacc(tc, 0.0);
+  for (int i = steps - 1; i >= 0; --i) {
+    for (int c = 0; c < tc; ++c) {
+      Sacc[c] = gam[(size_t)i * tc + c] + om[(size_t)i * tc + c] * Sacc[c];
+      coef[(size_t)i * tc + c] = (i == 0) ? Sacc[c] : rho[(size_t)i * tc + c] * Sacc[c];
+    }
+  }
+  std::vector<const float*> hblocks(std::max(steps, 1));
+  for (int i = 0; i < steps; ++i) hblocks[i] = (i == 0) ? nullptr : S->block(i);
+  DevBuf dcoef, dblk;
+  dcoef.ensure(coef.size() * sizeof(double));
+  dblk.ensure(hblocks.size() * sizeof(float*));
+  CUDA_TRY(cudaMemcpyAsync(dcoef.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(dblk.p, hblocks.data(), hblocks.size() * sizeof(float*), cudaMemcpyHostToDevice, st));
+  dim3 gr((unsigned)ceil_div(S->n, 256), tc);
+  lz_combine_kernel<<<gr, 256, 0, st>>>(dX, ldx, S->B.as<float>(), dblk.as<const float*>(), steps - 1,
+                                        dcoef.as<double>(), S->n, c0, tc);
+  LAUNCH_CHECK();
+  CUDA_TRY(cudaStreamSynchronize(st));   // the coefficient buffers are freed on return
+  return steps;
+}
+
+// Batched tridiagonal eigensolve on the GPU (host in/out, FP64).
+void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2)
+{
+  if (t <= 0 || nld <= 0) return;
+  std::vector<double> hd((size_t)t * nld), he((size_t)t * nld, 0.0);
+  for (int i = 0; i < nld; ++i)
+    for (int p = 0; p < t; ++p) {
+      hd[(size_t)i * t + p] = delta[(size_t)i * t + p];
+      if (i + 1 < nld) he[(size_t)i * t + p] = beta[(size_t)(i + 1) * t + p];
+    }
+  DevBuf dd, de, dz, df;
+  dd.ensure(hd.size() * sizeof(double));
+  de.ensure(he.size() * sizeof(double));
+  dz.ensure(hd.size() * sizeof(double));
+  df.ensure(sizeof(int));
+  CUDA_TRY(cudaMemcpy(dd.p, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(de.p, he.data(), he.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(df.p, 0, sizeof(int)));
+  tridiag_ql_kernel<<<(unsigned)ceil_div(t, 32), 32>>>(dd.as<double>(), de.as<double>(), dz.as<double>(), t, nld,
+                                                       df.as<int>());
+  LAUNCH_CHECK();
+  std::vector<double> hz(hd.size());
+  int fail = 0;
+  CUDA_TRY(cudaMemcpy(hd.data(), dd.p, hd.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(hz.data(), dz.p, hz.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(&fail, df.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (fail) SLEMM_THROW(SLEMM_ERR_NUMERIC, "tridiagonal QL did not converge in 64 sweeps");
+  // sort eigenvalues ascending per probe (column-major t×nld output)
+  std::vector<int> idx(nld);
+  for (int p = 0; p < t; ++p) {
+    for (int i = 0; i < nld; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return hd[(size_t)a * t + p] < hd[(size_t)b * t + p]; });
+    for (int i = 0; i < nld; ++i) {
+      D[(size_t)i * t + p] = hd[(size_t)idx[i] * t + p];
+      const double zz = hz[(size_t)idx[i] * t + p];
+      W2[(size_t)i * t + p] = zz * zz;
+    }
+  }
+}
+
+}  // namespace slemm
+
+extern "C" {
+
+int slemm_gpu_lanczos_seed(slemm_geno* g, int op_kind, float tau0, const float* B, int64_t ldb, int t,
+                           float tol, int maxit, int mem, slemm_lseed** out, int* iters)
+{
+  return guarded([&] {
+    CHECK_ARG(g && B && out, "null argument");
+    *out = nullptr;
+    CHECK_ARG(ldb >= g->n, "ldb < n");
+    DevBuf dB;
+    const float* src = B;
+    if (mem == SLEMM_MEM_HOST || ldb != g->n) {
+      dB.ensure((size_t)g->n * t * sizeof(float));
+      CUDA_TRY(cudaMemcpy2DAsync(dB.p, g->n * sizeof(float), B, ldb * sizeof(float), g->n * sizeof(float), t,
+                                 mem == SLEMM_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                 g->stream));
+      src = dB.as<float>();
+    }
+    slemm_lseed* S = lanczos_seed_device(g, op_kind, tau0, src, t, tol, maxit, false, {}, 5);
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    *out = S;
+    if (iters) *iters = S->iters;
+  });
+}
+
+int slemm_gpu_lseed_destroy(slemm_lseed* s)
+{
+  return guarded([&] {
+    if (s && s->g) cudaStreamSynchronize(s->g->stream);
+    delete s;
+  });
+}
+
+int slemm_gpu_lseed_coeffs(const slemm_lseed* s, double* beta, double* delta)
+{
+  return guarded([&] {
+    CHECK_ARG(s != nullptr, "null seed");
+    const int t = s->t, J = s->iters;
+    for (int j = 0; j <= J; ++j)
+      for (int c = 0; c < t; ++c) {
+        if (beta) beta[(size_t)j * t + c] = s->beta[(size_t)j * t + c];
+        if (delta && j < J) delta[(size_t)j * t + c] = s->delta[(size_t)j * t + c];
+      }
+  });
+}
+
+int slemm_gpu_lanczos_solve(slemm_lseed* s, float sigma, float tol, float* X, int64_t ldx, int mem)
+{
+  return guarded([&] {
+    CHECK_ARG(s && X, "null argument");
+    CHECK_ARG(ldx >= s->n, "ldx < n");
+    if (mem == SLEMM_MEM_DEVICE) {
+      lanczos_solve_device(s, sigma, tol, X, ldx, 0);
+      return;
+    }
+    DevBuf dX;
+    dX.ensure((size_t)s->n * s->t * sizeof(float));
+    lanczos_solve_device(s, sigma, tol, dX.as<float>(), s->n, 0);
+    CUDA_TRY(cudaMemcpy2D(X, ldx * sizeof(float), dX.p, s->n * sizeof(float), s->n * sizeof(float), s->t,
+                          cudaMemcpyDeviceToHost));
+  });
+}
+
+int slemm_gpu_tridiag_eig(const double* delta, const double* beta, int t, int nld, double* D, double* W2)
+{
+  return guarded([&] {
+    CHECK_ARG(delta && beta && D && W2, "null argument");
+    CHECK_ARG(t >= 1 && nld >= 1, "empty problem");
+    tridiag_eig_host(delta, beta, t, nld, D, W2);
+  });
+}
+
+}  // extern "C"
+
+namespace slemm {
+int lseed_iters(const slemm_lseed* S, int grp) { return S->group_iters[grp]; }
+const double* lseed_delta(const slemm_lseed* S) { return S->delta.data(); }
+const double* lseed_beta(const slemm_lseed* S) { return S->beta.data(); }
+int lseed_t(const slemm_lseed* S) { return S->t; }
+void lseed_free(slemm_lseed* S) { delete S; }
+}  // namespace slemm

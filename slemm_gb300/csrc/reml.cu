@@ -1,0 +1,696 @@
+// reml.cu — REML drivers on the GPU operators: DF-REML (SLDF_REML, src/reml.cpp:549-690) and
+// MC-REML (LMC_REML, src/reml.cpp:730-883).
+//
+// All vectors of length n or m stay in HBM; the host keeps the FP64 scalars (Lanczos/CG
+// coefficients, golden-section and secant state, c×c covariate algebra).  Probe draws come
+// from libstdc++'s std::mt19937 with the reference's distributions and draw order, so the GPU
+// engine sees the reference's probes.
+#include "internal.h"
+
+#include <chrono>
+#include <memory>
+#include <random>
+
+namespace slemm {
+
+// ---- host dense helpers (FP64) ---------------------------------------------------------------
+// Column-pivoted Householder QR of an n×c column-major matrix (the reference uses Eigen's
+// ColPivHouseholderQR, src/reml.cpp:583-588).  Returns Q (n×rank), R·Pᵀ (rank×c) and the rank
+// under Eigen's rule |R_ii| > eps_f32·min(n,c)·|R_00|.
+struct QRHost {
+  std::vector<double> Q;     // n×rank
+  std::vector<double> RPt;   // rank×c (column-major)
+  int rank = 0;
+};
+
+static QRHost qr_colpiv(const std::vector<double>& A0, int64_t n, int c)
+{
+  std::vector<double> A(A0);
+  std::vector<int> perm(c);
+  std::vector<double> tau(c, 0.0);
+  for (int j = 0; j < c; ++j) perm[j] = j;
+  auto col = [&](int j) { return A.data() + (size_t)j * n; };
+  const int kmax = (int)std::min<int64_t>(n, c);
+  for (int k = 0; k < kmax; ++k) {
+    // pivot: largest remaining column norm
+    int p = k;
+    double best = -1.0;
+    for (int j = k; j < c; ++j) {
+      double s = 0.0;
+      const double* a = col(j);
+      for (int64_t i = k; i < n; ++i) s += a[i] * a[i];
+      if (s > best) {
+        best = s;
+        p = j;
+      }
+    }
+    if (p != k) {
+      std::swap_ranges(col(k), col(k) + n, col(p));
+      std::swap(perm[k], perm[p]);
+    }
+    double* a = col(k);
+    const double nrm = std::sqrt(best);
+    if (nrm == 0.0) {
+      tau[k] = 0.0;
+      continue;
+    }
+    const double alpha = a[k] >= 0 ? -nrm : nrm;
+    const double v0 = a[k] - alpha;
+    // v = [1, a[k+1..]/v0], tau = (alpha - a_k)/alpha ... use explicit 2/(vᵀv)
+    for (int64_t i = k + 1; i < n; ++i) a[i] /= v0;
+    double vtv = 1.0;
+    for (int64_t i = k + 1; i < n; ++i) vtv += a[i] * a[i];
+    tau[k] = 2.0 / vtv;
+    a[k] = alpha;
+    for (int j = k + 1; j < c; ++j) {
+      double* b = col(j);
+      double s = b[k];
+      for (int64_t i = k + 1; i < n; ++i) s += a[i] * b[i];
+      s *= tau[k];
+      b[k] -= s;
+      for (int64_t i = k + 1; i < n; ++i) b[i] -= s * a[i];
+    }
+  }
+  QRHost r;
+  const double maxpiv = kmax ? std::fabs(A[0]) : 0.0;
+  const double thr = 1.1920928955078125e-07 * kmax * maxpiv;
+  int rank = 0;
+  for (int k = 0; k < kmax; ++k)
+    if (std::fabs(A[(size_t)k * n + k]) > thr) ++rank;
+  r.rank = rank;
+  // Q = H_0 … H_{kmax−1} · I[:, :rank]
+  r.Q.assign((size_t)n * rank, 0.0);
+  for (int j = 0; j < rank; ++j) {
+    double* q = r.Q.data() + (size_t)j * n;
+    q[j] = 1.0;
+    for (int k = kmax - 1; k >= 0; --k) {
+      if (tau[k] == 0.0) continue;
+      const double* v = col(k);
+      double s = q[k];
+      for (int64_t i = k + 1; i < n; ++i) s += v[i] * q[i];
+      s *= tau[k];
+      q[k] -= s;
+      for (int64_t i = k + 1; i < n; ++i) q[i] -= s * v[i];
+    }
+  }
+  // R·Pᵀ: column perm[j] of the result = column j of R (upper triangle)
+  r.RPt.assign((size_t)rank * c, 0.0);
+  for (int j = 0; j < c; ++j)
+    for (int i = 0; i < rank && i <= j; ++i) r.RPt[(size_t)perm[j] * rank + i] = A[(size_t)j * n + i];
+  return r;
+}
+
+// log|det M| and M^{-1} for a small c×c matrix (partial-pivot LU), column-major.
+static double logabsdet(std::vector<double> M, int c, std::vector<double>* inv = nullptr)
+{
+  std::vector<int> piv(c);
+  double ld = 0.0;
+  for (int k = 0; k < c; ++k) {
+    int p = k;
+    for (int i = k + 1; i < c; ++i)
+      if (std::fabs(M[(size_t)k * c + i]) > std::fabs(M[(size_t)k * c + p])) p = i;
+    piv[k] = p;
+    if (p != k)
+      for (int j = 0; j < c; ++j) std::swap(M[(size_t)j * c + k], M[(size_t)j * c + p]);
+    const double d = M[(size_t)k * c + k];
+    ld += std::log(std::fabs(d));
+    for (int i = k + 1; i < c; ++i) {
+      M[(size_t)k * c + i] /= d;
+      for (int j = k + 1; j < c; ++j) M[(size_t)j * c + i] -= M[(size_t)k * c + i] * M[(size_t)j * c + k];
+    }
+  }
+  if (inv) {
+    inv->assign((size_t)c * c, 0.0);
+    for (int col = 0; col < c; ++col) {
+      std::vector<double> b(c, 0.0);
+      b[col] = 1.0;
+      for (int k = 0; k < c; ++k) std::swap(b[k], b[piv[k]]);
+      for (int i = 0; i < c; ++i)
+        for (int j = 0; j < i; ++j) b[i] -= M[(size_t)j * c + i] * b[j];
+      for (int i = c - 1; i >= 0; --i) {
+        for (int j = i + 1; j < c; ++j) b[i] -= M[(size_t)j * c + i] * b[j];
+        b[i] /= M[(size_t)i * c + i];
+      }
+      for (int i = 0; i < c; ++i) (*inv)[(size_t)col * c + i] = b[i];
+    }
+  }
+  return ld;
+}
+
+// Solves the symmetric positive definite system M x = b (Cholesky), c small.
+static std::vector<double> spd_solve(std::vector<double> M, int c, std::vector<double> b)
+{
+  for (int j = 0; j < c; ++j) {
+    double s = M[(size_t)j * c + j];
+    for (int k = 0; k < j; ++k) s -= M[(size_t)k * c + j] * M[(size_t)k * c + j];
+    if (!(s > 0)) SLEMM_THROW(SLEMM_ERR_NUMERIC, "matrix not positive definite in BLUE solve");
+    const double d = std::sqrt(s);
+    M[(size_t)j * c + j] = d;
+    for (int i = j + 1; i < c; ++i) {
+      double t = M[(size_t)j * c + i];
+      for (int k = 0; k < j; ++k) t -= M[(size_t)k * c + i] * M[(size_t)k * c + j];
+      M[(size_t)j * c + i] = t / d;
+    }
+  }
+  for (int i = 0; i < c; ++i) {
+    for (int k = 0; k < i; ++k) b[i] -= M[(size_t)k * c + i] * b[k];
+    b[i] /= M[(size_t)i * c + i];
+  }
+  for (int i = c - 1; i >= 0; --i) {
+    for (int k = i + 1; k < c; ++k) b[i] -= M[(size_t)i * c + k] * b[k];
+    b[i] /= M[(size_t)i * c + i];
+  }
+  return b;
+}
+
+// ---- small device kernels ---------------------------------------------------------------------
+__global__ void scale_rows_kernel(float* __restrict__ X, int64_t ld, int64_t rows, int k,
+                                  const float* __restrict__ s, int sqrt_of_s)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i >= rows) return;
+  const float f = sqrt_of_s ? sqrtf(s[i]) : s[i];
+  X[(int64_t)c * ld + i] *= f;
+}
+
+static void scale_rows(slemm_geno* g, float* X, int64_t ld, int64_t rows, int k, const float* s,
+                       bool sq = false)
+{
+  dim3 gr((unsigned)ceil_div(rows, 256), k);
+  scale_rows_kernel<<<gr, 256, 0, g->stream>>>(X, ld, rows, k, s, sq ? 1 : 0);
+  LAUNCH_CHECK();
+}
+
+// Py[:,0] = PV[:,0]; Py[:,c] = PV[:,c] + st·PV[:,n_MC+c]   (src/reml.cpp:716-717)
+__global__ void lmc_combine_kernel(const float* __restrict__ PV, float* __restrict__ Py, int64_t n,
+                                   int n_MC, float st)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i >= n) return;
+  if (c == 0) Py[i] = PV[i];
+  else Py[(int64_t)c * n + i] = PV[(int64_t)c * n + i] + st * PV[(int64_t)(n_MC + c) * n + i];
+}
+
+// y_out[i] = r[i]·y[i] − s·rv[i]·p[i]  helper for the LMC BLUE residual (src/reml.cpp:872-874)
+__global__ void lmc_resid_kernel(const float* __restrict__ y, const float* __restrict__ zb,
+                                 const float* __restrict__ rvec, const float* __restrict__ Py, float tau1,
+                                 int64_t n, float* __restrict__ out)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = zb[i] + tau1 * (rvec[i] * Py[i]);
+  out[i] = y[i] - v;
+}
+
+static std::vector<double> d2h(slemm_geno* g, const double* d, size_t cnt)
+{
+  std::vector<double> h(cnt);
+  CUDA_TRY(cudaMemcpyAsync(h.data(), d, cnt * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+  CUDA_TRY(cudaStreamSynchronize(g->stream));
+  return h;
+}
+
+// Common set-up of both drivers: rr, Q (rank check), gm, gw (src/reml.cpp:574-622, 757-781).
+struct Setup {
+  std::vector<float> rr, gm, gw;
+  QRHost qr;
+  int c = 0;
+};
+
+static Setup reml_setup(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
+                        const float* persnp)
+{
+  const int64_t n = g->n, m = g->m;
+  CHECK_ARG(c >= 1 && c <= 64, "number of covariates must be in [1, 64]");
+  Setup S;
+  S.rr.resize(n);
+  for (int64_t i = 0; i < n; ++i) {
+    const float r = rvec ? rvec[i] : 1.0f;
+    if (!(r > 0.f) || !std::isfinite(r)) SLEMM_THROW(SLEMM_ERR_NUMERIC, "error variance weight must be > 0");
+    S.rr[i] = 1.0f / std::sqrt(r);   // Eigen rsqrt
+  }
+  std::vector<double> A((size_t)n * c);
+  for (int j = 0; j < c; ++j)
+    for (int64_t i = 0; i < n; ++i) {
+      const float xv = X[(size_t)j * ldx + i];
+      if (!std::isfinite(xv)) SLEMM_THROW(SLEMM_ERR_NUMERIC, "non-finite covariate");
+      A[(size_t)j * n + i] = (double)(S.rr[i] * xv);
+    }
+  S.qr = qr_colpiv(A, n, c);
+  if (S.qr.rank != c) SLEMM_THROW(SLEMM_ERR_RANK, "Fixed-effects design matrix is not of full rank.");
+  S.c = c;
+  // gm = nz_bits/float(n) from the GPU popcounts (bit-exact integers)
+  std::vector<int64_t> pc(m);
+  {
+    int st = slemm_gpu_genotype_counts(g, pc.data(), nullptr, nullptr, nullptr);
+    if (st != SLEMM_OK) SLEMM_THROW(st, "genotype counts failed");
+  }
+  S.gm.resize(m);
+  for (int64_t j = 0; j < m; ++j) S.gm[j] = (int)pc[j] / (float)n;
+  // gw = 1/(gm(2−gm)/2) / m · persnp/mean(persnp)  in FP32
+  float psum = 0.f;
+  for (int64_t j = 0; j < m; ++j) psum += persnp[j];
+  const float pmean = psum / (float)m;
+  S.gw.resize(m);
+  for (int64_t j = 0; j < m; ++j) {
+    const float v = S.gm[j] * (2.0f - S.gm[j]) / 2.0f;
+    S.gw[j] = (1.0f / v) / (float)m * (persnp[j] / pmean);
+    if (!std::isfinite(S.gw[j]))
+      SLEMM_THROW(SLEMM_ERR_NUMERIC, "monomorphic SNP " + std::to_string(j) + " gives an infinite weight");
+  }
+  int st = slemm_gpu_set_weights(g, S.gm.data(), S.gw.data(), S.rr.data());
+  if (st != SLEMM_OK) SLEMM_THROW(st, "set_weights failed");
+  std::vector<float> Qf((size_t)n * c);
+  for (size_t i = 0; i < Qf.size(); ++i) Qf[i] = (float)S.qr.Q[i];
+  st = slemm_gpu_set_projection(g, Qf.data(), n, c);
+  if (st != SLEMM_OK) SLEMM_THROW(st, "set_projection failed");
+  return S;
+}
+
+static void upload(slemm_geno* g, float* d, const float* h, size_t cnt)
+{
+  CUDA_TRY(cudaMemcpyAsync(d, h, cnt * sizeof(float), cudaMemcpyHostToDevice, g->stream));
+}
+
+// ================================================================================================
+// DF-REML
+// ================================================================================================
+struct Criterion {
+  double slogLL, vg, ve, lrt;
+};
+
+void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+               const float* persnp, const slemm_reml_opts& o, float* Py_out, float* blup_out,
+               float* blue_out, float* var_blue_out, slemm_reml_result* res)
+{
+  const auto t_start = std::chrono::steady_clock::now();
+  const int64_t n = g->n, m = g->m;
+  const bool verbose = o.verbose != 0;
+  if (verbose) printf("\nStarted stochastic Lanczos DF-REML.\n");
+  Setup S = reml_setup(g, rvec, X, ldx, c, persnp);
+  cudaStream_t st = g->stream;
+  const int n_V = o.n_V;
+  CHECK_ARG(n_V >= 1, "n_V must be >= 1");
+  // y_proj = (I − QQᵀ)(rr∘y)   (src/reml.cpp:591-592), FP64 on the host
+  std::vector<float> yproj(n);
+  {
+    std::vector<double> ry(n);
+    for (int64_t i = 0; i < n; ++i) ry[i] = (double)(S.rr[i] * y[i]);
+    for (int l = 0; l < c; ++l) {
+      const double* q = S.qr.Q.data() + (size_t)l * n;
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i) s += q[i] * ry[i];
+      for (int64_t i = 0; i < n; ++i) ry[i] -= s * q[i];
+    }
+    for (int64_t i = 0; i < n; ++i) yproj[i] = (float)ry[i];
+  }
+  if (verbose) printf("Projected covariates out of phenotypes.\nGenerating %d Rademacher probing vectors.\n", n_V);
+  // Rademacher probes: reml.cpp:597-605 (libstdc++ draws), column norms in FP32
+  const int tQV = c + n_V;
+  std::vector<float> QV((size_t)n * tQV);
+  for (size_t i = 0; i < (size_t)n * c; ++i) QV[i] = (float)S.qr.Q[i];
+  {
+    std::mt19937 rng(o.seed + 54321);
+    std::uniform_real_distribution<float> runif(0.0, 1.0);
+    for (int j = 0; j < n_V; ++j) {
+      float* v = QV.data() + (size_t)(c + j) * n;
+      for (int64_t i = 0; i < n; ++i) v[i] = (runif(rng) < 0.5) ? -1.0f : 1.0f;
+      const float nrm = std::sqrt((float)n);   // Σ(±1)² = n exactly
+      for (int64_t i = 0; i < n; ++i) v[i] /= nrm;
+    }
+  }
+  DevBuf d_y, d_QV, d_X, d_tmp;
+  d_y.ensure((size_t)n * sizeof(float));
+  d_QV.ensure((size_t)n * tQV * sizeof(float));
+  d_X.ensure((size_t)n * tQV * sizeof(float));
+  d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + 64 * 64 * sizeof(double));
+  upload(g, d_y.as<float>(), yproj.data(), n);
+  upload(g, d_QV.as<float>(), QV.data(), (size_t)n * tQV);
+  double* d_scal = d_tmp.as<double>();
+
+  const float tau0 = (1.0f - o.s2max) / o.s2max;
+  if (verbose) printf("\nPerforming Lanczos decomposition for phenotypes:\n");
+  slemm_lseed* seed_y = lanczos_seed_device(g, SLEMM_OP_QUADFORM, tau0, d_y.as<float>(), 1, o.tol_L, o.maxit,
+                                            verbose, {}, 5);
+  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold_y(seed_y, lseed_free);
+  if (verbose) printf("\nPerforming Lanczos decomposition for covariates and Rademacher vectors:\n");
+  // [Q V] share the ldet operator: one block, two stopping groups (the reference's seed_Q
+  // and seed_V calls, src/reml.cpp:629-631)
+  slemm_lseed* seed_QV = lanczos_seed_device(g, SLEMM_OP_LDET, tau0, d_QV.as<float>(), tQV, o.tol_L, o.maxit,
+                                             verbose, {c, n_V}, 5);
+  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold_qv(seed_QV, lseed_free);
+  const int nld = lseed_iters(seed_QV, 1);
+  // Jacobi matrices of the probes (rows c … c+n_V−1), src/reml.cpp:638-646
+  std::vector<double> dl((size_t)n_V * nld), bt((size_t)n_V * (nld + 1));
+  {
+    const double* D = lseed_delta(seed_QV);
+    const double* B = lseed_beta(seed_QV);
+    for (int j = 0; j < nld; ++j)
+      for (int p = 0; p < n_V; ++p) dl[(size_t)j * n_V + p] = D[(size_t)j * tQV + c + p];
+    for (int j = 0; j <= nld; ++j)
+      for (int p = 0; p < n_V; ++p) bt[(size_t)j * n_V + p] = B[(size_t)j * tQV + c + p];
+  }
+  std::vector<double> DV((size_t)n_V * nld), W2((size_t)n_V * nld);
+  tridiag_eig_host(dl.data(), bt.data(), n_V, nld, DV.data(), W2.data());
+
+  // ySy
+  col_dots(g, d_y.as<float>(), n, nullptr, 0, n, 1, d_scal);
+  const double ySy = d2h(g, d_scal, 1)[0];
+  int n_eval = 0;
+  // REML_criterion (src/reml.cpp:457-489)
+  auto criterion = [&](float ss) -> Criterion {
+    ++n_eval;
+    const float tau = (1 - ss) / ss;
+    const float sigma = tau - tau0;
+    lanczos_solve_device(seed_y, (double)sigma, 1e-6, d_X.as<float>(), n, 0);
+    col_dots(g, d_y.as<float>(), n, d_X.as<float>(), n, n, 1, d_scal);
+    const double yPy = d2h(g, d_scal, 1)[0];
+    Criterion r;
+    r.vg = yPy / (double)(n - c);
+    r.ve = r.vg * tau;
+    double ldet_H = 0.0;
+    for (size_t q = 0; q < DV.size(); ++q) ldet_H += W2[q] * std::log(DV[q] + sigma);
+    ldet_H = ldet_H * (double)n / (double)n_V;
+    r.lrt = (double)n * std::log(ySy / yPy) - ldet_H;
+    lanczos_solve_device(seed_QV, (double)sigma, 1e-6, d_X.as<float>(), n, 0);
+    proj_coeffs(g, d_X.as<float>(), n, c, d_scal);
+    std::vector<double> M = d2h(g, d_scal, (size_t)c * c);
+    r.slogLL = (double)(n - c) * std::log(ySy / yPy) - logabsdet(M, c) - ldet_H;
+    return r;
+  };
+  // REML_GSS (src/reml.cpp:493-547)
+  const double invphi = 0.618033988749894848204586834365638117720309179805762862135;
+  const double invphi2 = 0.381966011250105151795413165634361882279690820194237137864;
+  float a = o.s2min, b = o.s2max;
+  if (verbose) printf("\nDoing golden section search in (%g, %g)\n", a, b);
+  float h = b - a;
+  int nitr = (h < o.tol_VC) ? 1 : (int)std::ceil(std::log(o.tol_VC / h) / std::log(invphi));
+  if (verbose) printf("%d iterations:\n", nitr);
+  float cc = (float)(a + invphi2 * h), dd = (float)(a + invphi * h);
+  Criterion fc = criterion(cc), fd = criterion(dd), last = fd;
+  for (int i = 0; i < nitr; ++i) {
+    double fm;
+    if (fc.slogLL > fd.slogLL) {
+      b = dd;
+      dd = cc;
+      fd = fc;
+      h = (float)(h * invphi);
+      cc = (float)(a + invphi2 * h);
+      fc = criterion(cc);
+      last = fc;
+      fm = fc.slogLL;
+    } else {
+      a = cc;
+      cc = dd;
+      fc = fd;
+      h = (float)(h * invphi);
+      dd = (float)(a + invphi * h);
+      fd = criterion(dd);
+      last = fd;
+      fm = fd.slogLL;
+    }
+    if (verbose) printf("Itr %d: h2 in (%g, %g) and 2logLL = %g\n", i + 1, a, b, fm);
+  }
+  if (verbose) printf("\nCompleted golden section search.\n");
+  const float vg = (float)last.vg, ve = (float)last.ve, lrt = (float)last.lrt;
+  const float tau1 = ve / vg;
+
+  // Py = rr∘(I−QQᵀ)L_Solve(seed_y, y_proj, τ1−τ0)   (src/reml.cpp:659-661)
+  float* d_Py = d_X.as<float>();
+  lanczos_solve_device(seed_y, (double)(tau1 - tau0), 1e-6, d_Py, n, 0);
+  proj_coeffs(g, d_Py, n, 1, d_scal);
+  proj_apply(g, d_Py, n, 1, d_scal);
+  scale_rows(g, d_Py, n, n, 1, g->rr.as<float>());
+  // snp_blup = W Z_cᵀ Py  (src/reml.cpp:662)
+  DevBuf d_b;
+  d_b.ensure((size_t)m * sizeof(float));
+  op_device(g, SLEMM_OP_WRMATVEC, 0.f, d_Py, n, 1, d_b.as<float>(), m);
+  CUDA_TRY(cudaMemcpyAsync(Py_out, d_Py, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(blup_out, d_b.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+  check_device_error(g);
+  if (verbose) printf("\nVg,%g\nVe,%g\nh2,%g\nLRT,%g\n", vg, ve, vg / (vg + ve), lrt);
+
+  // BLUE and var(BLUE) (src/reml.cpp:674-677): with rr∘X = Q·qrR,
+  //   XᵀH⁻¹X = qrRᵀ (Qᵀ S) qrR and (H⁻¹X)ᵀy = qrRᵀ Sᵀ(rr∘y), S = L_Solve(seed_Q, Q, τ1−τ0)
+  float* d_S = d_X.as<float>();
+  lanczos_solve_device(seed_QV, (double)(tau1 - tau0), 1e-6, d_S, n, 0);
+  proj_coeffs(g, d_S, n, c, d_scal);
+  std::vector<double> QtS = d2h(g, d_scal, (size_t)c * c);
+  {
+    std::vector<float> ry(n);
+    for (int64_t i = 0; i < n; ++i) ry[i] = S.rr[i] * y[i];
+    upload(g, d_y.as<float>(), ry.data(), n);
+  }
+  std::vector<double> Sty(c);
+  for (int l = 0; l < c; ++l) {
+    col_dots(g, d_S + (size_t)l * n, n, d_y.as<float>(), n, n, 1, d_scal + 64 * 64);
+    Sty[l] = d2h(g, d_scal + 64 * 64, 1)[0];
+  }
+  const std::vector<double>& R = S.qr.RPt;   // c×c
+  std::vector<double> XtHX((size_t)c * c, 0.0), rhs(c, 0.0), T((size_t)c * c, 0.0);
+  for (int i = 0; i < c; ++i)          // T = (QᵀS)·R
+    for (int j = 0; j < c; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < c; ++k) s += QtS[(size_t)i * c + k] * R[(size_t)j * c + k];   // (QᵀS)[i][k] is row-major
+      T[(size_t)j * c + i] = s;
+    }
+  for (int i = 0; i < c; ++i)          // XtHX = Rᵀ T
+    for (int j = 0; j < c; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < c; ++k) s += R[(size_t)i * c + k] * T[(size_t)j * c + k];
+      XtHX[(size_t)j * c + i] = s;
+    }
+  for (int i = 0; i < c; ++i) {        // rhs = Rᵀ (Sᵀ rr∘y)
+    double s = 0.0;
+    for (int k = 0; k < c; ++k) s += R[(size_t)i * c + k] * Sty[k];
+    rhs[i] = s;
+  }
+  // symmetrise (the product is symmetric in exact arithmetic)
+  for (int i = 0; i < c; ++i)
+    for (int j = 0; j < i; ++j) {
+      const double v = 0.5 * (XtHX[(size_t)j * c + i] + XtHX[(size_t)i * c + j]);
+      XtHX[(size_t)j * c + i] = XtHX[(size_t)i * c + j] = v;
+    }
+  std::vector<double> blue = spd_solve(XtHX, c, rhs);
+  std::vector<double> inv;
+  logabsdet(XtHX, c, &inv);
+  for (int i = 0; i < c; ++i) blue_out[i] = (float)blue[i];
+  if (var_blue_out)
+    for (size_t q = 0; q < (size_t)c * c; ++q) var_blue_out[q] = (float)(inv[q] * vg);
+  if (verbose) {
+    printf("\nCompleted stochastic Lanczos DF-REML.\n");
+    if (o.s2max - vg / (vg + ve) < o.tol_VC)
+      printf("\nWarning: the h2 estimate is virtually the same as the max you specified.\nRerun with a higher --max_heritability.\n");
+  }
+  if (res) {
+    res->vg = vg;
+    res->ve = ve;
+    res->h2 = vg / (vg + ve);
+    res->lrt = lrt;
+    res->iters_y = lseed_iters(seed_y, 0);
+    res->iters_Q = lseed_iters(seed_QV, 0);
+    res->iters_V = nld;
+    res->n_criterion = n_eval;
+    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  }
+}
+
+// ================================================================================================
+// MC-REML
+// ================================================================================================
+void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+              const float* persnp, const slemm_reml_opts& o, float* Py_out, float* blup_out,
+              float* blue_out, slemm_reml_result* res)
+{
+  const auto t_start = std::chrono::steady_clock::now();
+  const int64_t n = g->n, m = g->m;
+  const bool verbose = o.verbose != 0;
+  if (verbose) printf("\nStarted Lanczos MC-REML.\n");
+  Setup S = reml_setup(g, rvec, X, ldx, c, persnp);
+  cudaStream_t st = g->stream;
+  const int n_MC = o.n_V;
+  CHECK_ARG(n_MC >= 1, "n_MC must be >= 1");
+  const int tV = 1 + 2 * n_MC;
+  // draws: u (m×n_MC) then e (n×n_MC) from one generator (src/reml.cpp:795-809)
+  std::vector<float> u((size_t)m * n_MC), V((size_t)n * tV);
+  {
+    if (verbose) printf("Generating %d MC samples for genetic effects.\n", n_MC);
+    std::mt19937 rng(o.seed + 54321);
+    std::normal_distribution<float> rnorm(0.0, 1.0);
+    for (int j = 0; j < n_MC; ++j)
+      for (int64_t i = 0; i < m; ++i) u[(size_t)j * m + i] = rnorm(rng);
+    if (verbose) printf("Generating %d MC samples for residuals.\n", n_MC);
+    for (int j = 1 + n_MC; j < tV; ++j)
+      for (int64_t i = 0; i < n; ++i) V[(size_t)j * n + i] = rnorm(rng);
+  }
+  for (int64_t i = 0; i < n; ++i) V[i] = y[i];
+  DevBuf d_V, d_u, d_PV, d_Py, d_ub, d_tmp, d_aux;
+  d_V.ensure((size_t)n * tV * sizeof(float));
+  d_u.ensure((size_t)m * n_MC * sizeof(float));
+  d_PV.ensure((size_t)n * tV * sizeof(float));
+  d_Py.ensure((size_t)n * (1 + n_MC) * sizeof(float));
+  d_ub.ensure((size_t)m * (1 + n_MC) * sizeof(float));
+  d_tmp.ensure((size_t)(64 * 64 + 4 * tV) * sizeof(double));
+  double* d_scal = d_tmp.as<double>();
+  upload(g, d_V.as<float>(), V.data(), (size_t)n * tV);
+  upload(g, d_u.as<float>(), u.data(), (size_t)m * n_MC);
+  // u *= sqrt(gw); V[:,1:1+n_MC] = Z_c u   (src/reml.cpp:801-802)
+  scale_rows(g, d_u.as<float>(), m, m, n_MC, g->w.as<float>(), true);
+  op_device(g, SLEMM_OP_MATVEC, 0.f, d_u.as<float>(), m, n_MC, d_V.as<float>() + n, n);
+  // V[:, :1+n_MC] *= rr; V −= QQᵀV   (src/reml.cpp:812-813)
+  if (verbose) printf("Projecting covariates out of phenotypes and MC samples.\n");
+  scale_rows(g, d_V.as<float>(), n, n, 1 + n_MC, g->rr.as<float>());
+  proj_coeffs(g, d_V.as<float>(), n, tV, d_scal);
+  proj_apply(g, d_V.as<float>(), n, tV, d_scal);
+
+  const float tau0 = (1.0f - o.s2max) / o.s2max;
+  if (verbose) printf("\nPerforming Lanczos decomposition:\n");
+  slemm_lseed* seed_V = lanczos_seed_device(g, SLEMM_OP_QUADFORM, tau0, d_V.as<float>(), tV, 10 * o.tol_L,
+                                            o.maxit, verbose, {}, 5);
+  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold(seed_V, lseed_free);
+  int n_eval = 0;
+  // REML_first_order (src/reml.cpp:696-728); leaves rr-scaled Py in d_Py
+  auto first_order = [&](float ss) -> float {
+    ++n_eval;
+    const float tau = (1 - ss) / ss;
+    const float sigma = tau - tau0;
+    lanczos_solve_device(seed_V, (double)sigma, 1e-6, d_PV.as<float>(), n, 0);
+    dim3 gr((unsigned)ceil_div(n, 256), 1 + n_MC);
+    lmc_combine_kernel<<<gr, 256, 0, st>>>(d_PV.as<float>(), d_Py.as<float>(), n, n_MC, std::sqrt(tau));
+    LAUNCH_CHECK();
+    proj_coeffs(g, d_Py.as<float>(), n, 1 + n_MC, d_scal);
+    proj_apply(g, d_Py.as<float>(), n, 1 + n_MC, d_scal);
+    col_dots(g, d_Py.as<float>(), n, nullptr, 0, n, 1 + n_MC, d_scal + 64 * 64);              // ‖e‖²
+    scale_rows(g, d_Py.as<float>(), n, n, 1 + n_MC, g->rr.as<float>());
+    op_device(g, SLEMM_OP_RMATVEC, 0.f, d_Py.as<float>(), n, 1 + n_MC, d_ub.as<float>(), m);
+    scale_rows(g, d_ub.as<float>(), m, m, 1 + n_MC, g->w.as<float>(), true);
+    col_dots(g, d_ub.as<float>(), m, nullptr, 0, m, 1 + n_MC, d_scal + 64 * 64 + (1 + n_MC));   // ‖u‖²
+    std::vector<double> h = d2h(g, d_scal + 64 * 64, 2 * (1 + n_MC));
+    double e0 = h[0], u0 = h[1 + n_MC], es = 0.0, us = 0.0;
+    for (int q = 1; q <= n_MC; ++q) {
+      es += h[q];
+      us += h[1 + n_MC + q];
+    }
+    return (float)std::log((u0 / e0) / (us / es));
+  };
+  if (verbose) printf("\nSecant iterations:\n");
+  float s2 = o.s2max / 2;
+  float log_tau1 = std::log((1 - s2) / s2);
+  float f1 = first_order(s2);
+  if (verbose) printf("  Iter 1: h2=%.4f log((1-h2)/h2)=%.4f funct=%.4f\n", s2, log_tau1, f1);
+  s2 = (f1 < 0) ? o.s2max / 4 : o.s2max;
+  float log_tau2 = std::log((1 - s2) / s2);
+  float f2 = first_order(s2);
+  if (verbose) printf("  Iter 2: h2=%.4f log((1-h2)/h2)=%.4f funct=%.4f\n", s2, log_tau2, f2);
+  for (int si = 3; si <= 9; ++si) {
+    float lt = (log_tau1 * f2 - log_tau2 * f1) / (f2 - f1);
+    if (lt > 9) lt = 9;
+    else if (lt < -9) lt = -9;
+    if (std::fabs(lt - log_tau2) < 0.002) break;
+    s2 = 1 / (std::exp(lt) + 1);
+    f1 = f2;
+    f2 = first_order(s2);
+    log_tau1 = log_tau2;
+    log_tau2 = lt;
+    if (verbose) printf("  Iter %d: h2=%.4f log((1-h2)/h2)=%.4f funct=%.4f\n", si, s2, lt, f2);
+  }
+  if (verbose && std::fabs(f2) > 0.005)
+    printf("\nWarning: secant iterations not converged. h2 close to 0 or small sample size?\n");
+  // Py = PyMC[:,0]; vg = y·Py/(n−c); ve = τ1·vg   (src/reml.cpp:855-858)
+  float* d_Py0 = d_Py.as<float>();
+  {
+    std::vector<float> hy(y, y + n);
+    upload(g, d_PV.as<float>(), hy.data(), n);
+  }
+  col_dots(g, d_PV.as<float>(), n, d_Py0, n, n, 1, d_scal);
+  const double yPy = d2h(g, d_scal, 1)[0];
+  const float vg = (float)(yPy / (double)(n - c));
+  const float tau1 = (1 - s2) / s2;
+  const float ve = tau1 * vg;
+  // snp_blup = W Z_cᵀ Py
+  op_device(g, SLEMM_OP_WRMATVEC, 0.f, d_Py0, n, 1, d_ub.as<float>(), m);
+  CUDA_TRY(cudaMemcpyAsync(Py_out, d_Py0, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(blup_out, d_ub.p, m * sizeof(float), cudaMemcpyDeviceToHost, st));
+  // BLUE: y − (Z_c b + τ1·R∘Py), then (XᵀX)⁻¹Xᵀ(·)   (src/reml.cpp:872-875)
+  float* d_zb = d_V.as<float>();   // reuse
+  op_device(g, SLEMM_OP_MATVEC, 0.f, d_ub.as<float>(), m, 1, d_zb, n);
+  {
+    std::vector<float> rv(n);
+    for (int64_t i = 0; i < n; ++i) rv[i] = rvec ? rvec[i] : 1.0f;
+    d_aux.ensure((size_t)n * 2 * sizeof(float));
+    upload(g, d_aux.as<float>(), rv.data(), n);
+    lmc_resid_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(d_PV.as<float>(), d_zb, d_aux.as<float>(), d_Py0,
+                                                                  tau1, n, d_aux.as<float>() + n);
+    LAUNCH_CHECK();
+  }
+  std::vector<float> resid(n);
+  CUDA_TRY(cudaMemcpyAsync(resid.data(), d_aux.as<float>() + n, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+  check_device_error(g);
+  {
+    std::vector<double> XtX((size_t)c * c, 0.0), Xtr(c, 0.0);
+    for (int a = 0; a < c; ++a) {
+      const float* xa = X + (size_t)a * ldx;
+      for (int b = 0; b <= a; ++b) {
+        const float* xb = X + (size_t)b * ldx;
+        double s = 0.0;
+        for (int64_t i = 0; i < n; ++i) s += (double)xa[i] * xb[i];
+        XtX[(size_t)b * c + a] = XtX[(size_t)a * c + b] = s;
+      }
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i) s += (double)xa[i] * resid[i];
+      Xtr[a] = s;
+    }
+    std::vector<double> blue = spd_solve(XtX, c, Xtr);
+    for (int a = 0; a < c; ++a) blue_out[a] = (float)blue[a];
+  }
+  if (verbose) {
+    printf("\nVg,%g\nVe,%g\nh2,%g\n", vg, ve, s2);
+    printf("\nCompleted Lanczos MC-REML.\n");
+    if (s2 > o.s2max)
+      printf("\nWarning: the h2 estimate is larger than the max you specified.\nCan rerun with a higher --max_heritability to gain accuracy.\n");
+  }
+  if (res) {
+    res->vg = vg;
+    res->ve = ve;
+    res->h2 = s2;
+    res->lrt = 0.f;
+    res->iters_y = res->iters_Q = 0;
+    res->iters_V = lseed_iters(seed_V, 0);
+    res->n_criterion = n_eval;
+    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  }
+}
+
+}  // namespace slemm
+
+using namespace slemm;
+
+extern "C" {
+
+int slemm_gpu_reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+                        const float* persnp, const slemm_reml_opts* opts, float* Py, float* snp_blup,
+                        float* blue, float* var_blue, slemm_reml_result* res)
+{
+  return guarded([&] {
+    CHECK_ARG(g && X && y && persnp && opts && Py && snp_blup && blue, "null argument");
+    CHECK_ARG(ldx >= g->n, "ldx < n");
+    CHECK_ARG(opts->s2max > opts->s2min && opts->s2min > 0 && opts->s2max < 1, "bad h2 bounds");
+    reml_sldf(g, rvec, X, ldx, c, y, persnp, *opts, Py, snp_blup, blue, var_blue, res);
+  });
+}
+
+int slemm_gpu_reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+                       const float* persnp, const slemm_reml_opts* opts, float* Py, float* snp_blup,
+                       float* blue, slemm_reml_result* res)
+{
+  return guarded([&] {
+    CHECK_ARG(g && X && y && persnp && opts && Py && snp_blup && blue, "null argument");
+    CHECK_ARG(ldx >= g->n, "ldx < n");
+    CHECK_ARG(opts->s2max > 0 && opts->s2max < 1, "bad h2 bound");
+    reml_lmc(g, rvec, X, ldx, c, y, persnp, *opts, Py, snp_blup, blue, res);
+  });
+}
+
+}  // extern "C"

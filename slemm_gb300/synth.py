@@ -1,0 +1,113 @@
+"""Seeded synthetic genotype/phenotype generator with the shapes of the benchmark workloads.
+
+Per SNP j the allele-2 frequency is p_j ~ U(0.05, 0.5); genotypes are Binomial(2, p_j), or, with
+``ld_rho > 0``, an AR(1) latent Gaussian along SNPs inside blocks of ``ld_block`` SNPs
+thresholded at the Binomial(2, p_j) quantiles.  ``missing`` sets that fraction of calls to the
+PLINK missing code 01.  The phenotype is y = Z_std·β + e with ``n_causal`` causal SNPs,
+β ~ N(0, h²/n_causal) and e ~ N(0, 1 − h²).
+
+PLINK .bed codes (SNP-major, 4 genotypes per byte, first genotype in the low bits):
+allele-2 count 0 → 00, 1 → 10, 2 → 11, missing → 01.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+BED_MAGIC = bytes([0x6C, 0x1B, 0x01])
+_CODE_OF_COUNT = np.array([0b00, 0b10, 0b11], dtype=np.uint8)
+
+
+def simulate_counts(n: int, m: int, seed: int = 1, ld_rho: float = 0.0, ld_block: int = 50,
+                    chunk: int = 2048):
+    """Returns (counts m×n uint8 in {0,1,2}, p m float64)."""
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(0.05, 0.5, size=m)
+    counts = np.empty((m, n), dtype=np.uint8)
+    if ld_rho <= 0.0:
+        for j0 in range(0, m, chunk):
+            j1 = min(m, j0 + chunk)
+            counts[j0:j1] = rng.binomial(2, p[j0:j1, None], size=(j1 - j0, n)).astype(np.uint8)
+        return counts, p
+    from scipy.special import ndtr
+    s = np.sqrt(1.0 - ld_rho * ld_rho)
+    z = np.empty(n)
+    for j in range(m):
+        if j % ld_block == 0:
+            z = rng.standard_normal(n)
+        else:
+            z = ld_rho * z + s * rng.standard_normal(n)
+        u = ndtr(z)
+        q0 = (1 - p[j]) ** 2
+        q1 = q0 + 2 * p[j] * (1 - p[j])
+        counts[j] = (u >= q0).astype(np.uint8) + (u >= q1).astype(np.uint8)
+    return counts, p
+
+
+def encode_bed(counts: np.ndarray, missing: float = 0.0, seed: int = 2) -> np.ndarray:
+    """m×n counts → m×ceil(n/4) .bed rows; a `missing` fraction of calls become code 01."""
+    m, n = counts.shape
+    codes = _CODE_OF_COUNT[counts]
+    if missing > 0:
+        rng = np.random.default_rng(seed)
+        codes = codes.copy()
+        codes[rng.random((m, n)) < missing] = 0b01
+    nb = (n + 3) // 4
+    pad = np.zeros((m, nb * 4), dtype=np.uint8)
+    pad[:, :n] = codes
+    pad = pad.reshape(m, nb, 4)
+    return (pad[:, :, 0] | (pad[:, :, 1] << 2) | (pad[:, :, 2] << 4) | (pad[:, :, 3] << 6)).astype(np.uint8)
+
+
+def counts_of_bed(rows: np.ndarray, n: int) -> np.ndarray:
+    """Vectorised decode with the missing→1 rule (bit0 + bit1 of each code)."""
+    m, nb = rows.shape
+    sh = np.array([0, 2, 4, 6], dtype=np.uint8)
+    codes = (rows[:, :, None] >> sh) & 3
+    codes = codes.reshape(m, nb * 4)[:, :n]
+    return ((codes & 1) + (codes >> 1)).astype(np.uint8)
+
+
+def simulate_phenotype(counts: np.ndarray, h2: float, n_causal: int = 1000, seed: int = 1):
+    """y = Z_std β + e (standardised causal genotypes), returns (y float64, causal idx, β)."""
+    m, n = counts.shape
+    rng = np.random.default_rng(seed + 7919)
+    n_causal = min(n_causal, m)
+    idx = np.sort(rng.choice(m, size=n_causal, replace=False))
+    beta = rng.normal(0.0, np.sqrt(h2 / n_causal), size=n_causal)
+    g = np.zeros(n)
+    for j, b in zip(idx, beta):
+        x = counts[j].astype(np.float64)
+        sd = x.std()
+        if sd > 0:
+            g += b * (x - x.mean()) / sd
+    e = rng.normal(0.0, np.sqrt(1.0 - h2), size=n)
+    return g + e, idx, beta
+
+
+def write_plink(prefix: str, rows: np.ndarray, n: int, chrom=None, snp_ids=None, iids=None,
+                a1="1", a2="2"):
+    """Writes prefix.bed/.bim/.fam.  Allele 2 (.bim column 6) is the counted allele."""
+    m = rows.shape[0]
+    os.makedirs(os.path.dirname(os.path.abspath(prefix)), exist_ok=True)
+    with open(prefix + ".bed", "wb") as f:
+        f.write(BED_MAGIC)
+        f.write(np.ascontiguousarray(rows, dtype=np.uint8).tobytes())
+    snp_ids = snp_ids if snp_ids is not None else [f"snp{j + 1}" for j in range(m)]
+    chrom = chrom if chrom is not None else [1 + (j * 30) // max(m, 1) for j in range(m)]
+    with open(prefix + ".bim", "w") as f:
+        for j in range(m):
+            f.write(f"{chrom[j]}\t{snp_ids[j]}\t0\t{1000 * (j + 1)}\t{a1}\t{a2}\n")
+    iids = iids if iids is not None else [f"{1000001 + i}" for i in range(n)]
+    with open(prefix + ".fam", "w") as f:
+        for i in range(n):
+            f.write(f"0 {iids[i]} 0 0 2 -9\n")
+    return snp_ids, iids
+
+
+def write_csv(path: str, header, columns):
+    with open(path, "w") as f:
+        f.write(",".join(header) + "\n")
+        for row in zip(*columns):
+            f.write(",".join("" if v is None else str(v) for v in row) + "\n")

@@ -1,0 +1,221 @@
+"""CPU checks of the oracle itself: pinned against the reference's own code and golden vectors,
+and against dense FP64 ground truth on tiny problems (known-answer tests)."""
+import json
+import math
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import slemm_np as orc
+from slemm_gb300 import synth
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+# ---- integer path --------------------------------------------------------------------------
+def test_bed_decode_known_answers():
+    """Hand-built bytes: codes LSB-first 00→0, 01 (missing)→1, 10→1, 11→2 (src/input.cpp:364-378)."""
+    rows = np.array([[0b11100100, 0b00000011]], dtype=np.uint8)   # codes 0,1,2,3 | 3,0,0,0
+    out = orc.bed_decode(rows, 5)
+    assert out.tolist() == [[0, 1, 1, 2, 2]]
+    keep = np.array([1, 0, 1, 0, 1], np.uint8)                   # skip individuals 1 and 3
+    assert orc.bed_decode(rows, 5, keep).tolist() == [[0, 1, 2]]
+    pc = orc.popcounts(out)
+    assert pc.tolist() == [6]
+    n0, n1, n2 = orc.hwe_counts(out)
+    assert (n0[0], n1[0], n2[0]) == (1, 2, 2)                     # missing counted as het
+
+
+def test_decode_matches_generator_encoding():
+    c, _ = synth.simulate_counts(333, 40, seed=5)
+    rows = synth.encode_bed(c)
+    assert np.array_equal(orc.bed_decode(rows, 333), c)
+    rows_m = synth.encode_bed(c, missing=0.1, seed=3)
+    d = orc.bed_decode(rows_m, 333)
+    assert np.array_equal(d, synth.counts_of_bed(rows_m, 333))
+    assert (d[c != d] == 1).all()                                 # every changed call became 1
+
+
+def test_maf_and_gm_are_fp32_like_reference():
+    pc = np.array([0, 1, 999, 1000, 1001, 2000], np.int64)
+    n = 1000
+    maf = orc.maf(pc, n)
+    f = (pc / np.float32(2 * n)).astype(np.float32)
+    expect = np.abs((f > 0.5).astype(np.float32) - f)
+    assert np.array_equal(maf, expect)
+    gm = orc.genotype_mean(pc, n)
+    assert np.array_equal(gm, (pc.astype(np.float32) / np.float32(n)).astype(np.float32))
+
+
+def test_rng_draws_match_golden():
+    """libstdc++ mt19937 draws of the reference's generators (reml.cpp:597-605, 795-809)."""
+    g = json.load(open(os.path.join(GOLD, "rng_draws.json")))
+    for seed in (0, 1, 42):
+        V = orc.rademacher(seed, 37, 3)
+        assert np.array_equal(np.sign(V).astype(int).T, np.array(g[f"rademacher_seed{seed}_n37_nv3"]))
+        assert np.allclose(np.linalg.norm(V, axis=0), 1.0, atol=1e-6)
+        u, e = orc.lmc_draws(seed, 11, 7, 2)
+        assert np.array_equal(u.T, np.array(g[f"lmc_seed{seed}_m11_n7_nmc2_u"], np.float32))
+        assert np.array_equal(e.T, np.array(g[f"lmc_seed{seed}_m11_n7_nmc2_e"], np.float32))
+
+
+def test_hwe_golden_fixture_sane():
+    """The fixture holds the reference SNPHWE2 outputs; p-values lie in (0, 1] and mid-p ≤ p."""
+    g = json.load(open(os.path.join(GOLD, "hwe_ref.json")))["cases"]
+    vals = {}
+    for het, h1, h2, midp, p in g:
+        assert 0.0 <= p <= 1.0 + 1e-12
+        vals[(het, h1, h2, midp)] = p
+    for (het, h1, h2, midp), p in vals.items():
+        if midp == 1:
+            assert p <= vals[(het, h1, h2, 0)] + 1e-12
+
+
+# ---- operators, Lanczos, SLQ: known answers -------------------------------------------------
+def _tiny(n=60, m=45, seed=1, c=2):
+    counts, _ = synth.simulate_counts(n, m, seed=seed)
+    pc = orc.popcounts(counts)
+    gm = orc.genotype_mean(pc, n)
+    rng = np.random.default_rng(seed)
+    gw = orc.snp_weights(gm, rng.uniform(0.5, 1.5, m).astype(np.float32), np.float64)
+    rr = rng.uniform(0.7, 1.3, n)
+    X = np.column_stack([np.ones(n), rng.standard_normal((n, c - 1))])
+    Q, qrR, rank = orc.qr_colpiv(rr[:, None] * X)
+    assert rank == c
+    return counts, gm.astype(np.float64), gw, rr, X, Q, qrR
+
+
+def test_operators_match_dense_fp64():
+    counts, gm, gw, rr, X, Q, _ = _tiny()
+    ops = orc.Operators(counts, gm, gw, rr, Q, subset_size=7, dtype=np.float64)
+    Z = counts.T.astype(np.float64) - gm
+    A = (rr[:, None] * Z) @ np.diag(gw) @ (Z.T * rr[None, :])
+    P = np.eye(Z.shape[0]) - Q @ Q.T
+    v = np.random.default_rng(2).standard_normal((Z.shape[0], 3))
+    tau0 = 0.37
+    assert np.allclose(ops.H0_quadform_mv(tau0, v), P @ A @ P @ v + tau0 * v - 0 * v, atol=1e-10)
+    assert np.allclose(ops.H0_ldet_mv(tau0, v), A @ v + tau0 * v, atol=1e-10)
+    assert np.allclose(ops.rmatvec(v), Z.T @ v, atol=1e-10)
+    assert np.allclose(ops.weighted_rmatvec(v), gw[:, None] * (Z.T @ v), atol=1e-10)
+    u = np.random.default_rng(3).standard_normal((Z.shape[1], 2))
+    assert np.allclose(ops.matvec(u), Z @ u, atol=1e-10)
+
+
+def test_lanczos_seed_and_shifted_solve_fp64():
+    counts, gm, gw, rr, X, Q, _ = _tiny()
+    ops = orc.Operators(counts, gm, gw, rr, Q, dtype=np.float64)
+    Z = counts.T.astype(np.float64) - gm
+    A = (rr[:, None] * Z) @ np.diag(gw) @ (Z.T * rr[None, :])
+    n = A.shape[0]
+    B = np.random.default_rng(4).standard_normal((n, 3))
+    tau0 = 0.25
+    seed = orc.L_Seed(ops, "ldet", tau0, B, tol=1e-12, maxit=400)
+    for sigma in (0.0, 0.3, 2.0):
+        X_ = orc.L_Solve(seed, B, sigma, tol=1e-11)
+        exact = np.linalg.solve(A + (tau0 + sigma) * np.eye(n), B)
+        assert np.allclose(X_, exact, rtol=1e-7, atol=1e-9)
+
+
+def test_slq_equals_exact_quadratic_form_with_full_krylov():
+    """With a complete Krylov basis, SLQ equals (n/n_V)·Σ vᵀ log(A+σI) v exactly."""
+    counts, gm, gw, rr, X, Q, _ = _tiny(n=40, m=30)
+    ops = orc.Operators(counts, gm, gw, rr, Q, dtype=np.float64)
+    Z = counts.T.astype(np.float64) - gm
+    A = (rr[:, None] * Z) @ np.diag(gw) @ (Z.T * rr[None, :])
+    n = A.shape[0]
+    V = orc.rademacher(0, n, 4).astype(np.float64)
+    tau0 = 0.5
+    seed = orc.L_Seed(ops, "ldet", tau0, V, tol=1e-13, maxit=n + 1)
+    D, W = orc.jacobi_eig(seed)
+    w, U = np.linalg.eigh(A + tau0 * np.eye(n))
+    for sigma in (0.0, 0.7):
+        L = U @ np.diag(np.log(w + sigma)) @ U.T
+        exact = n / 4 * sum(V[:, p] @ L @ V[:, p] for p in range(4))
+        assert math.isclose(orc.SLQ_LDet(D, W, n, 4, sigma), exact, rel_tol=1e-6)
+
+
+def test_reml_criterion_matches_dense_fp64():
+    """yᵀP̃y and log det(QᵀH⁻¹Q) of REML_criterion against dense FP64 algebra."""
+    counts, gm, gw, rr, X, Q, _ = _tiny()
+    ops = orc.Operators(counts, gm, gw, rr, Q, dtype=np.float64)
+    n = counts.shape[1]
+    y = np.random.default_rng(9).standard_normal(n)
+    yp = rr * y
+    yp = yp - Q @ (Q.T @ yp)
+    tau0 = (1 - 0.7) / 0.7
+    sy = orc.L_Seed(ops, "quadform", tau0, yp, tol=1e-12, maxit=300)
+    sq = orc.L_Seed(ops, "ldet", tau0, Q, tol=1e-12, maxit=300)
+    for h2 in (0.2, 0.5):
+        tau = (1 - h2) / h2
+        yPy = float(yp @ orc.L_Solve(sy, yp, tau - tau0, tol=1e-12)[:, 0])
+        M = Q.T @ orc.L_Solve(sq, Q, tau - tau0, tol=1e-12)
+        e_yPy, _, e_ld = orc.dense_reml_criterion(counts, gm, gw, rr, Q, yp, h2)
+        assert math.isclose(yPy, e_yPy, rel_tol=1e-8)
+        assert math.isclose(np.linalg.slogdet(M)[1], e_ld, rel_tol=1e-8, abs_tol=1e-8)
+
+
+def test_sldf_fp32_oracle_close_to_fp64_oracle():
+    """The FP32 restatement (reference arithmetic) and the FP64 oracle agree on h² within the
+    golden-section resolution: the search stops on a bracket of width (b−a)·0.618^nitr ≈ 7e-5 and
+    reports its last evaluated point, so two runs whose criteria differ by FP32 rounding can end
+    up to two brackets apart (3e-4 here, n = 400)."""
+    n, m = 400, 300
+    counts, _ = synth.simulate_counts(n, m, seed=11)
+    y, _, _ = synth.simulate_phenotype(counts, 0.5, n_causal=100, seed=11)
+    X = np.ones((n, 1))
+    r32 = orc.SLDF_REML(counts, None, X, y, np.ones(m), seed=1, n_V=10, dtype=np.float32)
+    r64 = orc.SLDF_REML(counts, None, X, y, np.ones(m), seed=1, n_V=10, dtype=np.float64)
+    assert abs(r32["h2"] - r64["h2"]) < 3e-4
+
+
+# ---- GWAS step 2 pinned by the reference script's own output ---------------------------------
+def test_gamma_oracle_matches_reference_script_output():
+    d = os.path.join(GOLD, "gamma_case")
+    n_fam = sum(1 for _ in open(os.path.join(d, "geno.fam")))
+    raw = np.fromfile(os.path.join(d, "geno.bed"), dtype=np.uint8)[3:]
+    rows = raw.reshape(-1, (n_fam + 3) // 4)
+    counts = orc.bed_decode(rows, n_fam)
+    py = [l.split() for l in open(os.path.join(d, "s1.reml.py.txt")).read().splitlines()[1:]]
+    Py = np.array([float(r[1]) for r in py], np.float32)
+    cov = np.array([[float(v) for v in r[2:-1]] for r in py], np.float32)
+    R = np.array([float(r[-1]) for r in py], np.float32)
+    rr = (1.0 / np.sqrt(R)).astype(np.float32)
+    from scipy import linalg
+    Q = linalg.qr(np.transpose(np.transpose(cov) * rr), mode="economic")[0]
+    xy, xx = orc.gamma_terms(counts, Py, rr, Q, mac=20)
+    gs = [l.split() for l in open(os.path.join(d, "s1.gstat.txt")).read().splitlines()[1:]]
+    cf = orc.mean_wo_outliers([float(r[9]) / float(r[7]) for r in gs])
+    vc = open(os.path.join(d, "s1.reml.vc.csv")).read().splitlines()
+    snp_var = float(vc[2].split(",")[1])
+    beta, se, chisq, p = orc.gamma_stats(xy, xx, cf, snp_var)
+    ref = [l.split("\t") for l in open(os.path.join(d, "gamma.txt")).read().splitlines()[1:]]
+    rb = np.array([float(r[6]) for r in ref])
+    rp = np.array([float(r[9]) for r in ref])
+    ok = np.isfinite(rb)
+    assert np.array_equal(ok, np.isfinite(beta))
+    assert np.allclose(beta[ok], rb[ok], rtol=2e-5, atol=1e-7)
+    assert np.max(np.abs(np.log10(p[ok]) - np.log10(rp[ok]))) < 1e-4
+
+
+# ---- window weighting -------------------------------------------------------------------------
+def test_window_weights_sliding_rule():
+    """option.cpp:505-511: sliding mean over window_size+1 SNPs with clamped ends, then the logistic."""
+    m, ws = 50, 10
+    rng = np.random.default_rng(0)
+    maf_v = rng.uniform(0.05, 0.5, m)
+    b = rng.standard_normal(m)
+    snpvar, w = orc.window_weights(maf_v, b, ws)
+    sv = 2 * maf_v.astype(np.float32) * (1 - maf_v.astype(np.float32)) * b.astype(np.float32) ** 2
+    sv = sv / sv.mean()
+    for i in (0, 4, 5, 25, 44, 45, 49):
+        if i < ws // 2:
+            seg = sv[: ws + 1]
+        elif i > m - ws // 2 - 1:
+            seg = sv[m - ws - 1:]
+        else:
+            seg = sv[i - ws // 2: i - ws // 2 + ws + 1]
+        x = seg.mean()
+        assert math.isclose(w[i], 0.001 / (0.001 + 0.999 * math.exp(-0.5 * x)), rel_tol=1e-5)
