@@ -1,0 +1,395 @@
+"""Benchmark of the GB300 engine on SLEMM's DF-REML + SNP-BLUP path.
+
+Workload (the benchmark's plain-FP32-vs-batched configuration): n = 100,000 individuals,
+m = 50,000 SNPs in a packed PLINK .bed (Binomial(2, p), p ~ U(0.05, 0.5), LD-free), h² = 0.4,
+one trait, intercept only; `slemm --reml --lrt` with 64 Rademacher probes (DF-REML: Lanczos seeds
+for y and [Q V], golden-section search on h², BLUP, BLUE).  Synthetic data, seed 1.
+
+One step = one REML + BLUP fit through the C ABI.
+  value  — device-timed (CUDA events on the library stream) wall time of one fit with the
+           packed genotypes already resident in HBM (packed Z is 1.25 GB ≫ the 129 MB L2, so
+           every pass streams from HBM);
+  e2e    — the same fit through the reference-facing calls with HOST buffers: genotype upload
+           from pinned host memory + fit + results back to the host, timed on the host;
+  roofline — the dominant packed-product kernel, measured per launch with CUDA events during
+           the timed steps;
+  cpu_baseline — the NumPy FP32 restatement of the reference operators on this host's cores,
+           timed on a bounded sample and extrapolated with the fit's Lanczos step counts.
+`--impl reference` times the reference's CPU path (the oracle port; the reference itself does
+not build here) on the same workload, on this host's cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "REML wall time + genotype-matvec GB/s, mixed-prec vs FP32 on GB300 at dh2<=1e-4"
+CONFIGS = {
+    1: dict(n=2000, m=10000, probes=30, h2=0.5, missing=0.01,
+            name="n=2000 m=10000, 1% missing, 30 Rademacher probes, DF-REML + BLUP"),
+    2: dict(n=100000, m=50000, probes=64, h2=0.4, missing=0.0,
+            name="n=100000 m=50000, 64 Rademacher probes in one block, DF-REML + BLUP"),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return dict(hbm=float(p["hbm_gbs"]), bf16=float(p["bf16_tflops"]),
+                    bf16_sus=float(p["bf16_tflops_sustained"]), src="measured")
+    except Exception:
+        return dict(hbm=6800.0, bf16=1900.0, bf16_sus=1700.0, src="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(cfg, device="cuda"):
+    from slemm_gb300 import synth
+    rows, y = synth.simulate_bed_torch(cfg["n"], cfg["m"], seed=1, h2=cfg["h2"], missing=cfg["missing"],
+                                       device=device)
+    n, m = cfg["n"], cfg["m"]
+    X = np.ones((n, 1), np.float32)
+    persnp = np.ones(m, np.float32)
+    return rows, y.astype(np.float32), X, persnp
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU path (oracle port): bounded sample of operator applications, extrapolated
+# ------------------------------------------------------------------------------------------------
+def cpu_operator_sample(rows_np, n, m, probes, subsets=4):
+    """Times H0_ldet_mv on the [Q V] block (1 + probes columns) and H0_quadform_mv on y over
+    `subsets` SNP subsets of 1000 and scales to all m SNPs.  Returns (s_ldet, s_quad, info)."""
+    from oracle import slemm_np as orc
+    rng = np.random.default_rng(0)
+    gm = rng.uniform(0.1, 0.9, m).astype(np.float32)     # values do not change the timing
+    w = np.full(m, 1.0 / m, np.float32)
+    Q = np.full((n, 1), 1.0 / np.sqrt(n), np.float32)
+    ops = orc.PackedOperators(rows_np, n, gm, w, None, Q, subset_size=1000, dtype=np.float32)
+    ops.subset_limit = subsets
+    scale = (m / 1000.0) / subsets
+    V = rng.standard_normal((n, 1 + probes)).astype(np.float32)
+    t0 = time.perf_counter()
+    ops.H0_ldet_mv(0.4285714, V)
+    s_ldet = (time.perf_counter() - t0) * scale
+    v = V[:, :1].copy()
+    t0 = time.perf_counter()
+    ops.H0_quadform_mv(0.4285714, v)
+    s_quad = (time.perf_counter() - t0) * scale
+    info = f"{subsets} subsets of 1000 SNPs × {n} individuals per operator, scaled ×{scale:.1f}"
+    return s_ldet, s_quad, info
+
+
+def cpu_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        return max(i.get("num_threads", 1) for i in threadpool_info()) or os.cpu_count()
+    except Exception:
+        return os.cpu_count()
+
+
+def run_reference(args, cfg):
+    """CPU reference arm: the oracle port of the reference's DF-REML on this host."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import slemm_np as orc
+    from slemm_gb300 import synth
+    n, m, probes = cfg["n"], cfg["m"], cfg["probes"]
+    # packed rows for the timing sample (NumPy generator; values do not affect CPU time)
+    rng = np.random.default_rng(1)
+    nb = (n + 3) // 4
+    rows_np = rng.integers(0, 256, size=(min(m, 4000), nb), dtype=np.uint8)   # timing only
+    # Lanczos step counts of the reference algorithm from a ratio-preserving 1/10 problem
+    small_n, small_m = max(n // 10, 500), max(m // 10, 500)
+    counts, _ = synth.simulate_counts(small_n, small_m, seed=1)
+    y, _, _ = synth.simulate_phenotype(counts, cfg["h2"], n_causal=min(1000, small_m), seed=1)
+    t0 = time.perf_counter()
+    rr = orc.SLDF_REML(counts, None, np.ones((small_n, 1)), y, np.ones(small_m), seed=0, n_V=probes,
+                       dtype=np.float32)
+    it_y, it_q, it_v = rr["iters"]
+    vals = []
+    for s in range(args.warmup + args.steps):
+        s_ldet, s_quad, info = cpu_operator_sample(rows_np, n, min(m, 4000), probes, subsets=2)
+        s_ldet *= m / min(m, 4000)
+        s_quad *= m / min(m, 4000)
+        est = max(it_q, it_v) * s_ldet + it_y * s_quad
+        if s >= args.warmup:
+            vals.append(est)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": cpu_threads(), "kind": "port",
+                         "sample": f"{info}; Lanczos steps (y {it_y}, Q {it_q}, V {it_v}) from the "
+                                   f"reference algorithm run in full on an n={small_n}, m={small_m} "
+                                   f"problem with the same n/m ratio"},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+def run_gpu(args, cfg):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from slemm_gb300 import api, _lib
+    api.init(local)
+    n, m, probes = cfg["n"], cfg["m"], cfg["probes"]
+    rows, y, X, persnp = make_inputs(cfg)
+    rows_np = rows.numpy()
+    opts = dict(seed=0, n_V=probes)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    g = api.Genotypes(rows_np, n)
+    stream = torch.cuda.ExternalStream(g.stream())
+    g.set_precision(_lib.PREC_BF16X2)
+    for _ in range(args.warmup):
+        r = g.SLDF_REML(None, X, y, persnp, **opts)
+    # ---- timed: REML + BLUP with genotypes resident ----
+    launches0 = api.launch_count()
+    _prof(g, 1)
+    times, res = [], None
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = g.SLDF_REML(None, X, y, persnp, **opts)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        barrier()
+    launches = api.launch_count() - launches0
+    prof = _prof(g, 0)
+    mean_step = statistics.mean(times)
+    if dist is not None:
+        tt = torch.tensor([mean_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        mean_step = float(tt.item())
+    # ---- e2e: host buffers through the reference-facing calls ----
+    e2e_times = []
+    for _ in range(max(2, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with api.Genotypes(rows_np, n) as g2:
+            g2.set_precision(_lib.PREC_BF16X2)
+            r2 = g2.SLDF_REML(None, X, y, persnp, **opts)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]
+    h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes
+    d2h = (n + m + 1 + 1) * 4
+    # ---- plain FP32 per-vector GPU path (the comparison the metric names), one fit ----
+    fp32 = None
+    if not args.skip_fp32:
+        g.set_precision(_lib.PREC_FP32)
+        g.set_per_vector(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rf = g.SLDF_REML(None, X, y, persnp, **opts)
+        torch.cuda.synchronize()
+        fp32 = {"s": time.perf_counter() - t0, "h2": rf["h2"], "iters": list(rf["iters"])}
+        g.set_per_vector(False)
+        g.set_precision(_lib.PREC_BF16X2)
+    # ---- roofline of the dominant packed-product launch shape ----
+    pk = peaks()
+    dom = max(prof, key=lambda r: r["ms"]) if prof else None
+    roof = None
+    matvec_gbs = None
+    if dom:
+        k = dom["k"]
+        t_launch = dom["ms"] / dom["launches"] / 1e3
+        packed = m * ((n + 3) // 4)
+        bytes_alg = packed + 4 * n * k + 4 * m * k
+        flops_alg = 2.0 * n * m * k
+        ach_tf = flops_alg / t_launch / 1e12
+        exe_tf = 2.0 * n * m * dom["N"] / t_launch / 1e12 if dom["tc"] else ach_tf
+        gbs = bytes_alg / t_launch / 1e9
+        matvec_gbs = packed / t_launch / 1e9
+        traffic = _traffic(dom)
+        tensor = dom["tc"] == 1
+        roof = {
+            "bound": "tensor" if tensor else "hbm",
+            "achieved": ach_tf if tensor else gbs,
+            "peak": pk["bf16_sus"] if tensor else pk["hbm"],
+            "unit": "TFLOP/s" if tensor else "GB/s",
+            "frac": (ach_tf / pk["bf16_sus"]) if tensor else gbs / pk["hbm"],
+            "traffic": traffic,
+            "kernel": "gemm_tc_kernel" if tensor else "gemm_simt_kernel",
+            "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],
+                       "direction": "Z^T U (M=SNPs)" if dom["dir"] == 1 else "Z V (M=individuals)",
+                       "avg_ms": t_launch * 1e3, "launches": dom["launches"]},
+            "executed_tflops": exe_tf, "frac_executed": exe_tf / pk["bf16_sus"],
+            "algorithmic_gbs": gbs, "frac_hbm": gbs / pk["hbm"],
+            "peak_source": f"{pk['src']} (bf16 sustained, MEASURED_PEAKS.json)" if pk["src"] == "measured" else "fallback",
+            "shapes": prof,
+        }
+    # ---- CPU baseline (oracle port), rank 0, N = 1 only ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        s_ldet, s_quad, info = cpu_operator_sample(rows_np, n, m, probes, subsets=args.cpu_subsets)
+        it_y, it_q, it_v = res["iters"]
+        est = max(it_q, it_v) * s_ldet + it_y * s_quad
+        cpu = {"value": est, "unit": "s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"{info}; REML time = {max(it_q, it_v)}·t(ldet, {1 + probes} cols) + "
+                         f"{it_y}·t(quadform, 1 col) with this fit's Lanczos step counts"}
+    line = {
+        "metric": METRIC, "value": mean_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "h2_sim": cfg["h2"],
+                   "precision": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars",
+                   "l2": "inputs larger than L2 (packed Z 1.25 GB per pass)", "parallelism": "replicas"},
+        "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
+        "lanczos_steps": {"y": res["iters"][0], "Q": res["iters"][1], "V": res["iters"][2]},
+        "matvec_gbs": matvec_gbs,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches / max(args.steps, 1)),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    if fp32:
+        line["fp32_per_vector"] = fp32
+        line["speedup_vs_fp32_per_vector"] = fp32["s"] / mean_step
+        line["dh2_vs_fp32"] = abs(fp32["h2"] - res["h2"])
+    g.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _prof(g, enable):
+    import ctypes
+    from slemm_gb300 import _lib
+    lib = _lib.load()
+    rows = ctypes.c_int(0)
+    info = (ctypes.c_int32 * (5 * 64))()
+    la = (ctypes.c_int64 * 64)()
+    ms = (ctypes.c_double * 64)()
+    _lib.check(lib.slemm_gpu_profile(g.h, enable, 64, ctypes.byref(rows), info, la, ms))
+    out = []
+    for r in range(min(rows.value, 64)):
+        out.append({"tc": info[5 * r], "N": info[5 * r + 1], "k": info[5 * r + 2],
+                    "pieces": info[5 * r + 3], "dir": info[5 * r + 4], "launches": int(la[r]),
+                    "ms": float(ms[r])})
+    return out
+
+
+def _traffic(dom):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            t = json.load(f)
+        key = f"tc{dom['tc']}_N{dom['N']}_dir{dom['dir']}"
+        return t.get(key)
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS))
+    ap.add_argument("--skip-fp32", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-subsets", type=int, default=3)
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        from slemm_gb300 import build
+        build.build()
+        run_gpu(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -169,6 +169,15 @@ int slemm_gpu_gebv(slemm_geno* g, const double* alpha, const uint8_t* flip, doub
  * come from the handle.  Outputs xy, xx (m, host). */
 int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, float* xx);
 
+/* ---- measurement ---------------------------------------------------------------------------------- */
+/* Per-launch timing of the packed products with CUDA events on the handle's stream (no
+ * counterpart in the reference, which only prints wall-clock times, src/option.cpp:21-34).
+ * Reads the statistics gathered so far (rows of info = {tc, N, k, pieces, dir}, launch count,
+ * total ms), then: enable = 1 clears and starts recording, 0 clears and stops, −1 leaves the
+ * state as it is.  *rows receives the number of distinct launch shapes. */
+int slemm_gpu_profile(slemm_geno* g, int enable, int max_rows, int* rows, int32_t* info,
+                      int64_t* launches, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

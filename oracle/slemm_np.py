@@ -219,6 +219,38 @@ class Operators:
         return out
 
 
+class PackedOperators(Operators):
+    """Same operators, decoding each `subset_size` block straight from the packed .bed rows of
+    the kept individuals (all individuals here), as the reference decodes kmat bits per subset
+    (src/reml.cpp:29-35) — used for the timed CPU baseline at full sizes."""
+
+    def __init__(self, bed_rows, n, gm, w, rr=None, Q=None, subset_size=1000, dtype=np.float32):
+        self.rows = bed_rows
+        self.m, self.n = bed_rows.shape[0], n
+        self.dt = dtype
+        self.gm = np.asarray(gm, dtype=dtype)
+        self.w = np.asarray(w, dtype=dtype)
+        self.rr = np.ones(n, dtype) if rr is None else np.asarray(rr, dtype=dtype)
+        self.Q = np.zeros((n, 0), dtype) if Q is None else np.asarray(Q, dtype=dtype)
+        self.s = int(subset_size)
+        # byte → 4 counts LUT (missing code 01 → 1, like b[k]+b[k+1])
+        codes = (np.arange(256)[:, None] >> np.array([0, 2, 4, 6])) & 3
+        self._lut4 = ((codes & 1) + (codes >> 1)).astype(dtype)
+        self.subset_limit = None
+
+    def _subsets(self):
+        nb = (self.n + 3) // 4
+        count = 0
+        for i0 in range(0, self.m, self.s):
+            if self.subset_limit is not None and count >= self.subset_limit:
+                return
+            i1 = min(self.m, i0 + self.s)
+            blk = np.asarray(self.rows[i0:i1, :nb])
+            Zc = self._lut4[blk].reshape(i1 - i0, nb * 4)[:, : self.n].T - self.gm[i0:i1]
+            count += 1
+            yield i0, i1, Zc
+
+
 # ------------------------------------------------------------------------------------------
 # Lanczos seed / solve / SLQ (src/reml.cpp:240-451)
 # ------------------------------------------------------------------------------------------

@@ -61,6 +61,7 @@ _SIGS = {
                                  ctypes.POINTER(RemlResult)]),
     "slemm_gpu_gebv": (I32, [P, P, P, P]),
     "slemm_gpu_score_terms": (I32, [P, P, I32, P, P]),
+    "slemm_gpu_profile": (I32, [P, I32, I32, ctypes.POINTER(I32), P, P, P]),
 }
 
 _LIB = None

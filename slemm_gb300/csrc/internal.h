@@ -22,6 +22,20 @@ struct slemm_geno {
   // work buffers
   slemm::DevBuf ws_B, ws_D, ws_red, ws_small, ws_T, ws_in, ws_out;
   slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
+  // optional per-launch timing of the packed products (CUDA events on `stream`)
+  struct GemmRecord {
+    cudaEvent_t start, stop;
+    int tc, N, k, pieces, splits, dir;   // dir 1: Zᵀ pass (M = SNPs), 2: Z pass (M = individuals)
+  };
+  bool profiling = false;
+  std::vector<GemmRecord> prof_pending;
+  std::vector<cudaEvent_t> event_pool;
+  struct GemmStat {
+    int tc, N, k, pieces, dir;
+    int64_t launches;
+    double ms;
+  };
+  std::vector<GemmStat> prof_stats;
 };
 
 namespace slemm {
@@ -57,5 +71,6 @@ void lseed_free(slemm_lseed* S);
 int64_t workspace_bytes(const slemm_geno* g);
 // Reads (and clears) the device error word; throws if a kernel gave up a bounded wait.
 void check_device_error(slemm_geno* g);
+void profile_collect(slemm_geno* g);
 
 }  // namespace slemm

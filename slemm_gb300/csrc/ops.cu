@@ -303,12 +303,56 @@ static int max_group(const slemm_geno* g)
   return 64;
 }
 
+static cudaEvent_t take_event(slemm_geno* g)
+{
+  if (!g->event_pool.empty()) {
+    cudaEvent_t e = g->event_pool.back();
+    g->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  CUDA_TRY(cudaEventCreate(&e));
+  return e;
+}
+
+// Folds completed launch records into the per-shape statistics (synchronises on the events).
+void profile_collect(slemm_geno* g)
+{
+  for (auto& r : g->prof_pending) {
+    CUDA_TRY(cudaEventSynchronize(r.stop));
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, r.start, r.stop));
+    bool found = false;
+    for (auto& s : g->prof_stats)
+      if (s.tc == r.tc && s.N == r.N && s.k == r.k && s.dir == r.dir && s.pieces == r.pieces) {
+        s.launches += 1;
+        s.ms += ms;
+        found = true;
+        break;
+      }
+    if (!found) g->prof_stats.push_back({r.tc, r.N, r.k, r.pieces, r.dir, 1, (double)ms});
+    g->event_pool.push_back(r.start);
+    g->event_pool.push_back(r.stop);
+  }
+  g->prof_pending.clear();
+}
+
 static void run_gemm(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t M_pad,
-                     int64_t K_pad, const void* B, float* D, int* err)
+                     int64_t K_pad, const void* B, float* D, int* err, int k, int dir)
 {
   GemmArgs a{A, M_pad, K_pad, B, p.N, D, p.splits, err};
+  slemm_geno::GemmRecord rec{};
+  if (g->profiling) {
+    if (g->prof_pending.size() >= 512) profile_collect(g);
+    rec = {take_event(g), take_event(g), p.tc ? 1 : 0, p.N, k, p.pieces, p.splits, dir};
+    CUDA_TRY(cudaEventRecord(rec.start, g->stream));
+  }
   if (p.tc) gemm_tc(a, g->stream);
   else gemm_simt(a, g->stream);
+  if (g->profiling) {
+    CUDA_TRY(cudaEventRecord(rec.stop, g->stream));
+    g->prof_pending.push_back(rec);
+  }
 }
 
 // Device scratch: small FP64 vectors + error word.
@@ -381,7 +425,7 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     LAUNCH_CHECK();
     reduce_partials(red, nblk_n, k, sm.colsum, st);
     // ---- pass 1: Cntᵀ over individuals ----
-    run_gemm(g, p1, g->G.as<uint8_t>(), g->m_pad, g->n_pad, B1, D, sm.err);
+    run_gemm(g, p1, g->G.as<uint8_t>(), g->m_pad, g->n_pad, B1, D, sm.err, k, 1);
     // ---- finalize 1 ----
     dim3 gridm(nblk_m, k);
     const float* wsc = (kind == SLEMM_OP_RMATVEC) ? nullptr : g->w.as<float>();
@@ -407,7 +451,7 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     reduce_partials(red, nblk_m, k, sm.tsum, st);
   }
   // ---- pass 2: Cnt over SNPs ----
-  run_gemm(g, p2, g->GT.as<uint8_t>(), g->n_pad, g->m_pad, B2, D, sm.err);
+  run_gemm(g, p2, g->GT.as<uint8_t>(), g->n_pad, g->m_pad, B2, D, sm.err, k, 2);
   // ---- finalize 2 ----
   dim3 gridn((unsigned)ceil_div(g->n, 256), k);
   if (kind == SLEMM_OP_MATVEC) {
@@ -491,5 +535,32 @@ extern "C" int slemm_gpu_op(slemm_geno* g, int op_kind, float tau0, const float*
     CUDA_TRY(cudaMemcpy2DAsync(out, ld_out * sizeof(float), dout, rows_out * sizeof(float),
                                rows_out * sizeof(float), k, cudaMemcpyDeviceToHost, g->stream));
     check_device_error(g);
+  });
+}
+
+extern "C" int slemm_gpu_profile(slemm_geno* g, int enable, int max_rows, int* rows, int32_t* info,
+                                 int64_t* launches, double* ms)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    profile_collect(g);
+    int r = 0;
+    for (const auto& s : g->prof_stats) {
+      if (r < max_rows && info && launches && ms) {
+        info[5 * r + 0] = s.tc;
+        info[5 * r + 1] = s.N;
+        info[5 * r + 2] = s.k;
+        info[5 * r + 3] = s.pieces;
+        info[5 * r + 4] = s.dir;
+        launches[r] = s.launches;
+        ms[r] = s.ms;
+      }
+      ++r;
+    }
+    if (rows) *rows = r;
+    if (enable >= 0) {
+      g->prof_stats.clear();
+      g->profiling = enable != 0;
+    }
   });
 }

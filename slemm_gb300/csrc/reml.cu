@@ -532,7 +532,9 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
   d_PV.ensure((size_t)n * tV * sizeof(float));
   d_Py.ensure((size_t)n * (1 + n_MC) * sizeof(float));
   d_ub.ensure((size_t)m * (1 + n_MC) * sizeof(float));
-  d_tmp.ensure((size_t)(64 * 64 + 4 * tV) * sizeof(double));
+  // scratch: c×tV projection coefficients first, then 4·tV norms from offset 64·64 (or later)
+  const size_t scal_off = std::max<size_t>(64 * 64, (size_t)c * tV);
+  d_tmp.ensure((scal_off + 4 * (size_t)tV) * sizeof(double));
   double* d_scal = d_tmp.as<double>();
   upload(g, d_V.as<float>(), V.data(), (size_t)n * tV);
   upload(g, d_u.as<float>(), u.data(), (size_t)m * n_MC);
@@ -562,12 +564,12 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
     LAUNCH_CHECK();
     proj_coeffs(g, d_Py.as<float>(), n, 1 + n_MC, d_scal);
     proj_apply(g, d_Py.as<float>(), n, 1 + n_MC, d_scal);
-    col_dots(g, d_Py.as<float>(), n, nullptr, 0, n, 1 + n_MC, d_scal + 64 * 64);              // ‖e‖²
+    col_dots(g, d_Py.as<float>(), n, nullptr, 0, n, 1 + n_MC, d_scal + scal_off);              // ‖e‖²
     scale_rows(g, d_Py.as<float>(), n, n, 1 + n_MC, g->rr.as<float>());
     op_device(g, SLEMM_OP_RMATVEC, 0.f, d_Py.as<float>(), n, 1 + n_MC, d_ub.as<float>(), m);
     scale_rows(g, d_ub.as<float>(), m, m, 1 + n_MC, g->w.as<float>(), true);
-    col_dots(g, d_ub.as<float>(), m, nullptr, 0, m, 1 + n_MC, d_scal + 64 * 64 + (1 + n_MC));   // ‖u‖²
-    std::vector<double> h = d2h(g, d_scal + 64 * 64, 2 * (1 + n_MC));
+    col_dots(g, d_ub.as<float>(), m, nullptr, 0, m, 1 + n_MC, d_scal + scal_off + (1 + n_MC));   // ‖u‖²
+    std::vector<double> h = d2h(g, d_scal + scal_off, 2 * (1 + n_MC));
     double e0 = h[0], u0 = h[1 + n_MC], es = 0.0, us = 0.0;
     for (int q = 1; q <= n_MC; ++q) {
       es += h[q];

@@ -111,3 +111,46 @@ def write_csv(path: str, header, columns):
         f.write(",".join(header) + "\n")
         for row in zip(*columns):
             f.write(",".join("" if v is None else str(v) for v in row) + "\n")
+
+
+def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal: int = 1000,
+                       missing: float = 0.0, device: str = "cuda", chunk: int = 2048):
+    """Device-side generator for benchmark-sized inputs (same model as the NumPy path, torch's
+    RNG): returns (.bed rows as a pinned host uint8 tensor m×ceil(n/4), y float32 numpy).
+    Torch is used only as a random-number and memory utility here."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    nb = (n + 3) // 4
+    rows = torch.empty((m, nb), dtype=torch.uint8, pin_memory=True)
+    p = torch.rand(m, generator=gen, device=device, dtype=torch.float64) * 0.45 + 0.05
+    code_of = torch.tensor([0b00, 0b10, 0b11], dtype=torch.uint8, device=device)
+    causal = torch.randperm(m, generator=gen, device=device)[: min(n_causal, m)]
+    causal_sorted, _ = torch.sort(causal)
+    beta = torch.randn(causal_sorted.numel(), generator=gen, device=device, dtype=torch.float64) * \
+        (h2 / max(causal_sorted.numel(), 1)) ** 0.5
+    g = torch.zeros(n, dtype=torch.float64, device=device)
+    shifts = torch.tensor([0, 2, 4, 6], dtype=torch.uint8, device=device)
+    for j0 in range(0, m, chunk):
+        j1 = min(m, j0 + chunk)
+        pj = p[j0:j1, None]
+        u1 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
+        u2 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
+        cnt = (u1 < pj).to(torch.uint8) + (u2 < pj).to(torch.uint8)       # Binomial(2, p)
+        sel = (causal_sorted >= j0) & (causal_sorted < j1)
+        if bool(sel.any()):
+            idx = causal_sorted[sel] - j0
+            x = cnt[idx].to(torch.float64)
+            sd = x.std(dim=1, unbiased=False).clamp_min(1e-12)
+            g += (beta[sel, None] * (x - x.mean(dim=1, keepdim=True)) / sd[:, None]).sum(0)
+        codes = code_of[cnt.long()]
+        if missing > 0:
+            miss = torch.rand((j1 - j0, n), generator=gen, device=device) < missing
+            codes = torch.where(miss, torch.ones_like(codes), codes)
+        pad = torch.zeros((j1 - j0, nb * 4), dtype=torch.uint8, device=device)
+        pad[:, :n] = codes
+        packed = (pad.view(j1 - j0, nb, 4) << shifts).sum(dim=2, dtype=torch.uint8)
+        rows[j0:j1].copy_(packed, non_blocking=False)
+    e = torch.randn(n, generator=gen, device=device, dtype=torch.float64) * (1.0 - h2) ** 0.5
+    y = (g + e).float().cpu().numpy()
+    return rows, y
