@@ -169,6 +169,20 @@ int slemm_gpu_gebv(slemm_geno* g, const double* alpha, const uint8_t* flip, doub
  * come from the handle.  Outputs xy, xx (m, host). */
 int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, float* xx);
 
+/* ---- operator without device allocation ----------------------------------------------------------- */
+/* No counterpart in the reference.  out (m×k) = Z_cᵀ v (n×k) on the FP32 CUDA-core path, the same
+ * product as slemm_gpu_op(SLEMM_OP_RMATVEC), for callers that cannot allocate device memory (a
+ * framework that has reserved the GPU's memory for its own pool, or a loop where cudaMalloc's
+ * device-wide synchronisation is not allowed).  v and out are device pointers; the call allocates
+ * nothing and returns without synchronising (work queued on the handle's stream).  Its scratch is
+ * one static device array of SLEMM_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library;
+ * calls needing more (about 4·k·(n + m) bytes plus split-K partials) fail with
+ * SLEMM_ERR_UNSUPPORTED.  The first call on a device looks up the array's address — make it
+ * before any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+#define SLEMM_NOALLOC_SCRATCH_BYTES (32u << 20)
+int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t ldv, int k, float* out,
+                              int64_t ldo);
+
 /* ---- measurement ---------------------------------------------------------------------------------- */
 /* Per-launch timing of the packed products with CUDA events on the handle's stream (no
  * counterpart in the reference, which only prints wall-clock times, src/option.cpp:21-34).
