@@ -249,7 +249,7 @@ def run_gpu(args, cfg):
         mean_step = float(tt.item())
     # ---- e2e: host buffers through the reference-facing calls ----
     e2e_times = []
-    for _ in range(max(2, args.steps)):
+    for _ in range(0 if args.skip_e2e else max(2, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with api.Genotypes(rows_np, n) as g2:
@@ -257,7 +257,7 @@ def run_gpu(args, cfg):
             r2 = g2.SLDF_REML(None, X, y, persnp, **opts)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    e2e = statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]
+    e2e = (statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]) if e2e_times else None
     h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes
     d2h = (n + m + 1 + 1) * 4
     # ---- plain FP32 per-vector GPU path (the comparison the metric names), one fit ----
@@ -371,8 +371,45 @@ def _traffic(dom):
         return None
 
 
+def run_kernel_case(args):
+    """Small profiling case for ncu: n = 40,000, m = 20,000 (each packed copy 200 MB, above the
+    129 MB L2), H0_ldet_mv on a 65-column block: 3 warm-up applications, then 2 timed (each is
+    one Zᵀ and one Z pass, i.e. 2 gemm_tc_kernel launches)."""
+    import torch
+    from slemm_gb300 import api, _lib, synth
+    torch.cuda.set_device(0)
+    api.init(0)
+    n, m, k = 40000, 20000, 65
+    rows, _ = synth.simulate_bed_torch(n, m, seed=3)
+    rows_np = rows.numpy()
+    g = api.Genotypes(rows_np, n)
+    gm = np.full(m, 0.55, np.float32)
+    w = np.full(m, 1.0 / m, np.float32)
+    g.set_weights(gm, w)
+    g.set_precision(_lib.PREC_BF16X3 if args.kernel_prec == 3 else _lib.PREC_BF16X2)
+    v = torch.randn(k, n, device="cuda")
+    out = torch.empty(k, n, device="cuda")
+    for _ in range(3):
+        g.op_device(_lib.OP_LDET, v, out, 0.4285714)
+    stream = torch.cuda.ExternalStream(g.stream())
+    _prof(g, 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(2):
+        g.op_device(_lib.OP_LDET, v, out, 0.4285714)
+    e1.record(stream)
+    e1.synchronize()
+    prof = _prof(g, 0)
+    print(json.dumps({"case": "kernel", "n": n, "m": m, "k": k, "op_ms": e0.elapsed_time(e1) / 2,
+                      "shapes": prof}), flush=True)
+    g.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel-case", action="store_true", help="small operator case for ncu captures")
+    ap.add_argument("--kernel-prec", type=int, default=2, choices=[2, 3])
+    ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -383,6 +420,11 @@ def main():
     ap.add_argument("--cpu-subsets", type=int, default=3)
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
+    if args.kernel_case:
+        from slemm_gb300 import build
+        build.build()
+        run_kernel_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

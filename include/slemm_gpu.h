@@ -119,6 +119,12 @@ int slemm_gpu_lseed_coeffs(const slemm_lseed* s, double* beta, double* delta);
 int slemm_gpu_lanczos_solve(slemm_lseed* s, float sigma, float tol, float* X, int64_t ldx,
                             int mem);
 
+/* ---- probes (src/reml.cpp:597-605) ------------------------------------------------------------ */
+/* The reference's normalised Rademacher block: V (n×n_V, column-major, ld) gets ±1/√n with the
+ * signs of std::mt19937(seed + 54321) + uniform_real_distribution<float>(0,1) < 0.5, draw for
+ * draw, generated on the GPU.  mem selects a host or device V. */
+int slemm_gpu_rademacher(int seed, int64_t n, int n_V, float* V, int64_t ldv, int mem);
+
 /* ---- batched tridiagonal eigensolve + SLQ (src/reml.cpp:440-451, 638-646) -------------- */
 /* For t Jacobi matrices (diag delta t×nld, off-diag beta t×(nld+1) with beta[:,1:nld] used),
  * returns eigenvalues D (t×nld) and squared first eigenvector components W2 (t×nld), FP64,

@@ -62,6 +62,7 @@ _SIGS = {
     "slemm_gpu_gebv": (I32, [P, P, P, P]),
     "slemm_gpu_score_terms": (I32, [P, P, I32, P, P]),
     "slemm_gpu_profile": (I32, [P, I32, I32, ctypes.POINTER(I32), P, P, P]),
+    "slemm_gpu_rademacher": (I32, [I32, I64, I32, P, I64, I32]),
 }
 
 _LIB = None

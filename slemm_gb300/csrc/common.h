@@ -72,6 +72,7 @@ inline void count_launch(int k = 1) { g_launches.fetch_add(k, std::memory_order_
 constexpr int kTileM = 128;          // rows of one packed tile (M of one MMA)
 constexpr int kTileK = 64;           // K elements of one packed tile (one 128-B bf16 row)
 constexpr int kTileBytes = kTileM * kTileK / 4;   // 2048 packed bytes per tile
+constexpr int kPadRows = 256;        // n and m are padded to this (two row tiles per TC CTA)
 __host__ __device__ inline int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
 __host__ __device__ inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }

@@ -1,18 +1,29 @@
-// decode.cuh — 2-bit plane-encoded counts → BF16 / FP32 (device helpers shared by the kernels).
+// decode.cuh — 2-bit packed counts → BF16 / FP32 (device helpers shared by the kernels).
 //
-// A 32-bit word holds 16 counts x (layout in geno.cu): for element pair q (elements 2q, 2q+1),
-// (word >> q) has nz_even at bit 0, hi_even at bit 8, nz_odd at bit 16, hi_odd at bit 24.
-// BF16(x) = nz·0x3F80 + hi·0x0080 (0 → 0x0000, 1 → 0x3F80, 2 → 0x4000), so one AND, one
-// shift-AND and one integer multiply-add give the packed BF16 pair of both elements.
+// A 32-bit word holds 16 counts x ∈ {0,1,2} as 2-bit binary fields (layout in geno.cu): the even
+// elements 2q in bits 2q..2q+1 of the low half-word, the odd elements 2q+1 in bits 16+2q.. of the
+// high half-word.  For the element pair q (elements 2q, 2q+1) and k = 2·(q mod 4), taking
+// src = word (q < 4) or word ≫ 8 (q ≥ 4):
+//   (src & (0x00030003 ≪ k)) | 0x43004300
+// is a BF16 pair whose halves are exactly 128 + x·2^k (0x4300 is 128; the count lands in the
+// mantissa, or for k = 6 and x = 2 carries into the exponent, which is still 256 = 128 + 2·64).
+// One BF16 FMA, v·2^−k − 128·2^−k, then gives x exactly.  So a pair costs one AND-OR on the
+// integer pipe and one HFMA2 on the FMA pipe (plus one shift per 8 pairs).
 #pragma once
 #include <cstdint>
+#include <cuda_bf16.h>
 
 namespace slemm {
 
 __device__ __forceinline__ uint32_t bf16pair_of(uint32_t word, int q)
 {
-  const uint32_t s = word >> q;
-  return (s & 0x00010001u) * 0x3F80u + ((s >> 1) & 0x00800080u);
+  const uint32_t src = (q < 4) ? word : (word >> 8);
+  const int k = 2 * (q & 3);
+  const uint32_t bits = (src & (0x00030003u << k)) | 0x43004300u;
+  const float sc = 1.0f / (float)(1 << k);
+  const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&bits);
+  const __nv_bfloat162 r = __hfma2(v, __float2bfloat162_rn(sc), __float2bfloat162_rn(-128.0f * sc));
+  return *reinterpret_cast<const uint32_t*>(&r);
 }
 
 // The 4 BF16 pairs of elements 8h … 8h+7 of a word (h = 0: pairs 0-3, h = 1: pairs 4-7).
@@ -32,6 +43,12 @@ __device__ __forceinline__ void f32pair_of(uint32_t word, int q, float& even, fl
   const uint32_t p = bf16pair_of(word, q);
   even = __uint_as_float(p << 16);
   odd = __uint_as_float(p & 0xFFFF0000u);
+}
+
+// Count of element e (0..15) of a word, as an integer.
+__device__ __forceinline__ uint32_t count_at(uint32_t word, int e)
+{
+  return (word >> ((e & 1) * 16 + 2 * (e >> 1))) & 3u;
 }
 
 }  // namespace slemm

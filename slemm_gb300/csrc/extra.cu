@@ -93,17 +93,14 @@ score_kernel(const uint4* __restrict__ G, int64_t K_tiles, const float* __restri
       for (int w = 0; w < 4; ++w) {
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
-          const int q = e >> 1;
-          const uint32_t sh = w4[w] >> q;
-          const uint32_t nz = (e & 1) ? ((sh >> 16) & 1u) : (sh & 1u);
-          const uint32_t hi = (e & 1) ? ((sh >> 24) & 1u) : ((sh >> 8) & 1u);
-          if (!nz) continue;
+          const uint32_t cnt = count_at(w4[w], e);
+          if (!cnt) continue;
           const int kk = u * kTileK + w * 16 + e;
-          const double x = (double)(nz + hi);
+          const double x = (double)cnt;
           acc[0] = fma(x, (double)sb[kk][0], acc[0]);
           const double r2 = (double)sb[kk][1];
           acc[1] = fma(x, r2, acc[1]);
-          if (hi) acc[2] += r2;
+          if (cnt == 2u) acc[2] += r2;
 #pragma unroll
           for (int l = 2; l < C; ++l) acc[l + 1] = fma(x, (double)sb[kk][l], acc[l + 1]);
         }

@@ -2,17 +2,15 @@
 //
 // Device layout of the counts.  The reference keeps genotypes as m rows of 2n bits
 // (std::vector<std::vector<bool>>, src/option.cpp:347) decoded byte by byte from the .bed
-// (src/input.cpp:343-386).  Here each allele-2 count x ∈ {0,1,2} is stored as two bits
-// (nz = [x≠0], hi = [x==2]) in a tiled layout:
+// (src/input.cpp:343-386).  Here each allele-2 count x ∈ {0,1,2} is a 2-bit binary field in a
+// tiled layout:
 //   tile (mt, kt) = 128 rows × 64 K-elements = 2048 contiguous bytes at
 //   ((mt·K_tiles + kt)·128 + r)·16; the 16 bytes of row r hold K-elements kt·64 … kt·64+63 as
 //   four 32-bit words, word w covering elements 16w … 16w+15 with
-//     bits  0-7 : nz of the even elements 16w+2q (bit q)
-//     bits  8-15: hi of the even elements        (bit 8+q)
-//     bits 16-23: nz of the odd elements 16w+2q+1 (bit 16+q)
-//     bits 24-31: hi of the odd elements          (bit 24+q)
-// so that (word >> q) puts element pair q where one integer multiply-add turns it into a
-// BF16 pair (see decode.cuh).  Two copies are kept: G (rows = SNPs, K = individuals) and GT
+//     bits  2q, 2q+1      : the even element 16w+2q
+//     bits 16+2q, 17+2q   : the odd element 16w+2q+1
+// so that an element pair becomes a BF16 pair with one AND-OR and one BF16 FMA (decode.cuh).
+// Two copies are kept: G (rows = SNPs, K = individuals) and GT
 // (rows = individuals, K = SNPs), so both products read K-contiguous tiles with one 2048-byte
 // bulk copy per tile.  Padding rows/columns hold count 0.
 #include "internal.h"
@@ -67,10 +65,9 @@ __device__ __forceinline__ unsigned count_of(const uint8_t* __restrict__ row, in
 
 __device__ __forceinline__ unsigned plane_bits(unsigned x, int e)
 {
-  // element e (0..15) of a word; x = count
-  const unsigned nz = x != 0u, hi = x == 2u;
+  // element e (0..15) of a word; x = count as a 2-bit field
   const int q = e >> 1;
-  return (e & 1) ? ((nz << (16 + q)) | (hi << (24 + q))) : ((nz << q) | (hi << (8 + q)));
+  return (e & 1) ? (x << (16 + 2 * q)) : (x << (2 * q));
 }
 
 // G words: thread → (SNP row j, word wi along individuals).
@@ -121,7 +118,7 @@ __global__ void pack_GT_kernel(const uint8_t* __restrict__ raw, int64_t row_byte
   GT[((mt * K_tiles_T + kt) * 128 + r) * 4 + wr] = word;
 }
 
-// Per-row integer counts over the G copy: allele count, n1 (one nz bit, no hi), n2 (hi bits).
+// Per-row integer counts over the G copy: n1 = fields 01, n2 = fields 10, allele count n1 + 2·n2.
 __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int64_t K_tiles,
                                   int64_t* __restrict__ pc, int32_t* __restrict__ c1,
                                   int32_t* __restrict__ c2)
@@ -131,21 +128,21 @@ __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int
   const int lane = threadIdx.x & 31;
   if (warp >= m) return;
   const int64_t mt = warp / 128, r = warp % 128;
-  long long nz = 0, hi = 0;
+  long long ones = 0, twos = 0;
   for (int64_t wi = lane; wi < K_tiles * 4; wi += 32) {
     const int64_t kt = wi / 4, wr = wi % 4;
     const uint32_t w = G[((mt * K_tiles + kt) * 128 + r) * 4 + wr];
-    nz += __popc(w & 0x00FF00FFu);
-    hi += __popc(w & 0xFF00FF00u);
+    ones += __popc(w & 0x55555555u);   // low bit of a field: count 1
+    twos += __popc(w & 0xAAAAAAAAu);   // high bit of a field: count 2
   }
   for (int o = 16; o; o >>= 1) {
-    nz += __shfl_xor_sync(0xffffffffu, nz, o);
-    hi += __shfl_xor_sync(0xffffffffu, hi, o);
+    ones += __shfl_xor_sync(0xffffffffu, ones, o);
+    twos += __shfl_xor_sync(0xffffffffu, twos, o);
   }
   if (lane == 0) {
-    pc[warp] = nz + hi;
-    c1[warp] = (int32_t)(nz - hi);
-    c2[warp] = (int32_t)hi;
+    pc[warp] = ones + 2 * twos;
+    c1[warp] = (int32_t)ones;
+    c2[warp] = (int32_t)twos;
   }
 }
 
@@ -203,8 +200,9 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       g->own_stream = true;
       g->n = n;
       g->m = m;
-      g->n_pad = round_up(n, kTileM);
-      g->m_pad = round_up(m, kTileM);
+      // rows padded to 256 so every tensor-core CTA (two 128-row tiles) is full
+      g->n_pad = round_up(n, kPadRows);
+      g->m_pad = round_up(m, kPadRows);
       const int64_t Kt_G = g->n_pad / kTileK, Kt_GT = g->m_pad / kTileK;
       const size_t bytes_G = (size_t)(g->m_pad / kTileM) * Kt_G * kTileBytes;
       const size_t bytes_GT = (size_t)(g->n_pad / kTileM) * Kt_GT * kTileBytes;

@@ -43,6 +43,10 @@ namespace slemm {
 // ops.cu — one operator application on device buffers (column-major, ld given).
 void op_device(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                float* out, int64_t ld_out);
+// H0 operator on a mixed block: columns 0 … nq−1 as H0_quadform_mv, the rest as H0_ldet_mv
+// (kind LDET; QUADFORM means nq = k).
+void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
+                     float* out, int64_t ld_out, int nq);
 
 // Column reductions with FP64 accumulation, deterministic two-stage (ops.cu).
 // dots[c] = Σ_i a[i,c]·b[i,c] over i < n for c < k (b == nullptr → Σ a²).  Result on device.
@@ -57,7 +61,7 @@ void proj_apply(slemm_geno* g, float* X, int64_t ldx, int k, const double* d_QtX
 // groups with their own stopping rule (empty = one group).
 slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const float* dB, int t,
                                  float tol, int maxit, bool verbose, std::vector<int> groups,
-                                 int p_freq);
+                                 int p_freq, int nq = 0);
 // Solve for the columns of group `grp`; X has that group's columns (ld = ldx) on device.
 int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp);
 void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2);
@@ -67,6 +71,9 @@ const double* lseed_delta(const slemm_lseed* S);   // iters × t (row j = step j
 const double* lseed_beta(const slemm_lseed* S);    // (iters+1) × t
 int lseed_t(const slemm_lseed* S);
 void lseed_free(slemm_lseed* S);
+
+// probes.cu — the reference's normalised Rademacher block (n×n_V, ld) on the device.
+void rademacher_device(int seed, int64_t n, int n_V, float* dV, int64_t ld, cudaStream_t st);
 
 int64_t workspace_bytes(const slemm_geno* g);
 // Reads (and clears) the device error word; throws if a kernel gave up a bounded wait.

@@ -35,6 +35,7 @@ struct slemm_lseed {
   // Column groups that share one stopping rule (the reference runs each group as its own
   // L_Seed call); group_iters[g] is the step at which group g met the tolerance.
   std::vector<int> group_start, group_iters;
+  slemm::DevBuf solve_coef, solve_blk;       // reused by every shifted solve
   ~slemm_lseed()
   {
     for (auto* c : chunks) delete c;
@@ -235,8 +236,10 @@ namespace slemm {
 // Runs L_Seed on a device RHS block B (n×t, ld = n).  Returns the seed object.
 slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const float* dB, int t,
                                  float tol, int maxit, bool verbose, std::vector<int> groups,
-                                 int p_freq)
+                                 int p_freq, int nq)
 {
+  // projected (H0_quadform_mv) leading columns; QUADFORM projects all of them
+  const int nq_eff = (kind == SLEMM_OP_QUADFORM) ? t : std::max(0, std::min(nq, t));
   if (groups.empty()) groups.push_back(t);
   {
     int tot = 0;
@@ -307,7 +310,7 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     while (j < maxit - 1) {
       float* Uj = S->block(j);
       float* Uprev = j > 0 ? S->block(j - 1) : nullptr;
-      op_device(g, kind, tau0, Uj, n, t, tmp, n);
+      op_device_mixed(g, kind, tau0, Uj, n, t, tmp, n, nq_eff);
       if (j > 0)
         CUDA_TRY(cudaMemcpyAsync(d_beta, S->beta.data() + (size_t)j * t, t * sizeof(double),
                                  cudaMemcpyHostToDevice, st));
@@ -409,7 +412,8 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
   }
   std::vector<const float*> hblocks(std::max(steps, 1));
   for (int i = 0; i < steps; ++i) hblocks[i] = (i == 0) ? nullptr : S->block(i);
-  DevBuf dcoef, dblk;
+  DevBuf& dcoef = S->solve_coef;
+  DevBuf& dblk = S->solve_blk;
   dcoef.ensure(coef.size() * sizeof(double));
   dblk.ensure(hblocks.size() * sizeof(float*));
   CUDA_TRY(cudaMemcpyAsync(dcoef.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -418,7 +422,7 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
   lz_combine_kernel<<<gr, 256, 0, st>>>(dX, ldx, S->B.as<float>(), dblk.as<const float*>(), steps - 1,
                                         dcoef.as<double>(), S->n, c0, tc);
   LAUNCH_CHECK();
-  CUDA_TRY(cudaStreamSynchronize(st));   // the coefficient buffers are freed on return
+  CUDA_TRY(cudaStreamSynchronize(st));   // the host coefficient vectors go out of scope on return
   return steps;
 }
 
@@ -482,7 +486,7 @@ int slemm_gpu_lanczos_seed(slemm_geno* g, int op_kind, float tau0, const float* 
                                  g->stream));
       src = dB.as<float>();
     }
-    slemm_lseed* S = lanczos_seed_device(g, op_kind, tau0, src, t, tol, maxit, false, {}, 5);
+    slemm_lseed* S = lanczos_seed_device(g, op_kind, tau0, src, t, tol, maxit, false, {}, 5, 0);
     CUDA_TRY(cudaStreamSynchronize(g->stream));
     *out = S;
     if (iters) *iters = S->iters;

@@ -163,11 +163,12 @@ __device__ __forceinline__ double store_operand(float x, int npieces, void* Bv, 
   return sum;
 }
 
-// Direction-1 operand (K = individuals): x = in[i,c]; optionally x −= Σ_l Q[i,l]·QtV[l,c];
-// optionally x *= rr[i]; rows i ≥ n are 0.  red[c][blk] = Σ_i stored(x).
+// Direction-1 operand (K = individuals): x = in[i,c]; for the first nq columns
+// x −= Σ_l Q[i,l]·QtV[l,c]; optionally x *= rr[i]; rows i ≥ n are 0.
+// red[c][blk] = Σ_i stored(x).
 __global__ void prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n,
                                       int64_t n_pad, int k, const float* __restrict__ Q,
-                                      int64_t ldq, int cq, const double* __restrict__ QtV,
+                                      int64_t ldq, int cq, const double* __restrict__ QtV, int nq,
                                       const float* __restrict__ rr, int npieces, void* B,
                                       double* __restrict__ red, int nblk)
 {
@@ -180,9 +181,9 @@ __global__ void prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, 
     float x = 0.f;
     if (i < n) {
       x = in[(int64_t)c * ld + i];
-      if (QtV) {
+      if (QtV && c < nq) {
         double p = 0.0;
-        for (int l = 0; l < cq; ++l) p += (double)Q[(int64_t)l * ldq + i] * QtV[l * k + c];
+        for (int l = 0; l < cq; ++l) p += (double)Q[(int64_t)l * ldq + i] * QtV[l * nq + c];
         x = x - (float)p;
       }
       if (rr) x *= rr[i];
@@ -257,16 +258,16 @@ __global__ void prologue_snp_kernel(const float* __restrict__ in, int64_t ld, in
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// Direction-2 finalize (rows = individuals): val = raw − t_c, times rr_i when rr != nullptr,
-// plus tau0·v when V != nullptr.  out[i,c] = val for i < n.
+// Direction-2 finalize (rows = individuals) of columns c0 + blockIdx.y: val = raw − t_c, times
+// rr_i when rr != nullptr, plus tau0·v when V != nullptr.  out[i,c] = val for i < n.
 __global__ void finalize_indiv_kernel(const float* __restrict__ D, int splits, int N,
                                       int64_t n_pad, int pieces, int k, int64_t n,
                                       const double* __restrict__ tsum, const float* __restrict__ rr,
                                       const float* __restrict__ V, int64_t ldv, float tau0,
-                                      float* __restrict__ out, int64_t ldo)
+                                      float* __restrict__ out, int64_t ldo, int c0)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
+  const int c = c0 + blockIdx.y;
   if (i >= n) return;
   const float raw = gather_D(D, splits, N, n_pad, pieces, k, c, i);
   float val = (float)((double)raw - tsum[c]);
@@ -290,7 +291,7 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
   p.pieces = g->prec == SLEMM_PREC_BF16X3 ? 3 : (g->prec == SLEMM_PREC_BF16X2 ? 2 : 1);
   p.N = p.tc ? (int)round_up((int64_t)p.pieces * k, 16) : k;
   const int64_t M_tiles = M_pad / kTileM, K_tiles = K_pad / kTileK;
-  p.splits = p.tc ? choose_splits(M_tiles, K_tiles, 1, num_sms())
+  p.splits = p.tc ? choose_splits(M_tiles / 2, K_tiles, 1, num_sms())
                   : choose_splits(M_tiles, K_tiles, 8, num_sms());
   return p;
 }
@@ -377,10 +378,13 @@ static Small small_ws(slemm_geno* g, int k)
   return s;
 }
 
-// One operator application on a column group (k ≤ max_group).
+// One operator application on a column group (k ≤ max_group).  For the H0 operators (kind
+// LDET, or QUADFORM) the first nq columns get the projections of H0_quadform_mv and the others
+// are plain H0_ldet_mv columns, so one block can carry both kinds of seed systems.
 static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
-                     float* out, int64_t ld_out)
+                     float* out, int64_t ld_out, int nq)
 {
+  if (kind == SLEMM_OP_QUADFORM) kind = SLEMM_OP_LDET;   // nq carries the projected columns
   cudaStream_t st = g->stream;
   Small sm = small_ws(g, k);
   const bool dir1 = kind != SLEMM_OP_MATVEC;                          // needs Zᵀ pass
@@ -408,19 +412,19 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     CUDA_TRY(cudaMemsetAsync((uint16_t*)B2 + (size_t)p2.pieces * k * g->m_pad, 0,
                              (size_t)(p2.N - p2.pieces * k) * g->m_pad * 2, st));
 
-  const bool quad = kind == SLEMM_OP_QUADFORM;
-  const bool h0 = quad || kind == SLEMM_OP_LDET;
+  // H0 operators: the first nq columns are projected (H0_quadform_mv), the rest are not (H0_ldet_mv)
+  const bool h0 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET;
 
   if (dir1) {
     // ---- prologue 1: v_adj = rr∘(v − QQᵀv) (quadform), rr∘v (ldet), v (rmatvec) ----
     const double* QtV = nullptr;
-    if (quad && g->c > 0) {
-      proj_coeffs(g, in, ld_in, k, sm.QtV);
+    if (h0 && nq > 0 && g->c > 0) {
+      proj_coeffs(g, in, ld_in, nq, sm.QtV);
       QtV = sm.QtV;
     }
     dim3 grid(nblk_n, k);
     prologue_indiv_kernel<<<grid, kRedThreads, 0, st>>>(
-        in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad, g->c, QtV,
+        in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad, g->c, QtV, nq,
         h0 ? g->rr.as<float>() : nullptr, np1, B1, red, nblk_n);
     LAUNCH_CHECK();
     reduce_partials(red, nblk_n, k, sm.colsum, st);
@@ -453,40 +457,55 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   // ---- pass 2: Cnt over SNPs ----
   run_gemm(g, p2, g->GT.as<uint8_t>(), g->n_pad, g->m_pad, B2, D, sm.err, k, 2);
   // ---- finalize 2 ----
-  dim3 gridn((unsigned)ceil_div(g->n, 256), k);
+  const unsigned gx = (unsigned)ceil_div(g->n, 256);
   if (kind == SLEMM_OP_MATVEC) {
-    finalize_indiv_kernel<<<gridn, 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n,
-                                                 sm.tsum, nullptr, nullptr, 0, 0.f, out, ld_out);
+    finalize_indiv_kernel<<<dim3(gx, k), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n,
+                                                       sm.tsum, nullptr, nullptr, 0, 0.f, out, ld_out, 0);
     LAUNCH_CHECK();
-  } else if (kind == SLEMM_OP_LDET) {
-    finalize_indiv_kernel<<<gridn, 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n,
-                                                 sm.tsum, g->rr.as<float>(), in, ld_in, tau0, out,
-                                                 ld_out);
+    return;
+  }
+  // ldet columns nq … k−1: out = rr∘(Z_c W Z_cᵀ rr∘v) + τ0 v
+  if (nq < k) {
+    finalize_indiv_kernel<<<dim3(gx, k - nq), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k,
+                                                            g->n, sm.tsum, g->rr.as<float>(), in, ld_in,
+                                                            tau0, out, ld_out, nq);
     LAUNCH_CHECK();
-  } else {
-    // T = rr∘(Z_c W Z_cᵀ v_adj); out = T + τ0 v − QQᵀT
-    finalize_indiv_kernel<<<gridn, 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n,
-                                                 sm.tsum, g->rr.as<float>(), nullptr, 0, 0.f, out,
-                                                 ld_out);
+  }
+  // quadform columns 0 … nq−1: T = rr∘(Z_c W Z_cᵀ v_adj); out = T + τ0 v − QQᵀT
+  if (nq > 0) {
+    finalize_indiv_kernel<<<dim3(gx, nq), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k,
+                                                        g->n, sm.tsum, g->rr.as<float>(), nullptr, 0, 0.f,
+                                                        out, ld_out, 0);
     LAUNCH_CHECK();
-    if (g->c > 0) proj_coeffs(g, out, ld_out, k, sm.QtT);
-    proj_apply_kernel<<<gridn, 256, 0, st>>>(g->Q.as<float>(), g->n_pad, g->c, out, ld_out, g->n, k,
-                                             sm.QtT, in, ld_in, tau0);
+    if (g->c > 0) proj_coeffs(g, out, ld_out, nq, sm.QtT);
+    proj_apply_kernel<<<dim3(gx, nq), 256, 0, st>>>(g->Q.as<float>(), g->n_pad, g->c, out, ld_out, g->n,
+                                                    nq, sm.QtT, in, ld_in, tau0);
     LAUNCH_CHECK();
+  }
+}
+
+void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
+                     float* out, int64_t ld_out, int nq)
+{
+  if (!g->weights_set) SLEMM_THROW(SLEMM_ERR_STATE, "set_weights must be called before operators");
+  CHECK_ARG(kind >= SLEMM_OP_QUADFORM && kind <= SLEMM_OP_WRMATVEC, "unknown operator kind");
+  CHECK_ARG(k >= 1, "k must be >= 1");
+  if (kind == SLEMM_OP_QUADFORM) nq = k;
+  const bool h0 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET;
+  if (!h0) nq = 0;
+  CHECK_ARG(nq >= 0 && nq <= k, "bad number of projected columns");
+  const int grp = max_group(g);
+  for (int c0 = 0; c0 < k; c0 += grp) {
+    const int kc = std::min(grp, k - c0);
+    const int nqg = std::max(0, std::min(kc, nq - c0));
+    op_group(g, kind, tau0, in + (int64_t)c0 * ld_in, ld_in, kc, out + (int64_t)c0 * ld_out, ld_out, nqg);
   }
 }
 
 void op_device(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                float* out, int64_t ld_out)
 {
-  if (!g->weights_set) SLEMM_THROW(SLEMM_ERR_STATE, "set_weights must be called before operators");
-  CHECK_ARG(kind >= SLEMM_OP_QUADFORM && kind <= SLEMM_OP_WRMATVEC, "unknown operator kind");
-  CHECK_ARG(k >= 1, "k must be >= 1");
-  const int grp = max_group(g);
-  for (int c0 = 0; c0 < k; c0 += grp) {
-    const int kc = std::min(grp, k - c0);
-    op_group(g, kind, tau0, in + (int64_t)c0 * ld_in, ld_in, kc, out + (int64_t)c0 * ld_out, ld_out);
-  }
+  op_device_mixed(g, kind, tau0, in, ld_in, k, out, ld_out, kind == SLEMM_OP_QUADFORM ? k : 0);
 }
 
 int64_t workspace_bytes(const slemm_geno* g)

@@ -307,50 +307,41 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     for (int64_t i = 0; i < n; ++i) yproj[i] = (float)ry[i];
   }
   if (verbose) printf("Projected covariates out of phenotypes.\nGenerating %d Rademacher probing vectors.\n", n_V);
-  // Rademacher probes: reml.cpp:597-605 (libstdc++ draws), column norms in FP32
-  const int tQV = c + n_V;
-  std::vector<float> QV((size_t)n * tQV);
-  for (size_t i = 0; i < (size_t)n * c; ++i) QV[i] = (float)S.qr.Q[i];
-  {
-    std::mt19937 rng(o.seed + 54321);
-    std::uniform_real_distribution<float> runif(0.0, 1.0);
-    for (int j = 0; j < n_V; ++j) {
-      float* v = QV.data() + (size_t)(c + j) * n;
-      for (int64_t i = 0; i < n; ++i) v[i] = (runif(rng) < 0.5) ? -1.0f : 1.0f;
-      const float nrm = std::sqrt((float)n);   // Σ(±1)² = n exactly
-      for (int64_t i = 0; i < n; ++i) v[i] /= nrm;
-    }
-  }
+  // One block [y_proj | Q | V] (t = 1 + c + n_V) through one Lanczos recurrence: column 0 uses
+  // the projected operator (seed_y, H0_quadform_mv), the rest the plain one (seed_Q and seed_V,
+  // H0_ldet_mv); each of the three groups keeps its own stopping rule, as the reference's three
+  // L_Seed calls do (src/reml.cpp:627-631).
+  const int tQV = 1 + c + n_V;
+  std::vector<float> QV((size_t)n * (1 + c));
+  std::copy(yproj.begin(), yproj.end(), QV.begin());
+  for (size_t i = 0; i < (size_t)n * c; ++i) QV[(size_t)n + i] = (float)S.qr.Q[i];
   DevBuf d_y, d_QV, d_X, d_tmp;
   d_y.ensure((size_t)n * sizeof(float));
   d_QV.ensure((size_t)n * tQV * sizeof(float));
   d_X.ensure((size_t)n * tQV * sizeof(float));
   d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + 64 * 64 * sizeof(double));
   upload(g, d_y.as<float>(), yproj.data(), n);
-  upload(g, d_QV.as<float>(), QV.data(), (size_t)n * tQV);
+  upload(g, d_QV.as<float>(), QV.data(), (size_t)n * (1 + c));
+  // Rademacher probes (src/reml.cpp:597-605), the reference's mt19937 draws generated on the GPU
+  rademacher_device(o.seed, n, n_V, d_QV.as<float>() + (size_t)(1 + c) * n, n, g->stream);
   double* d_scal = d_tmp.as<double>();
 
   const float tau0 = (1.0f - o.s2max) / o.s2max;
-  if (verbose) printf("\nPerforming Lanczos decomposition for phenotypes:\n");
-  slemm_lseed* seed_y = lanczos_seed_device(g, SLEMM_OP_QUADFORM, tau0, d_y.as<float>(), 1, o.tol_L, o.maxit,
-                                            verbose, {}, 5);
-  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold_y(seed_y, lseed_free);
-  if (verbose) printf("\nPerforming Lanczos decomposition for covariates and Rademacher vectors:\n");
-  // [Q V] share the ldet operator: one block, two stopping groups (the reference's seed_Q
-  // and seed_V calls, src/reml.cpp:629-631)
-  slemm_lseed* seed_QV = lanczos_seed_device(g, SLEMM_OP_LDET, tau0, d_QV.as<float>(), tQV, o.tol_L, o.maxit,
-                                             verbose, {c, n_V}, 5);
-  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold_qv(seed_QV, lseed_free);
-  const int nld = lseed_iters(seed_QV, 1);
-  // Jacobi matrices of the probes (rows c … c+n_V−1), src/reml.cpp:638-646
+  if (verbose) printf("\nPerforming Lanczos decomposition for phenotypes, covariates and Rademacher vectors:\n");
+  slemm_lseed* seed = lanczos_seed_device(g, SLEMM_OP_LDET, tau0, d_QV.as<float>(), tQV, o.tol_L, o.maxit,
+                                          verbose, {1, c, n_V}, 5, 1);
+  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold(seed, lseed_free);
+  constexpr int GY = 0, GQ = 1, GV = 2;
+  const int nld = lseed_iters(seed, GV);
+  // Jacobi matrices of the probes (columns 1+c ... c+n_V), src/reml.cpp:638-646
   std::vector<double> dl((size_t)n_V * nld), bt((size_t)n_V * (nld + 1));
   {
-    const double* D = lseed_delta(seed_QV);
-    const double* B = lseed_beta(seed_QV);
+    const double* D = lseed_delta(seed);
+    const double* B = lseed_beta(seed);
     for (int j = 0; j < nld; ++j)
-      for (int p = 0; p < n_V; ++p) dl[(size_t)j * n_V + p] = D[(size_t)j * tQV + c + p];
+      for (int p = 0; p < n_V; ++p) dl[(size_t)j * n_V + p] = D[(size_t)j * tQV + 1 + c + p];
     for (int j = 0; j <= nld; ++j)
-      for (int p = 0; p < n_V; ++p) bt[(size_t)j * n_V + p] = B[(size_t)j * tQV + c + p];
+      for (int p = 0; p < n_V; ++p) bt[(size_t)j * n_V + p] = B[(size_t)j * tQV + 1 + c + p];
   }
   std::vector<double> DV((size_t)n_V * nld), W2((size_t)n_V * nld);
   tridiag_eig_host(dl.data(), bt.data(), n_V, nld, DV.data(), W2.data());
@@ -364,7 +355,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     ++n_eval;
     const float tau = (1 - ss) / ss;
     const float sigma = tau - tau0;
-    lanczos_solve_device(seed_y, (double)sigma, 1e-6, d_X.as<float>(), n, 0);
+    lanczos_solve_device(seed, (double)sigma, 1e-6, d_X.as<float>(), n, GY);
     col_dots(g, d_y.as<float>(), n, d_X.as<float>(), n, n, 1, d_scal);
     const double yPy = d2h(g, d_scal, 1)[0];
     Criterion r;
@@ -374,7 +365,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     for (size_t q = 0; q < DV.size(); ++q) ldet_H += W2[q] * std::log(DV[q] + sigma);
     ldet_H = ldet_H * (double)n / (double)n_V;
     r.lrt = (double)n * std::log(ySy / yPy) - ldet_H;
-    lanczos_solve_device(seed_QV, (double)sigma, 1e-6, d_X.as<float>(), n, 0);
+    lanczos_solve_device(seed, (double)sigma, 1e-6, d_X.as<float>(), n, GQ);
     proj_coeffs(g, d_X.as<float>(), n, c, d_scal);
     std::vector<double> M = d2h(g, d_scal, (size_t)c * c);
     r.slogLL = (double)(n - c) * std::log(ySy / yPy) - logabsdet(M, c) - ldet_H;
@@ -419,7 +410,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
 
   // Py = rr∘(I−QQᵀ)L_Solve(seed_y, y_proj, τ1−τ0)   (src/reml.cpp:659-661)
   float* d_Py = d_X.as<float>();
-  lanczos_solve_device(seed_y, (double)(tau1 - tau0), 1e-6, d_Py, n, 0);
+  lanczos_solve_device(seed, (double)(tau1 - tau0), 1e-6, d_Py, n, GY);
   proj_coeffs(g, d_Py, n, 1, d_scal);
   proj_apply(g, d_Py, n, 1, d_scal);
   scale_rows(g, d_Py, n, n, 1, g->rr.as<float>());
@@ -435,7 +426,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   // BLUE and var(BLUE) (src/reml.cpp:674-677): with rr∘X = Q·qrR,
   //   XᵀH⁻¹X = qrRᵀ (Qᵀ S) qrR and (H⁻¹X)ᵀy = qrRᵀ Sᵀ(rr∘y), S = L_Solve(seed_Q, Q, τ1−τ0)
   float* d_S = d_X.as<float>();
-  lanczos_solve_device(seed_QV, (double)(tau1 - tau0), 1e-6, d_S, n, 0);
+  lanczos_solve_device(seed, (double)(tau1 - tau0), 1e-6, d_S, n, GQ);
   proj_coeffs(g, d_S, n, c, d_scal);
   std::vector<double> QtS = d2h(g, d_scal, (size_t)c * c);
   {
@@ -489,8 +480,8 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     res->ve = ve;
     res->h2 = vg / (vg + ve);
     res->lrt = lrt;
-    res->iters_y = lseed_iters(seed_y, 0);
-    res->iters_Q = lseed_iters(seed_QV, 0);
+    res->iters_y = lseed_iters(seed, GY);
+    res->iters_Q = lseed_iters(seed, GQ);
     res->iters_V = nld;
     res->n_criterion = n_eval;
     res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();

@@ -143,3 +143,13 @@ def test_score_terms_vs_reference_script(gpu):
     ok = np.isfinite(rp)
     assert np.array_equal(ok, np.isfinite(p))
     assert np.max(np.abs(np.log10(p[ok]) - np.log10(rp[ok]))) <= 1e-3
+
+
+@pytest.mark.parametrize("seed,n,n_V", [(0, 37, 3), (1, 1000, 5), (42, 2049, 2), (7, 100003, 1)])
+def test_gpu_probes_match_reference_draws(gpu, seed, n, n_V):
+    """The GPU MT19937 probe block equals the libstdc++ draws of src/reml.cpp:597-605 bit for bit."""
+    import ctypes
+    V = np.zeros((n, n_V), np.float32, order="F")
+    _lib.check(gpu.slemm_gpu_rademacher(seed, n, n_V, V.ctypes.data_as(ctypes.c_void_p), n, 0))
+    ref = orc.rademacher(seed, n, n_V)
+    assert np.array_equal(V, ref)
