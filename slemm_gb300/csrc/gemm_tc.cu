@@ -1,21 +1,31 @@
 // gemm_tc.cu — tcgen05 packed-genotype product for sm_103a.
 //
-// D[s][n][r] = Σ_{K in split s} count[r,K] · B[n][K].  One CTA owns 256 rows as two 128-row
-// tiles, each with its own TMEM accumulator (128 lanes × N FP32 columns), and both consume every
-// B tile, so each B byte fetched from L2 feeds twice the MMA work.
+// D[s][n][r] = Σ_{K in split s} count[r,K] · B[n][K].  One CTA owns SUB (1 or 2) tiles of 128
+// rows, each with its own TMEM accumulator (128 lanes × N FP32 columns); every B tile feeds all
+// of them.  The decoded counts (the MMA's A operand) never touch shared memory: decoder threads
+// turn their row's 16 packed bytes into 32 BF16 pairs in registers and write them into tensor
+// memory with tcgen05.st; the MMA reads A from TMEM and B from shared memory.
 //
-// Three decoupled shared-memory rings:
-//   packed ring (kPk = 8 stages × 2 tiles × 2 KB) ← warp 0: two cp.async.bulk per stage (DRAM);
-//   B ring      (nb stages × N·128 B)             ← warp 1: one TMA tile, 128-byte swizzle (L2);
-//   A ring      (na stages × 2 × 16 KB BF16)      ← warps 3..10 decode packed → BF16 in the
-//                                                   canonical K-major SWIZZLE_128B layout;
-// warp 2 allocates TMEM and issues 2 × 4 tcgen05.mma (M=128, N, K=16) per stage, committing to
-// the A- and B-ring "empty" barriers; the decoder warps then run the epilogue (tcgen05.ld →
-// FP32 partials), one warp per TMEM lane quarter and accumulator.
+// What limits tcgen05 here is the issuing thread, not the tensor pipe: measured on GB300, one
+// thread issuing M=128, K=16 BF16 MMAs back to back sustains N/2 cycles per MMA (8192 FLOP/clk
+// per SM), but every instruction between two MMAs delays the next, and an mbarrier wait costs
+// ~250 cycles even when its phase has long completed.  So each tile has its own MMA-issuing warp
+// (one waits while the other issues), each stage has ONE full and ONE empty barrier (decoders and
+// the B copy arrive on the same full barrier; each MMA warp commits once to the empty barrier),
+// and the four MMAs of a stage use descriptors advanced by constants.
 //
-// Every mbarrier wait is bounded by a %globaltimer budget; a wait that gives up sets a bit in
-// *err, raises the CTA's abort flag, and the CTA drains the copies and MMAs it issued (again with
-// bounded waits), frees its TMEM and returns.  The host reads *err after the operator.
+// Roles (warp w):
+//   w = 0          packed-tile producer: SUB cp.async.bulk of 2 KB per stage, 8-deep ring;
+//   w = 1          B producer: one TMA tile (N rows × 64 BF16, 128-byte swizzle) per stage;
+//   w = 2 … 1+SUB  MMA issuers, one per tile (w = 2 also allocates TMEM);
+//   w = 2+SUB …    NG groups of 4·SUB decoder warps; group g decodes stages i ≡ g (mod NG).
+//                  Warp w covers TMEM lanes 32·(w mod 4) …, i.e. those rows of its tile.  Group 0
+//                  also runs the epilogue (tcgen05.ld → FP32 partials).
+//
+// TMEM columns: accumulators [0, SUB·N), then S stages of SUB × 32 columns of A (64 BF16 of K per
+// row).  Every mbarrier wait is bounded by a %globaltimer budget; a wait that gives up sets a bit
+// in *err, raises the CTA's abort flag, and the CTA drains what it issued (bounded), frees its
+// TMEM and returns.  The host reads *err after the operator.
 #include "common.h"
 #include "decode.cuh"
 
@@ -24,35 +34,34 @@
 namespace slemm {
 
 constexpr int kPk = 8;                 // packed-tile stages
-constexpr int kMaxRing = 8;            // barrier array size for the A and B rings
-constexpr int kThreads = 352;          // 11 warps
-constexpr int kDecWarps = 8;           // warps 3..10
-constexpr int kTileA = 16384;          // one 128×64 BF16 tile
+constexpr int kS = 3;                  // A (TMEM) + B (smem) stages
+constexpr int kNG = 2;                 // decoder groups
+constexpr int kMaxThreads = 64 + 2 * 32 + kNG * 2 * 128;   // SUB = 2
 constexpr uint64_t kWaitBudgetNs = 2000000000ull;   // 2 s per wait
 constexpr size_t kSmemBudget = 227 * 1024;
 
-struct TcSmemLayout {
-  int N, na, nb;
-  size_t a_off, b_off, pk_off, bar_off, total;
-  __host__ __device__ TcSmemLayout(int N_, int na_, int nb_) : N(N_), na(na_), nb(nb_)
+struct TcPlan {
+  int N, sub;
+  size_t b_off, pk_off, bar_off, total;
+  __host__ __device__ TcPlan(int N_, int sub_) : N(N_), sub(sub_)
   {
-    a_off = 0;                                             // na × 2 × 16 KB (1024-aligned)
-    b_off = a_off + (size_t)na * 2 * kTileA;               // nb × N·128 B (1024-aligned, N%8==0)
-    pk_off = b_off + (size_t)nb * N * 128;                 // kPk × 2 × 2 KB
-    bar_off = pk_off + (size_t)kPk * 2 * kTileBytes;       // barriers, TMEM slot, abort flag
-    total = bar_off + 512 + 1024;                          // + slack for the 1024-B base alignment
+    b_off = 0;                                         // kS × N·128 B (1024-aligned, N%8==0)
+    pk_off = b_off + (size_t)kS * N * 128;             // kPk × sub × 2 KB
+    bar_off = pk_off + (size_t)kPk * sub * kTileBytes;
+    total = bar_off + 512 + 1024;                      // barriers/slots + 1024-B base alignment
   }
+  __host__ __device__ int mma_warp0() const { return 2; }
+  __host__ __device__ int dec_warp0() const { return 2 + sub; }
+  __host__ __device__ int threads() const { return 32 * (2 + sub + kNG * 4 * sub); }
+  // first A column: after the accumulators, 32-column aligned for tcgen05.st
+  __host__ __device__ uint32_t acol() const { return (uint32_t)(((sub * N + 31) / 32) * 32); }
 };
 
-// Ring depths for a given N: as deep a B ring as fits after 3 (else 2) A stages.
-static TcSmemLayout plan_smem(int N)
+// Two tiles when their accumulators and kS A-stages fit the 512 TMEM columns, else one.
+static TcPlan plan_tc(int N)
 {
-  for (int na = 3; na >= 2; --na)
-    for (int nb = kMaxRing; nb >= 2; --nb) {
-      TcSmemLayout L(N, na, nb);
-      if (L.total <= kSmemBudget) return L;
-    }
-  return TcSmemLayout(N, 2, 2);
+  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * kS <= 512) return TcPlan(N, 2);
+  return TcPlan(N, 1);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -97,19 +106,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
   return ok != 0;
 }
 
-// Bounded wait; on timeout sets `code` in *err and the CTA abort flag, returns false.
+// Bounded wait; on timeout sets `code` in *err and the CTA abort flag, returns false.  The abort
+// flag and the timer are looked at only every 64 polls, and `sleep_ns` > 0 makes a waiter back
+// off between polls, so waiting warps do not crowd the barrier and shared-memory pipes that the
+// MMA-issuing thread depends on.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code,
-                                          volatile int* abort_flag)
+                                          volatile int* abort_flag, uint32_t sleep_ns = 0)
 {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
-  while (true) {
+  for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (*abort_flag) return false;
-    if (globaltimer() - t0 > kWaitBudgetNs) {
-      atomicOr(err, code);
-      *abort_flag = 1;
-      return false;
+    if (sleep_ns) __nanosleep(sleep_ns);
+    if ((it & 63u) == 0) {
+      if (*abort_flag) return false;
+      if (globaltimer() - t0 > kWaitBudgetNs) {
+        atomicOr(err, code);
+        *abort_flag = 1;
+        return false;
+      }
     }
   }
 }
@@ -162,14 +177,15 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int N)
          | ((uint32_t)(128 >> 4) << 24);  // M / 16
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate)
+// D[tmem] (+)= A[tmem] · B[smem]
+__device__ __forceinline__ void mma_bf16_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate)
 {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -192,31 +208,43 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+// 32 consecutive TMEM columns of this warp's 32 lanes ← 32 registers per thread.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32])
+{
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+      "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(
+          taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+      "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+      "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+      "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1)
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
-               float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N,
-               int na, int nb, uint32_t tmem_cols, int* __restrict__ err)
+               float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
+               int* __restrict__ err)
 {
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment of the shared-window address (SWIZZLE_128B tiles need it)
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  const TcSmemLayout L(N, na, nb);
-  uint8_t* sA = smem + L.a_off;
-  uint8_t* sB = smem + L.b_off;
-  uint8_t* sPk = smem + L.pk_off;
-  uint64_t* pk_full = (uint64_t*)(smem + L.bar_off);
+  const TcPlan P(N, sub);
+  uint8_t* sB = smem + P.b_off;
+  uint8_t* sPk = smem + P.pk_off;
+  uint64_t* pk_full = (uint64_t*)(smem + P.bar_off);
   uint64_t* pk_empty = pk_full + kPk;
-  uint64_t* b_full = pk_empty + kPk;
-  uint64_t* b_empty = b_full + kMaxRing;
-  uint64_t* a_full = b_empty + kMaxRing;
-  uint64_t* a_empty = a_full + kMaxRing;
-  uint64_t* accum = a_empty + kMaxRing;
+  uint64_t* st_full = pk_empty + kPk;
+  uint64_t* st_empty = st_full + kS;
+  uint64_t* accum = st_empty + kS;
   uint32_t* tmem_slot = (uint32_t*)(accum + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int64_t mt0 = (int64_t)blockIdx.x * 2;   // first of the CTA's two 128-row tiles
+  const int dec_warps = sub * 4;               // decoder warps per group
+  const int64_t mt0 = (int64_t)blockIdx.x * sub;
   const int split = blockIdx.y;
   const int kt0 = split * tiles_per_split;
   const int kt1 = min(K_tiles, kt0 + tiles_per_split);
@@ -225,22 +253,20 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   if (threadIdx.x == 0) {
     for (int s = 0; s < kPk; ++s) {
       mbar_init(&pk_full[s], 1);
-      mbar_init(&pk_empty[s], kDecWarps);
+      mbar_init(&pk_empty[s], dec_warps);
     }
-    for (int s = 0; s < kMaxRing; ++s) {
-      mbar_init(&b_full[s], 1);
-      mbar_init(&b_empty[s], 1);
-      mbar_init(&a_full[s], kDecWarps);
-      mbar_init(&a_empty[s], 1);
+    for (int s = 0; s < kS; ++s) {
+      mbar_init(&st_full[s], dec_warps + 1);   // decoder warps + the B producer's expect_tx
+      mbar_init(&st_empty[s], sub);            // one commit per MMA warp
     }
-    mbar_init(accum, 1);
+    mbar_init(accum, sub);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(tmem_cols)
+                 "r"(512)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -248,6 +274,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem_base = *tmem_slot;
+  const uint32_t acol = P.acol();
 
   if (warp == 0) {
     // ---------------- packed-tile producer (DRAM) ----------------
@@ -256,14 +283,14 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       for (int i = 0; i < nk; ++i) {
         const int s = i % kPk;
         const uint32_t round = (uint32_t)(i / kPk);
-        if (i >= kPk && !mbar_wait(&pk_empty[s], (round - 1) & 1, err, 1, abort_flag)) break;
+        if (i >= kPk && !mbar_wait(&pk_empty[s], (round - 1) & 1, err, 1, abort_flag, 128)) break;
         if (*abort_flag) break;
-        mbar_arrive_expect_tx(&pk_full[s], 2u * kTileBytes);
+        mbar_arrive_expect_tx(&pk_full[s], (uint32_t)(sub * kTileBytes));
         const int kt = kt0 + i;
-        uint8_t* dst = sPk + (size_t)s * 2 * kTileBytes;
-        bulk_copy_g2s(dst, A + ((size_t)mt0 * K_tiles + kt) * kTileBytes, kTileBytes, &pk_full[s]);
-        bulk_copy_g2s(dst + kTileBytes, A + ((size_t)(mt0 + 1) * K_tiles + kt) * kTileBytes, kTileBytes,
-                      &pk_full[s]);
+        uint8_t* dst = sPk + (size_t)s * sub * kTileBytes;
+        for (int t = 0; t < sub; ++t)
+          bulk_copy_g2s(dst + t * kTileBytes, A + ((size_t)(mt0 + t) * K_tiles + kt) * kTileBytes, kTileBytes,
+                        &pk_full[s]);
         ++issued;
       }
       if (*abort_flag)   // let issued copies land before the CTA's shared memory is released
@@ -276,88 +303,95 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       const uint32_t bytes = (uint32_t)N * 128u;
       int issued = 0;
       for (int i = 0; i < nk; ++i) {
-        const int s = i % nb;
-        const uint32_t round = (uint32_t)(i / nb);
-        if (i >= nb && !mbar_wait(&b_empty[s], (round - 1) & 1, err, 16, abort_flag)) break;
+        const int s = i % kS;
+        const uint32_t round = (uint32_t)(i / kS);
+        if (i >= kS && !mbar_wait(&st_empty[s], (round - 1) & 1, err, 16, abort_flag, 128)) break;
         if (*abort_flag) break;
-        mbar_arrive_expect_tx(&b_full[s], bytes);
-        tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, &b_full[s]);
+        mbar_arrive_expect_tx(&st_full[s], bytes);
+        tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, &st_full[s]);
         ++issued;
       }
       if (*abort_flag)
-        for (int i = max(0, issued - nb); i < issued; ++i)
-          mbar_wait_drain(&b_full[i % nb], (uint32_t)(i / nb) & 1);
+        for (int i = max(0, issued - kS); i < issued; ++i)
+          mbar_wait_drain(&st_full[i % kS], (uint32_t)(i / kS) & 1);
     }
-  } else if (warp == 2) {
-    // ---------------- MMA issuer ----------------
+  } else if (warp < P.dec_warp0()) {
+    // ---------------- MMA issuer for tile t ----------------
+    const int t = warp - P.mma_warp0();
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16(N);
+      const uint64_t bdesc0 = sw128_desc(smem_u32(sB));
+      const uint32_t bstep = (uint32_t)(N * 128) >> 4;          // descriptor units per B stage
+      const uint32_t d_tmem = tmem_base + (uint32_t)(t * N);
+      const uint32_t a_base = tmem_base + acol + (uint32_t)(t * 32);
+      const uint32_t a_step = (uint32_t)(sub * 32);             // columns per A stage
+      int s = 0;
+      uint32_t phase = 0;
       for (int i = 0; i < nk; ++i) {
-        const int sa = i % na, sb = i % nb;
-        if (!mbar_wait(&a_full[sa], (uint32_t)(i / na) & 1, err, 2, abort_flag)) break;
-        if (!mbar_wait(&b_full[sb], (uint32_t)(i / nb) & 1, err, 32, abort_flag)) break;
+        if (!mbar_wait(&st_full[s], phase, err, 2, abort_flag)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a0 = smem_u32(sA + (size_t)sa * 2 * kTileA);
-        const uint32_t b0 = smem_u32(sB + (size_t)sb * N * 128);
-#pragma unroll
-        for (int t = 0; t < 2; ++t)
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(tmem_base + (uint32_t)(t * N), sw128_desc(a0 + t * kTileA + kk * 32),
-                     sw128_desc(b0 + kk * 32), idesc, (i > 0 || kk > 0) ? 1u : 0u);
-        mma_commit(&a_empty[sa]);
-        mma_commit(&b_empty[sb]);
+        const uint64_t bd = bdesc0 + (uint64_t)(s * bstep);
+        const uint32_t ad = a_base + (uint32_t)s * a_step;
+        mma_bf16_ts(d_tmem, ad, bd, idesc, i > 0 ? 1u : 0u);
+        mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
+        mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
+        mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
+        mma_commit(&st_empty[s]);
+        if (++s == kS) {
+          s = 0;
+          phase ^= 1u;
+        }
       }
-      mma_commit(accum);   // arrives once every MMA issued above has completed
+      mma_commit(accum);   // arrives once every MMA this thread issued has completed
     }
   } else {
-    // ---------------- decoders (thread → one row of the 256), then epilogue ----------------
-    const int t = threadIdx.x - 96;        // 0..255
-    const int sub = t >> 7, r = t & 127;   // tile 0/1, row in tile
-    for (int i = 0; i < nk; ++i) {
-      const int sp = i % kPk, sa = i % na;
-      bool got = mbar_wait(&pk_full[sp], (uint32_t)(i / kPk) & 1, err, 4, abort_flag);
+    // ---------------- decoders (one row per thread), then epilogue ----------------
+    const int dw = warp - P.dec_warp0();     // decoder warp index
+    const int grp = dw / dec_warps;          // group: stages i ≡ grp (mod kNG)
+    const int tsub = (dw % dec_warps) >> 2;  // tile 0 … sub−1
+    const int lq = warp & 3;                 // TMEM lane quarter = row quarter
+    const int r = lq * 32 + lane;            // row within the tile
+    for (int i = grp; i < nk; i += kNG) {
+      const int sp = i % kPk, s = i % kS;
+      bool got = mbar_wait(&pk_full[sp], (uint32_t)(i / kPk) & 1, err, 4, abort_flag, 64);
       if (!__all_sync(0xffffffffu, got)) break;   // warp-uniform exit
-      const uint4 pk = *reinterpret_cast<const uint4*>(sPk + ((size_t)sp * 2 + sub) * kTileBytes + r * 16);
+      const uint4 pk = *reinterpret_cast<const uint4*>(sPk + ((size_t)sp * sub + tsub) * kTileBytes + r * 16);
       __syncwarp();
       if (lane == 0) mbar_arrive(&pk_empty[sp]);
-      if (i >= na) {
-        got = mbar_wait(&a_empty[sa], (uint32_t)(i / na - 1) & 1, err, 64, abort_flag);
-        if (!__all_sync(0xffffffffu, got)) break;
-      }
-      uint8_t* rowp = sA + ((size_t)sa * 2 + sub) * kTileA + r * 128;
+      uint32_t v[32];
       const uint32_t words[4] = {pk.x, pk.y, pk.z, pk.w};
 #pragma unroll
-      for (int w = 0; w < 4; ++w) {
+      for (int w = 0; w < 4; ++w)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int chunk = 2 * w + h;   // 16-byte chunk of the 128-byte row
-          *reinterpret_cast<uint4*>(rowp + ((chunk ^ (r & 7)) << 4)) = bf16x8_of(words[w], h);
-        }
+        for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
+      if (i >= kS) {
+        got = mbar_wait(&st_empty[s], (uint32_t)(i / kS - 1) & 1, err, 64, abort_flag, 64);
+        if (!__all_sync(0xffffffffu, got)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tmem_st32(tmem_base + ((uint32_t)(lq * 32) << 16) + acol + (uint32_t)((s * sub + tsub) * 32), v);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(&a_full[sa]);
+      if (lane == 0) mbar_arrive(&st_full[s]);
     }
-    // epilogue: warps 3..6 read accumulator 0, warps 7..10 accumulator 1; each warp owns TMEM
-    // lanes 32·(warp%4) … +31 (its rows within the tile)
-    const int acc = (warp - 3) >> 2;
-    const int lq = warp & 3;
-    const int row = lq * 32 + lane;
-    const bool got = mbar_wait(accum, 0, err, 8, abort_flag);
-    const bool ok = __all_sync(0xffffffffu, got && !*abort_flag);   // tcgen05.ld is warp-wide
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-      float* Dbase = D + ((size_t)split * N) * M_pad + (mt0 + acc) * 128 + row;
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        uint32_t v[16];
-        tmem_ld16(tmem_base + ((uint32_t)(lq * 32) << 16) + (uint32_t)(acc * N + c0), v);
-        if (nk == 0) {
+    // epilogue (group 0): each warp owns its lane quarter of one tile's accumulator
+    if (grp == 0) {
+      const bool got = mbar_wait(accum, 0, err, 8, abort_flag, 256);
+      const bool ok = __all_sync(0xffffffffu, got && !*abort_flag);   // tcgen05.ld is warp-wide
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (ok) {
+        float* Dbase = D + ((size_t)split * N) * M_pad + (mt0 + tsub) * 128 + r;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          uint32_t o[16];
+          tmem_ld16(tmem_base + ((uint32_t)(lq * 32) << 16) + (uint32_t)(tsub * N + c0), o);
+          if (nk == 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = 0u;
+            for (int j = 0; j < 16; ++j) o[j] = 0u;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) Dbase[(size_t)(c0 + j) * M_pad] = __uint_as_float(o[j]);
         }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) Dbase[(size_t)(c0 + j) * M_pad] = __uint_as_float(v[j]);
       }
     }
   }
@@ -368,8 +402,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     if (*abort_flag && lane == 0) mbar_wait_drain(accum, 0);   // MMAs finished before freeing TMEM
     __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
-                 "r"(tmem_cols)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512)
                  : "memory");
   }
 }
@@ -394,12 +427,16 @@ static PFN_encodeTiled get_encode()
   return fn;
 }
 
+int gemm_tc_rows_per_cta(int N) { return plan_tc(N).sub * kTileM; }
+
 void gemm_tc(const GemmArgs& a, cudaStream_t st)
 {
   CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
-  CHECK_ARG(a.M_pad % (2 * kTileM) == 0 && a.K_pad % 128 == 0, "unpadded operand");
+  const TcPlan P = plan_tc(a.N);
+  CHECK_ARG(a.M_pad % (P.sub * kTileM) == 0 && a.K_pad % 128 == 0, "unpadded operand");
   CHECK_ARG(((uintptr_t)a.A % 16) == 0 && ((uintptr_t)a.B % 16) == 0, "misaligned operand");
-  const int64_t M2 = a.M_pad / (2 * kTileM);
+  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * kS <= 512, "no TMEM/shared-memory plan for this N");
+  const int64_t Mc = a.M_pad / (P.sub * kTileM);
   const int K_tiles = (int)(a.K_pad / kTileK);
   const int tps = (int)ceil_div(K_tiles, a.splits);
 
@@ -414,18 +451,16 @@ void gemm_tc(const GemmArgs& a, cudaStream_t st)
                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) SLEMM_THROW(SLEMM_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 
-  const TcSmemLayout L = plan_smem(a.N);
-  CHECK_ARG(L.total <= kSmemBudget, "shared-memory plan exceeds 227 KB");
-  static size_t configured = 0;
-  if (L.total > configured) {
+  static bool configured = false;
+  if (!configured) {
     CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
-    configured = kSmemBudget;
+    configured = true;
   }
-  // two accumulators of N columns: allocate the next power of two ≥ 2N (≤ 512)
-  const uint32_t cols = 2 * a.N <= 32 ? 32u : 2 * a.N <= 64 ? 64u : 2 * a.N <= 128 ? 128u : 2 * a.N <= 256 ? 256u : 512u;
-  dim3 grid((unsigned)M2, (unsigned)a.splits);
-  gemm_tc_kernel<<<grid, kThreads, L.total, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, L.na, L.nb, cols,
-                                                  a.err);
+  // Each CTA allocates all 512 TMEM columns: request enough shared memory that only one CTA is
+  // resident per SM, so no allocation ever has to wait for another CTA's release.
+  const size_t smem = std::max<size_t>(P.total, 120 * 1024);
+  dim3 grid((unsigned)Mc, (unsigned)a.splits);
+  gemm_tc_kernel<<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub, a.err);
   LAUNCH_CHECK();
 }
 

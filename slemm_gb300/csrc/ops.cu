@@ -291,7 +291,7 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
   p.pieces = g->prec == SLEMM_PREC_BF16X3 ? 3 : (g->prec == SLEMM_PREC_BF16X2 ? 2 : 1);
   p.N = p.tc ? (int)round_up((int64_t)p.pieces * k, 16) : k;
   const int64_t M_tiles = M_pad / kTileM, K_tiles = K_pad / kTileK;
-  p.splits = p.tc ? choose_splits(M_tiles / 2, K_tiles, 1, num_sms())
+  p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms())
                   : choose_splits(M_tiles, K_tiles, 8, num_sms());
   return p;
 }
