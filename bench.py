@@ -324,6 +324,7 @@ def run_gpu(args, cfg):
                    "l2": "inputs larger than L2 (packed Z 1.25 GB per pass)", "parallelism": "replicas"},
         "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
         "lanczos_steps": {"y": res["iters"][0], "Q": res["iters"][1], "V": res["iters"][2]},
+        "phases_s": res.get("phases"),
         "matvec_gbs": matvec_gbs,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches / max(args.steps, 1)),

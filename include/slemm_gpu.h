@@ -149,6 +149,10 @@ typedef struct {
   int   iters_y, iters_Q, iters_V;   /* Lanczos steps per seed system                     */
   int   n_criterion;      /* REML criterion (or first-order function) evaluations          */
   double seconds;         /* wall time inside the call                                     */
+  double t_setup;         /* QR, weights, probe or MC draws                                */
+  double t_seed;          /* Lanczos recurrence (operator applications)                    */
+  double t_search;        /* golden-section or secant search on h2                         */
+  double t_final;         /* BLUP, BLUE and copies back                                    */
 } slemm_reml_result;
 
 /* DF-REML with Rademacher probes + golden-section search (src/reml.cpp:549-690).

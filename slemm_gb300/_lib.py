@@ -30,7 +30,9 @@ class RemlOpts(ctypes.Structure):
 
 class RemlResult(ctypes.Structure):
     _fields_ = [("vg", F32), ("ve", F32), ("h2", F32), ("lrt", F32), ("iters_y", I32),
-                ("iters_Q", I32), ("iters_V", I32), ("n_criterion", I32), ("seconds", ctypes.c_double)]
+                ("iters_Q", I32), ("iters_V", I32), ("n_criterion", I32), ("seconds", ctypes.c_double),
+                ("t_setup", ctypes.c_double), ("t_seed", ctypes.c_double), ("t_search", ctypes.c_double),
+                ("t_final", ctypes.c_double)]
 
 
 _SIGS = {

@@ -184,7 +184,8 @@ class Genotypes:
                                             _ptr(blue), _ptr(vb), ctypes.byref(r)))
         return dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue,
                     var_blue=vb, iters=(r.iters_y, r.iters_Q, r.iters_V),
-                    n_criterion=r.n_criterion, seconds=r.seconds)
+                    n_criterion=r.n_criterion, seconds=r.seconds,
+                    phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
     def LMC_REML(self, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, s2min=1e-4,
                  maxit=600, verbose=False):
@@ -198,7 +199,8 @@ class Genotypes:
                                            _ptr(ps), ctypes.byref(o), _ptr(Py), _ptr(b),
                                            _ptr(blue), ctypes.byref(r)))
         return dict(vg=r.vg, ve=r.ve, h2=r.h2, Py=Py, snp_blup=b, blue=blue, iters=r.iters_V,
-                    n_criterion=r.n_criterion, seconds=r.seconds)
+                    n_criterion=r.n_criterion, seconds=r.seconds,
+                    phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
     def gebv(self, alpha, flip=None):
         """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""

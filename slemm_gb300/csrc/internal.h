@@ -65,6 +65,11 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
 // Solve for the columns of group `grp`; X has that group's columns (ld = ldx) on device.
 int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp);
 void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2);
+// L_Solve coefficients of group grp at shift σ (X = Σ_i coef[i·tc+c]·V_i[:,c], V_0 = B, V_i = U_i).
+int solve_coeffs(const slemm_lseed* S, double sigma, double tol, int grp, std::vector<double>& coef);
+// Inner products B[:,a]ᵀV_i[:,b] for i = 0 … J and each (a, b) pair (V_0 = B), host result
+// mom[i·npairs + p].
+void lanczos_moments(slemm_lseed* S, const std::vector<std::pair<int, int>>& pairs, int J, std::vector<double>& mom);
 // Accessors of the seed object (defined in lanczos.cu).
 int lseed_iters(const slemm_lseed* S, int grp);
 const double* lseed_delta(const slemm_lseed* S);   // iters × t (row j = step j)

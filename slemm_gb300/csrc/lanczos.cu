@@ -373,14 +373,13 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
   return S;
 }
 
-// X = (A + σI)^{-1}B for the columns of group `grp` (all columns when the seed has one group),
-// using at most that group's basis; X on device (tc columns, ld = ldx).  Returns the CG steps.
-int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp)
+// Coefficients of L_Solve for group `grp` at shift σ: X = Σ_i coef[i·tc + c]·V_i[:,c] with
+// V_0 = B and V_i = U_i (i ≥ 1), i < steps.  Returns steps.
+int solve_coeffs(const slemm_lseed* S, double sigma, double tol, int grp, std::vector<double>& coef)
 {
   const int t = S->t;
   const int c0 = S->group_start[grp], tc = S->group_start[grp + 1] - c0;
   const int J = S->group_iters[grp];
-  cudaStream_t st = S->g->stream;
   // forward pass: γ, ω, ρ with the reference's stopping rule (src/reml.cpp:404-426)
   std::vector<double> gam((size_t)(J + 1) * tc, 0.0), om((size_t)(J + 1) * tc, 0.0), rho((size_t)(J + 1) * tc, 0.0);
   for (int c = 0; c < tc; ++c) rho[c] = S->bnorm[c0 + c];
@@ -402,7 +401,7 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
   }
   // backward pass: S_i = γ_i + ω_i S_{i+1}; X = S_0 B + Σ_{i=1}^{steps-1} ρ_i S_i U_i
   // (the R and P of the last step are not folded into X: X is updated before R).
-  std::vector<double> coef((size_t)steps * tc, 0.0);
+  coef.assign((size_t)steps * tc, 0.0);
   std::vector<double> Sacc(tc, 0.0);
   for (int i = steps - 1; i >= 0; --i) {
     for (int c = 0; c < tc; ++c) {
@@ -410,6 +409,62 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
       coef[(size_t)i * tc + c] = (i == 0) ? Sacc[c] : rho[(size_t)i * tc + c] * Sacc[c];
     }
   }
+  return steps;
+}
+
+// mom[i·npairs + p] = Σ_r B[r, a_p]·V_i[r, b_p] for i = 0 … J (V_0 = B, V_i = U_i); FP64 sums of
+// the stored FP32 vectors, one pass over the basis.
+__global__ void lz_moments_kernel(const float* __restrict__ B, const float* const* __restrict__ blocks,
+                                  const int2* __restrict__ pairs, int npairs, int64_t n,
+                                  double* __restrict__ red, int nblk)
+{
+  __shared__ double sh[32];
+  const int p = blockIdx.y, i = blockIdx.z;
+  const int2 ab = pairs[p];
+  const float* Vi = (i == 0) ? B : blocks[i];
+  const int64_t r0 = (int64_t)blockIdx.x * kLzRows, r1 = min64(n, r0 + kLzRows);
+  double acc = 0.0;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+    acc += (double)B[(int64_t)ab.x * n + r] * (double)Vi[(int64_t)ab.y * n + r];
+  const double s = lz_block_sum(acc, sh);
+  if (threadIdx.x == 0) red[((int64_t)i * npairs + p) * nblk + blockIdx.x] = s;
+}
+
+void lanczos_moments(slemm_lseed* S, const std::vector<std::pair<int, int>>& pairs, int J, std::vector<double>& mom)
+{
+  const int npairs = (int)pairs.size();
+  CHECK_ARG(J >= 0 && J <= S->iters && npairs >= 1, "bad moments request");
+  cudaStream_t st = S->g->stream;
+  const int nblk = (int)ceil_div(S->n, kLzRows);
+  std::vector<const float*> hb(J + 1, nullptr);
+  for (int i = 1; i <= J; ++i) hb[i] = S->block(i);
+  std::vector<int2> hp(npairs);
+  for (int q = 0; q < npairs; ++q) hp[q] = make_int2(pairs[q].first, pairs[q].second);
+  DevBuf dblk, dpairs, dred, dout;
+  dblk.ensure(hb.size() * sizeof(float*));
+  dpairs.ensure(hp.size() * sizeof(int2));
+  const int nq = (J + 1) * npairs;
+  dred.ensure((size_t)nq * nblk * sizeof(double));
+  dout.ensure((size_t)nq * sizeof(double));
+  CUDA_TRY(cudaMemcpyAsync(dblk.p, hb.data(), hb.size() * sizeof(float*), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(dpairs.p, hp.data(), hp.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+  lz_moments_kernel<<<dim3(nblk, npairs, J + 1), 256, 0, st>>>(S->B.as<float>(), dblk.as<const float*>(),
+                                                               dpairs.as<int2>(), npairs, S->n, dred.as<double>(), nblk);
+  LAUNCH_CHECK();
+  lz_reduce(dred.as<double>(), nblk, nq, dout.as<double>(), st);
+  mom.resize(nq);
+  CUDA_TRY(cudaMemcpyAsync(mom.data(), dout.p, nq * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// X = (A + σI)^{-1}B for the columns of group `grp` (all columns when the seed has one group),
+// using at most that group's basis; X on device (tc columns, ld = ldx).  Returns the CG steps.
+int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp)
+{
+  const int c0 = S->group_start[grp], tc = S->group_start[grp + 1] - c0;
+  cudaStream_t st = S->g->stream;
+  std::vector<double> coef;
+  const int steps = solve_coeffs(S, sigma, tol, grp, coef);
   std::vector<const float*> hblocks(std::max(steps, 1));
   for (int i = 0; i < steps; ++i) hblocks[i] = (i == 0) ? nullptr : S->block(i);
   DevBuf& dcoef = S->solve_coef;

@@ -286,6 +286,10 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
                float* blue_out, float* var_blue_out, slemm_reml_result* res)
 {
   const auto t_start = std::chrono::steady_clock::now();
+  auto stamp = [&]() {
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  };
   const int64_t n = g->n, m = g->m;
   const bool verbose = o.verbose != 0;
   if (verbose) printf("\nStarted stochastic Lanczos DF-REML.\n");
@@ -324,6 +328,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   upload(g, d_QV.as<float>(), QV.data(), (size_t)n * (1 + c));
   // Rademacher probes (src/reml.cpp:597-605), the reference's mt19937 draws generated on the GPU
   rademacher_device(o.seed, n, n_V, d_QV.as<float>() + (size_t)(1 + c) * n, n, g->stream);
+  const double t_a = stamp();
   double* d_scal = d_tmp.as<double>();
 
   const float tau0 = (1.0f - o.s2max) / o.s2max;
@@ -332,6 +337,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
                                           verbose, {1, c, n_V}, 5, 1);
   std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold(seed, lseed_free);
   constexpr int GY = 0, GQ = 1, GV = 2;
+  const double t_b = stamp();
   const int nld = lseed_iters(seed, GV);
   // Jacobi matrices of the probes (columns 1+c ... c+n_V), src/reml.cpp:638-646
   std::vector<double> dl((size_t)n_V * nld), bt((size_t)n_V * (nld + 1));
@@ -346,18 +352,29 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   std::vector<double> DV((size_t)n_V * nld), W2((size_t)n_V * nld);
   tridiag_eig_host(dl.data(), bt.data(), n_V, nld, DV.data(), W2.data());
 
-  // ySy
-  col_dots(g, d_y.as<float>(), n, nullptr, 0, n, 1, d_scal);
-  const double ySy = d2h(g, d_scal, 1)[0];
+  // Moments of the stored basis: every shifted solve the criterion needs is a combination
+  // X = Σ_i coef_i·V_i of the seed vectors (V_0 = the right-hand side), so yᵀX and QᵀX follow
+  // from the inner products y·V_i[:,0] and Q_k·V_i[:,1+l], computed once here in one pass.
+  const int Jy = lseed_iters(seed, GY), JQ = lseed_iters(seed, GQ);
+  const int Jm = std::max(Jy, JQ);
+  std::vector<std::pair<int, int>> pairs;
+  pairs.push_back({0, 0});
+  for (int k = 0; k < c; ++k)
+    for (int l = 0; l < c; ++l) pairs.push_back({1 + k, 1 + l});
+  const int npairs = (int)pairs.size();
+  std::vector<double> mom;
+  lanczos_moments(seed, pairs, Jm, mom);
+  const double ySy = mom[0];
   int n_eval = 0;
   // REML_criterion (src/reml.cpp:457-489)
   auto criterion = [&](float ss) -> Criterion {
     ++n_eval;
     const float tau = (1 - ss) / ss;
     const float sigma = tau - tau0;
-    lanczos_solve_device(seed, (double)sigma, 1e-6, d_X.as<float>(), n, GY);
-    col_dots(g, d_y.as<float>(), n, d_X.as<float>(), n, n, 1, d_scal);
-    const double yPy = d2h(g, d_scal, 1)[0];
+    std::vector<double> cy, cq;
+    const int sy = solve_coeffs(seed, (double)sigma, 1e-6, GY, cy);
+    double yPy = 0.0;
+    for (int i = 0; i < sy; ++i) yPy += cy[i] * mom[(size_t)i * npairs];
     Criterion r;
     r.vg = yPy / (double)(n - c);
     r.ve = r.vg * tau;
@@ -365,9 +382,12 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     for (size_t q = 0; q < DV.size(); ++q) ldet_H += W2[q] * std::log(DV[q] + sigma);
     ldet_H = ldet_H * (double)n / (double)n_V;
     r.lrt = (double)n * std::log(ySy / yPy) - ldet_H;
-    lanczos_solve_device(seed, (double)sigma, 1e-6, d_X.as<float>(), n, GQ);
-    proj_coeffs(g, d_X.as<float>(), n, c, d_scal);
-    std::vector<double> M = d2h(g, d_scal, (size_t)c * c);
+    const int sq = solve_coeffs(seed, (double)sigma, 1e-6, GQ, cq);
+    std::vector<double> M((size_t)c * c, 0.0);   // M[k][l] = Q_kᵀ X_l, row-major
+    for (int i = 0; i < sq; ++i)
+      for (int k = 0; k < c; ++k)
+        for (int l = 0; l < c; ++l)
+          M[(size_t)k * c + l] += cq[(size_t)i * c + l] * mom[(size_t)i * npairs + 1 + k * c + l];
     r.slogLL = (double)(n - c) * std::log(ySy / yPy) - logabsdet(M, c) - ldet_H;
     return r;
   };
@@ -408,6 +428,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   const float vg = (float)last.vg, ve = (float)last.ve, lrt = (float)last.lrt;
   const float tau1 = ve / vg;
 
+  const double t_c = stamp();
   // Py = rr∘(I−QQᵀ)L_Solve(seed_y, y_proj, τ1−τ0)   (src/reml.cpp:659-661)
   float* d_Py = d_X.as<float>();
   lanczos_solve_device(seed, (double)(tau1 - tau0), 1e-6, d_Py, n, GY);
@@ -484,7 +505,11 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     res->iters_Q = lseed_iters(seed, GQ);
     res->iters_V = nld;
     res->n_criterion = n_eval;
-    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    res->seconds = stamp();
+    res->t_setup = t_a;
+    res->t_seed = t_b - t_a;
+    res->t_search = t_c - t_b;
+    res->t_final = res->seconds - t_c;
   }
 }
 
@@ -496,6 +521,10 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
               float* blue_out, slemm_reml_result* res)
 {
   const auto t_start = std::chrono::steady_clock::now();
+  auto stamp = [&]() {
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  };
   const int64_t n = g->n, m = g->m;
   const bool verbose = o.verbose != 0;
   if (verbose) printf("\nStarted Lanczos MC-REML.\n");
@@ -538,6 +567,7 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
   proj_coeffs(g, d_V.as<float>(), n, tV, d_scal);
   proj_apply(g, d_V.as<float>(), n, tV, d_scal);
 
+  const double t_a = stamp();
   const float tau0 = (1.0f - o.s2max) / o.s2max;
   if (verbose) printf("\nPerforming Lanczos decomposition:\n");
   slemm_lseed* seed_V = lanczos_seed_device(g, SLEMM_OP_QUADFORM, tau0, d_V.as<float>(), tV, 10 * o.tol_L,
@@ -568,6 +598,7 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
     }
     return (float)std::log((u0 / e0) / (us / es));
   };
+  const double t_b = stamp();
   if (verbose) printf("\nSecant iterations:\n");
   float s2 = o.s2max / 2;
   float log_tau1 = std::log((1 - s2) / s2);
@@ -591,6 +622,7 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
   }
   if (verbose && std::fabs(f2) > 0.005)
     printf("\nWarning: secant iterations not converged. h2 close to 0 or small sample size?\n");
+  const double t_c = stamp();
   // Py = PyMC[:,0]; vg = y·Py/(n−c); ve = τ1·vg   (src/reml.cpp:855-858)
   float* d_Py0 = d_Py.as<float>();
   {
@@ -652,7 +684,11 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
     res->iters_y = res->iters_Q = 0;
     res->iters_V = lseed_iters(seed_V, 0);
     res->n_criterion = n_eval;
-    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    res->seconds = stamp();
+    res->t_setup = t_a;
+    res->t_seed = t_b - t_a;
+    res->t_search = t_c - t_b;
+    res->t_final = res->seconds - t_c;
   }
 }
 
