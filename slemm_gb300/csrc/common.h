@@ -79,16 +79,27 @@ inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 __host__ __device__ inline int64_t ceil_div(int64_t x, int64_t a) { return (x + a - 1) / a; }
 
 // ---- device buffer -----------------------------------------------------------------------------
+// Plain buffers use cudaMalloc/cudaFree.  A buffer bound to a stream (DevBuf(stream)) is
+// allocated and freed stream-ordered from the device's default memory pool, whose release
+// threshold configure_pool raises so that freed blocks stay cached for the next fit: such
+// allocations cost no device synchronisation.  A stream-bound buffer must be released before its
+// stream is destroyed.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  bool ordered = false;
   DevBuf() = default;
+  explicit DevBuf(cudaStream_t s) : stream(s), ordered(true) {}
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release()
   {
-    if (p) cudaFree(p);
+    if (p) {
+      if (ordered) cudaFreeAsync(p, stream);
+      else cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -98,11 +109,11 @@ struct DevBuf {
     if (nbytes <= bytes) return p;
     release();
     if (nbytes == 0) return nullptr;
-    cudaError_t e = cudaMalloc(&p, nbytes);
+    cudaError_t e = ordered ? cudaMallocAsync(&p, nbytes, stream) : cudaMalloc(&p, nbytes);
     if (e != cudaSuccess) {
       p = nullptr;
-      throw Error{SLEMM_ERR_NOMEM, "cudaMalloc(" + std::to_string(nbytes) + ") -> " +
-                                       cudaGetErrorString(e)};
+      throw Error{SLEMM_ERR_NOMEM, std::string(ordered ? "cudaMallocAsync(" : "cudaMalloc(") +
+                                       std::to_string(nbytes) + ") -> " + cudaGetErrorString(e)};
     }
     bytes = nbytes;
     return p;
@@ -110,6 +121,39 @@ struct DevBuf {
   template <class T>
   T* as() const { return static_cast<T*>(p); }
 };
+// Small page-locked host array mapped into the device address space: kernels write scalars that
+// the host reads after a stream synchronisation, without a separate copy.
+struct HostScal {
+  double* h = nullptr;   // host view
+  double* d = nullptr;   // device view
+  size_t count = 0;
+  HostScal() = default;
+  HostScal(const HostScal&) = delete;
+  HostScal& operator=(const HostScal&) = delete;
+  ~HostScal()
+  {
+    if (h) cudaFreeHost(h);
+  }
+  double* ensure(size_t n)
+  {
+    if (n <= count) return d;
+    if (h) cudaFreeHost(h);
+    h = d = nullptr;
+    count = 0;
+    cudaError_t e = cudaHostAlloc((void**)&h, n * sizeof(double), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&d, h, 0);
+    if (e != cudaSuccess) {
+      if (h) cudaFreeHost(h);
+      h = d = nullptr;
+      throw Error{SLEMM_ERR_NOMEM, std::string("cudaHostAlloc -> ") + cudaGetErrorString(e)};
+    }
+    count = n;
+    return d;
+  }
+};
+
+// Keeps freed stream-ordered blocks of the device's default pool cached (idempotent).
+void configure_pool(int device);
 
 // ---- packed product plan ------------------------------------------------------------------------
 // D[M_pad × N] = Cnt[M_pad × K_pad] · B where the count matrix is a tiled 2-bit packed array

@@ -24,6 +24,19 @@ std::atomic<int64_t> g_launches{0};
 static thread_local std::string t_last_error;
 void set_error(const std::string& msg) { t_last_error = msg; }
 
+void configure_pool(int device)
+{
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  cudaMemPool_t pool;
+  CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t keep = UINT64_MAX;   // this process's pool only: freed blocks stay cached for reuse
+  CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  done.push_back(device);
+}
+
 int num_sms()
 {
   static int sms = 0;
@@ -171,6 +184,7 @@ int slemm_gpu_init(int device)
     if (!(p.major == 10 && p.minor == 3))
       SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "this build targets sm_103a; device is sm_" +
                                              std::to_string(p.major) + std::to_string(p.minor));
+    configure_pool(device);
   });
 }
 
@@ -196,6 +210,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
     auto* g = new slemm_geno();
     try {
       CUDA_TRY(cudaGetDevice(&g->device));
+      configure_pool(g->device);
       CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
       g->own_stream = true;
       g->n = n;

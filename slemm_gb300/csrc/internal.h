@@ -22,6 +22,7 @@ struct slemm_geno {
   // work buffers
   slemm::DevBuf ws_B, ws_D, ws_red, ws_small, ws_T, ws_in, ws_out;
   slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
+  slemm::HostScal scal;           // mapped host scalars of the Lanczos steps
   // optional per-launch timing of the packed products (CUDA events on `stream`)
   struct GemmRecord {
     cudaEvent_t start, stop;

@@ -1,9 +1,13 @@
 // lanczos.cu — Lanczos seed systems, shifted solves and the batched tridiagonal eigensolve.
 //
 // L_Seed (src/reml.cpp:246-339): per-column Lanczos on a block B (n×t) with the operator of
-// ops.cu.  The basis vectors are FP32 in HBM like the reference's std::vector<MatrixXf>; every
+// ops.cu.  The basis vectors are FP32 in HBM like the reference's std::vector<MatrixXf>; the
+// vector updates run in FP32 (with the FP64 scalars applied as double-float pairs) and every
 // scalar of the three-term recurrence (δ = uᵀAu, β = ‖·‖, the CG coefficients γ, ω, ρ and the
-// residual test) is accumulated and kept in FP64.
+// residual test) is accumulated to FP64 accuracy (reduce.cuh) and kept in FP64.  One step is
+// three vector kernels whose block partials the next kernel sums itself in a fixed order, and one
+// small kernel that writes the step's scalars into mapped host memory: one synchronisation per
+// step, no copies.
 //
 // L_Solve (src/reml.cpp:369-431): the reference rebuilds CG on (A + σI) from the stored basis
 // step by step.  Unrolling its recurrences (P_0 = B, P_j = ρ_j U_j + ω_{j−1} P_{j−1},
@@ -12,9 +16,10 @@
 // forms the weighted sum over the stored basis — one pass instead of one pass per step.
 //
 // Tridiagonal eigensolve (src/reml.cpp:638-646): per probe, implicit QL with Wilkinson shifts in
-// FP64, one thread per probe, tracking only the first row of the eigenvector matrix (all the
-// quadrature needs).
+// FP64 on the host (a few hundred flops per probe), tracking only the first row of the
+// eigenvector matrix (all the quadrature needs).
 #include "internal.h"
+#include "reduce.cuh"
 
 #include <chrono>
 
@@ -25,6 +30,7 @@ struct slemm_lseed {
   int t = 0;
   int iters = 0;   // j: basis holds U_0 … U_j
   int64_t n = 0;
+  cudaStream_t st = nullptr;                 // the handle's stream: buffers are stream-ordered on it
   static constexpr int kChunk = 16;          // basis blocks per allocation
   std::vector<slemm::DevBuf*> chunks;        // each holds kChunk blocks of n×t FP32
   slemm::DevBuf B;                           // right-hand side block (n×t)
@@ -44,7 +50,7 @@ struct slemm_lseed {
   {
     const int c = j / kChunk;
     while ((int)chunks.size() <= c) {
-      auto* b = new slemm::DevBuf();
+      auto* b = new slemm::DevBuf(st);
       b->ensure((size_t)kChunk * n * t * sizeof(float));
       chunks.push_back(b);
     }
@@ -54,95 +60,130 @@ struct slemm_lseed {
 
 namespace slemm {
 
-constexpr int kLzRows = 4096;
+constexpr int kLzRows = 4096;     // rows of one block of the vector kernels
+constexpr int kLzThreads = 256;
 
-__device__ __forceinline__ double lz_block_sum(double v, double* sh)
-{
-  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
-  return r;
-}
-
-// tmp ← tmp − U_prev·β (β = nullptr at j = 0); red[c][blk] = Σ U_cur·tmp
-__global__ void lz_dot_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur,
-                              const float* __restrict__ Uprev, const double* __restrict__ beta,
-                              int64_t n, double* __restrict__ red, int nblk)
+// red[c][blk] = Σ src²  (norm partials of the right-hand side)
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_norm_kernel(const float* __restrict__ src, int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
-  const double b = beta ? beta[c] : 0.0;
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
+    float x[V];
+    ldv<V>(src + (int64_t)c * n + i, x);
+#pragma unroll
+    for (int q = 0; q < V; ++q) df_fma(acc, x[q], x[q]);
+  }
+  const double s = block_sum_d(df_value(acc), sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
+// tmp ← tmp − β·U_prev with β = √(Σ nrm_prev partials) (skipped at step 0);
+// red_dot[c][blk] = Σ U_cur·tmp
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_dot_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur, const float* __restrict__ Uprev,
+              const double* __restrict__ nrm_prev, int64_t n, double* __restrict__ red, int nblk)
+{
+  __shared__ double sh[32];
+  __shared__ float sb[2];
+  const int c = blockIdx.y;
+  float bh = 0.f, bl = 0.f;
+  if (Uprev) block_scalar([&] { return sqrt(sum_partials(nrm_prev + (int64_t)c * nblk, nblk)); }, sb, bh, bl);
+  const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
     const int64_t o = (int64_t)c * n + i;
-    double x = tmp[o];
+    float x[V], u[V];
+    ldv<V>(tmp + o, x);
+    ldv<V>(Ucur + o, u);
     if (Uprev) {
-      x -= (double)Uprev[o] * b;
-      tmp[o] = (float)x;
-      x = (double)(float)x;
+      float p[V];
+      ldv<V>(Uprev + o, p);
+#pragma unroll
+      for (int q = 0; q < V; ++q) x[q] = __fmaf_rn(-bl, p[q], __fmaf_rn(-bh, p[q], x[q]));
+      stv<V>(tmp + o, x);
     }
-    acc += (double)Ucur[o] * x;
+#pragma unroll
+    for (int q = 0; q < V; ++q) df_fma(acc, u[q], x[q]);
   }
-  const double s = lz_block_sum(acc, sh);
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// tmp ← tmp − U_cur·δ; red[c][blk] = Σ tmp²
-__global__ void lz_orth_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur,
-                               const double* __restrict__ delta, int64_t n,
-                               double* __restrict__ red, int nblk)
+// tmp ← tmp − δ·U_cur with δ = Σ dot partials; red_nrm[c][blk] = Σ tmp²
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_orth_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur, const double* __restrict__ dot,
+               int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
+  __shared__ float sb[2];
   const int c = blockIdx.y;
+  float dh, dlo;
+  block_scalar([&] { return sum_partials(dot + (int64_t)c * nblk, nblk); }, sb, dh, dlo);
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
-  const double d = delta[c];
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
     const int64_t o = (int64_t)c * n + i;
-    const float x = (float)((double)tmp[o] - (double)Ucur[o] * d);
-    tmp[o] = x;
-    acc += (double)x * (double)x;
+    float x[V], u[V];
+    ldv<V>(tmp + o, x);
+    ldv<V>(Ucur + o, u);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      x[q] = __fmaf_rn(-dlo, u[q], __fmaf_rn(-dh, u[q], x[q]));
+      df_fma(acc, x[q], x[q]);
+    }
+    stv<V>(tmp + o, x);
   }
-  const double s = lz_block_sum(acc, sh);
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// U_next ← src / scale (scale = sqrt(nrm2)); red[c][blk] = Σ U_next²
-__global__ void lz_scale_kernel(float* __restrict__ Unext, const float* __restrict__ src,
-                                const double* __restrict__ nrm2, int64_t n,
-                                double* __restrict__ red, int nblk)
+// U_next ← src / √(Σ nrm partials); red_un[c][blk] = Σ U_next²
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_scale_kernel(float* __restrict__ Unext, const float* __restrict__ src, const double* __restrict__ nrm,
+                int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
+  __shared__ float sb[2];
   const int c = blockIdx.y;
+  float ih, il;
+  block_scalar([&] { return 1.0 / sqrt(sum_partials(nrm + (int64_t)c * nblk, nblk)); }, sb, ih, il);
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
-  const double inv = 1.0 / sqrt(nrm2[c]);
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
     const int64_t o = (int64_t)c * n + i;
-    const float x = (float)((double)src[o] * inv);
-    Unext[o] = x;
-    acc += (double)x * (double)x;
+    float x[V];
+    ldv<V>(src + o, x);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      x[q] = __fmaf_rn(x[q], ih, __fmul_rn(x[q], il));
+      df_fma(acc, x[q], x[q]);
+    }
+    stv<V>(Unext + o, x);
   }
-  const double s = lz_block_sum(acc, sh);
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-__global__ void lz_reduce_kernel(const double* __restrict__ red, int nblk, int t,
-                                 double* __restrict__ out)
+// out[c] = Σ dot, out[t+c] = Σ nrm, out[2t+c] = Σ un (the consumers' order); out[3t] = error word.
+__global__ void lz_final_kernel(const double* __restrict__ dot, const double* __restrict__ nrm,
+                                const double* __restrict__ un, int t, int nblk, const int* __restrict__ err,
+                                double* __restrict__ out)
 {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= t) return;
-  double s = 0.0;
-  for (int b = lane; b < nblk; b += 32) s += red[(int64_t)c * nblk + b];
-  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) out[c] = s;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < t) {
+    out[c] = dot ? sum_partials(dot + (int64_t)c * nblk, nblk) : 0.0;
+    out[t + c] = sum_partials(nrm + (int64_t)c * nblk, nblk);
+    out[2 * t + c] = sum_partials(un + (int64_t)c * nblk, nblk);
+  }
+  if (c == 0) out[3 * t] = (double)*err;
 }
 
 // X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]   (FP64 accumulation)
@@ -158,73 +199,6 @@ __global__ void lz_combine_kernel(float* __restrict__ X, int64_t ldx, const floa
   double acc = coef[c] * (double)B[o];
   for (int j = 1; j <= J; ++j) acc += coef[(int64_t)j * tc + c] * (double)blocks[j][o];
   X[(int64_t)c * ldx + i] = (float)acc;
-}
-
-// Batched implicit QL on symmetric tridiagonal matrices, first eigenvector row only.
-// d: t×nld diagonals (column-major in t), e: t×nld off-diagonals e[0..nld−2] (e[nld−1] = 0).
-__global__ void tridiag_ql_kernel(double* __restrict__ d, double* __restrict__ e,
-                                  double* __restrict__ z, int t, int nld, int* __restrict__ fail)
-{
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= t) return;
-  auto D = [&](int i) -> double& { return d[(int64_t)i * t + p]; };
-  auto E = [&](int i) -> double& { return e[(int64_t)i * t + p]; };
-  auto Z = [&](int i) -> double& { return z[(int64_t)i * t + p]; };
-  for (int i = 0; i < nld; ++i) Z(i) = (i == 0) ? 1.0 : 0.0;
-  if (nld > 0) E(nld - 1) = 0.0;
-  const double eps = 2.220446049250313e-16;
-  for (int l = 0; l < nld; ++l) {
-    for (int iter = 0;; ++iter) {
-      int mm = l;
-      for (; mm < nld - 1; ++mm) {
-        const double dd = fabs(D(mm)) + fabs(D(mm + 1));
-        if (fabs(E(mm)) <= eps * dd) break;
-      }
-      if (mm == l) break;
-      if (iter >= 64) {
-        atomicOr(fail, 1);
-        break;
-      }
-      // Wilkinson-type shift from the leading 2×2 block
-      double g = (D(l + 1) - D(l)) / (2.0 * E(l));
-      double r = hypot(g, 1.0);
-      g = D(mm) - D(l) + E(l) / (g + (g >= 0 ? r : -r));
-      double s = 1.0, c = 1.0, pp = 0.0;
-      int i = mm - 1;
-      bool deflated = false;
-      for (; i >= l; --i) {
-        const double f = s * E(i), b = c * E(i);
-        r = hypot(f, g);
-        E(i + 1) = r;
-        if (r == 0.0) {
-          D(i + 1) -= pp;
-          E(mm) = 0.0;
-          deflated = true;
-          break;
-        }
-        s = f / r;
-        c = g / r;
-        g = D(i + 1) - pp;
-        r = (D(i) - g) * s + 2.0 * c * b;
-        pp = s * r;
-        D(i + 1) = g + pp;
-        g = c * r - b;
-        const double zf = Z(i + 1);
-        Z(i + 1) = s * Z(i) + c * zf;
-        Z(i) = c * Z(i) - s * zf;
-      }
-      if (deflated) continue;
-      D(l) -= pp;
-      E(l) = g;
-      E(mm) = 0.0;
-    }
-  }
-}
-
-static void lz_reduce(const double* red, int nblk, int t, double* out, cudaStream_t st)
-{
-  lz_reduce_kernel<<<(unsigned)ceil_div(t, 8), 256, 0, st>>>(red, nblk, t, out);
-  LAUNCH_CHECK();
 }
 
 }  // namespace slemm
@@ -256,6 +230,11 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
   auto* S = new slemm_lseed();
   try {
     S->g = g;
+    S->st = st;
+    for (slemm::DevBuf* b : {&S->B, &S->solve_coef, &S->solve_blk}) {
+      b->stream = st;
+      b->ordered = true;
+    }
     S->kind = kind;
     S->tau0 = tau0;
     S->t = t;
@@ -272,36 +251,51 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     S->B.ensure((size_t)n * t * sizeof(float));
     CUDA_TRY(cudaMemcpyAsync(S->B.p, dB, (size_t)n * t * sizeof(float), cudaMemcpyDeviceToDevice, st));
     const int nblk = (int)ceil_div(n, kLzRows);
-    DevBuf red, scal, tmpb;
-    red.ensure((size_t)nblk * t * sizeof(double));
-    scal.ensure((size_t)4 * t * sizeof(double));   // [0]=dots [1]=nrm2 [2]=unorm2 [3]=beta(device)
+    // partials [t][nblk] of δ (dot), ‖·‖² after orthogonalisation (nrm) and ‖U_{j+1}‖² (un);
+    // nrm stays valid until the next step's lz_dot has taken β_{j+1} from it
+    DevBuf red(st), tmpb(st);
+    red.ensure((size_t)3 * nblk * t * sizeof(double));
     tmpb.ensure((size_t)n * t * sizeof(float));
-    double* d_dot = scal.as<double>();
-    double* d_nrm = d_dot + t;
-    double* d_un = d_nrm + t;
-    double* d_beta = d_un + t;
+    double* r_dot = red.as<double>();
+    double* r_nrm = r_dot + (size_t)nblk * t;
+    double* r_un = r_nrm + (size_t)nblk * t;
     float* tmp = tmpb.as<float>();
-    std::vector<double> h(3 * t);
+    double* d_out = g->scal.ensure((size_t)3 * t + 1);
+    const double* h = g->scal.h;
+    const bool v4 = (n % 4) == 0;
+    const dim3 gr(nblk, t);
+    const int* err = g->err.as<int>();
+    // Waits for the step's scalars in the mapped buffer and checks the kernels' error word.
+    auto fetch = [&](const double* dot) {
+      lz_final_kernel<<<(unsigned)ceil_div(t, 128), 128, 0, st>>>(dot, r_nrm, r_un, t, nblk, err, d_out);
+      LAUNCH_CHECK();
+      CUDA_TRY(cudaStreamSynchronize(st));
+      if (h[3 * t] != 0.0) {
+        CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), st));
+        SLEMM_THROW(SLEMM_ERR_CUDA, "a tensor-core kernel gave up a bounded wait (code " +
+                                        std::to_string((int)h[3 * t]) + ")");
+      }
+    };
 
     // B_norm, U_0 = B / β_0
-    col_dots(g, S->B.as<float>(), n, nullptr, 0, n, t, d_nrm);
-    dim3 gr(nblk, t);
-    lz_scale_kernel<<<gr, 256, 0, st>>>(S->block(0), S->B.as<float>(), d_nrm, n, red.as<double>(), nblk);
+    if (v4) lz_norm_kernel<4><<<gr, kLzThreads, 0, st>>>(S->B.as<float>(), n, r_nrm, nblk);
+    else lz_norm_kernel<1><<<gr, kLzThreads, 0, st>>>(S->B.as<float>(), n, r_nrm, nblk);
     LAUNCH_CHECK();
-    lz_reduce(red.as<double>(), nblk, t, d_un, st);
-    CUDA_TRY(cudaMemcpyAsync(h.data(), d_nrm, 2 * t * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    if (v4) lz_scale_kernel<4><<<gr, kLzThreads, 0, st>>>(S->block(0), S->B.as<float>(), r_nrm, n, r_un, nblk);
+    else lz_scale_kernel<1><<<gr, kLzThreads, 0, st>>>(S->block(0), S->B.as<float>(), r_nrm, n, r_un, nblk);
+    LAUNCH_CHECK();
+    fetch(nullptr);
     S->bnorm.resize(t);
     S->beta.assign(t, 0.0);
     S->unorm.assign(t, 0.0);
     for (int c = 0; c < t; ++c) {
-      S->bnorm[c] = std::sqrt(h[c]);
+      S->bnorm[c] = std::sqrt(h[t + c]);
       S->beta[c] = S->bnorm[c];
-      S->unorm[c] = std::sqrt(h[t + c]);
+      S->unorm[c] = std::sqrt(h[2 * t + c]);
       if (!(S->bnorm[c] > 0.0) || !std::isfinite(S->bnorm[c]))
         SLEMM_THROW(SLEMM_ERR_NUMERIC, "right-hand side column " + std::to_string(c) + " has zero or non-finite norm");
     }
-    std::vector<double> rho(t), gamma(t, 1.0), omega(t, 0.0), gamma_prev(t), omega_prev(t);
+    std::vector<double> rho(t), gamma(t, 1.0), omega(t, 0.0);
     for (int c = 0; c < t; ++c) rho[c] = S->bnorm[c];
     int j = 0;
     bool cnvg = false;
@@ -310,22 +304,24 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     while (j < maxit - 1) {
       float* Uj = S->block(j);
       float* Uprev = j > 0 ? S->block(j - 1) : nullptr;
-      op_device_mixed(g, kind, tau0, Uj, n, t, tmp, n, nq_eff);
-      if (j > 0)
-        CUDA_TRY(cudaMemcpyAsync(d_beta, S->beta.data() + (size_t)j * t, t * sizeof(double),
-                                 cudaMemcpyHostToDevice, st));
-      lz_dot_kernel<<<gr, 256, 0, st>>>(tmp, Uj, Uprev, j > 0 ? d_beta : nullptr, n, red.as<double>(), nblk);
-      LAUNCH_CHECK();
-      lz_reduce(red.as<double>(), nblk, t, d_dot, st);
-      lz_orth_kernel<<<gr, 256, 0, st>>>(tmp, Uj, d_dot, n, red.as<double>(), nblk);
-      LAUNCH_CHECK();
-      lz_reduce(red.as<double>(), nblk, t, d_nrm, st);
       float* Un = S->block(j + 1);
-      lz_scale_kernel<<<gr, 256, 0, st>>>(Un, tmp, d_nrm, n, red.as<double>(), nblk);
-      LAUNCH_CHECK();
-      lz_reduce(red.as<double>(), nblk, t, d_un, st);
-      CUDA_TRY(cudaMemcpyAsync(h.data(), d_dot, 3 * t * sizeof(double), cudaMemcpyDeviceToHost, st));
-      check_device_error(g);   // synchronises
+      op_device_mixed(g, kind, tau0, Uj, n, t, tmp, n, nq_eff);
+      if (v4) {
+        lz_dot_kernel<4><<<gr, kLzThreads, 0, st>>>(tmp, Uj, Uprev, r_nrm, n, r_dot, nblk);
+        LAUNCH_CHECK();
+        lz_orth_kernel<4><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
+        LAUNCH_CHECK();
+        lz_scale_kernel<4><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
+        LAUNCH_CHECK();
+      } else {
+        lz_dot_kernel<1><<<gr, kLzThreads, 0, st>>>(tmp, Uj, Uprev, r_nrm, n, r_dot, nblk);
+        LAUNCH_CHECK();
+        lz_orth_kernel<1><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
+        LAUNCH_CHECK();
+        lz_scale_kernel<1><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
+        LAUNCH_CHECK();
+      }
+      fetch(r_dot);
       double res = 0.0;
       for (int c = 0; c < t; ++c) {
         const double dl = h[c], bt = std::sqrt(h[t + c]), un = std::sqrt(h[2 * t + c]);
@@ -412,22 +408,29 @@ int solve_coeffs(const slemm_lseed* S, double sigma, double tol, int grp, std::v
   return steps;
 }
 
-// mom[i·npairs + p] = Σ_r B[r, a_p]·V_i[r, b_p] for i = 0 … J (V_0 = B, V_i = U_i); FP64 sums of
-// the stored FP32 vectors, one pass over the basis.
-__global__ void lz_moments_kernel(const float* __restrict__ B, const float* const* __restrict__ blocks,
-                                  const int2* __restrict__ pairs, int npairs, int64_t n,
-                                  double* __restrict__ red, int nblk)
+// mom[i·npairs + p] = Σ_r B[r, a_p]·V_i[r, b_p] for i = 0 … J (V_0 = B, V_i = U_i); double-float
+// sums of the stored FP32 vectors, one pass over the basis.
+__global__ void __launch_bounds__(kLzThreads)
+lz_moments_kernel(const float* __restrict__ B, const float* const* __restrict__ blocks,
+                  const int2* __restrict__ pairs, int npairs, int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
   const int p = blockIdx.y, i = blockIdx.z;
   const int2 ab = pairs[p];
   const float* Vi = (i == 0) ? B : blocks[i];
   const int64_t r0 = (int64_t)blockIdx.x * kLzRows, r1 = min64(n, r0 + kLzRows);
-  double acc = 0.0;
-  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-    acc += (double)B[(int64_t)ab.x * n + r] * (double)Vi[(int64_t)ab.y * n + r];
-  const double s = lz_block_sum(acc, sh);
+  DF acc;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += kLzThreads)
+    df_fma(acc, B[(int64_t)ab.x * n + r], Vi[(int64_t)ab.y * n + r]);
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[((int64_t)i * npairs + p) * nblk + blockIdx.x] = s;
+}
+
+// out[q] = Σ_b red[q][b] in block order, q < nq
+__global__ void lz_sum_kernel(const double* __restrict__ red, int nblk, int nq, double* __restrict__ out)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) out[q] = sum_partials(red + (int64_t)q * nblk, nblk);
 }
 
 void lanczos_moments(slemm_lseed* S, const std::vector<std::pair<int, int>>& pairs, int J, std::vector<double>& mom)
@@ -440,21 +443,21 @@ void lanczos_moments(slemm_lseed* S, const std::vector<std::pair<int, int>>& pai
   for (int i = 1; i <= J; ++i) hb[i] = S->block(i);
   std::vector<int2> hp(npairs);
   for (int q = 0; q < npairs; ++q) hp[q] = make_int2(pairs[q].first, pairs[q].second);
-  DevBuf dblk, dpairs, dred, dout;
+  DevBuf dblk(st), dpairs(st), dred(st);
   dblk.ensure(hb.size() * sizeof(float*));
   dpairs.ensure(hp.size() * sizeof(int2));
   const int nq = (J + 1) * npairs;
   dred.ensure((size_t)nq * nblk * sizeof(double));
-  dout.ensure((size_t)nq * sizeof(double));
+  double* out = S->g->scal.ensure((size_t)nq);
   CUDA_TRY(cudaMemcpyAsync(dblk.p, hb.data(), hb.size() * sizeof(float*), cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(dpairs.p, hp.data(), hp.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-  lz_moments_kernel<<<dim3(nblk, npairs, J + 1), 256, 0, st>>>(S->B.as<float>(), dblk.as<const float*>(),
-                                                               dpairs.as<int2>(), npairs, S->n, dred.as<double>(), nblk);
+  lz_moments_kernel<<<dim3(nblk, npairs, J + 1), kLzThreads, 0, st>>>(
+      S->B.as<float>(), dblk.as<const float*>(), dpairs.as<int2>(), npairs, S->n, dred.as<double>(), nblk);
   LAUNCH_CHECK();
-  lz_reduce(dred.as<double>(), nblk, nq, dout.as<double>(), st);
-  mom.resize(nq);
-  CUDA_TRY(cudaMemcpyAsync(mom.data(), dout.p, nq * sizeof(double), cudaMemcpyDeviceToHost, st));
+  lz_sum_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(dred.as<double>(), nblk, nq, out);
+  LAUNCH_CHECK();
   CUDA_TRY(cudaStreamSynchronize(st));
+  mom.assign(S->g->scal.h, S->g->scal.h + nq);
 }
 
 // X = (A + σI)^{-1}B for the columns of group `grp` (all columns when the seed has one group),
@@ -481,42 +484,78 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
   return steps;
 }
 
-// Batched tridiagonal eigensolve on the GPU (host in/out, FP64).
+// Eigenvalues and squared first eigenvector components of one symmetric tridiagonal matrix
+// (diagonal d[0 … nld−1], off-diagonal e[0 … nld−2]): implicit QL with Wilkinson shifts, FP64,
+// tracking only the first row z of the eigenvector matrix (all the quadrature needs).  These are
+// a few hundred flops per probe, so they run on the host.  Returns false if a sweep limit is hit.
+static bool tridiag_ql(double* d, double* e, double* z, int nld)
+{
+  for (int i = 0; i < nld; ++i) z[i] = (i == 0) ? 1.0 : 0.0;
+  if (nld > 0) e[nld - 1] = 0.0;
+  const double eps = 2.220446049250313e-16;
+  for (int l = 0; l < nld; ++l) {
+    for (int iter = 0;; ++iter) {
+      int mm = l;
+      for (; mm < nld - 1; ++mm) {
+        const double dd = std::fabs(d[mm]) + std::fabs(d[mm + 1]);
+        if (std::fabs(e[mm]) <= eps * dd) break;
+      }
+      if (mm == l) break;
+      if (iter >= 64) return false;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[mm] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
+      double s = 1.0, c = 1.0, pp = 0.0;
+      bool deflated = false;
+      for (int i = mm - 1; i >= l; --i) {
+        const double f = s * e[i], b = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= pp;
+          e[mm] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - pp;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        pp = s * r;
+        d[i + 1] = g + pp;
+        g = c * r - b;
+        const double zf = z[i + 1];
+        z[i + 1] = s * z[i] + c * zf;
+        z[i] = c * z[i] - s * zf;
+      }
+      if (deflated) continue;
+      d[l] -= pp;
+      e[l] = g;
+      e[mm] = 0.0;
+    }
+  }
+  return true;
+}
+
+// Batched tridiagonal eigensolve (host in/out, FP64).  delta is nld×t (row i = step i), beta
+// (nld+1)×t; D and W2 are nld×t with eigenvalues ascending per probe.
 void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2)
 {
   if (t <= 0 || nld <= 0) return;
-  std::vector<double> hd((size_t)t * nld), he((size_t)t * nld, 0.0);
-  for (int i = 0; i < nld; ++i)
-    for (int p = 0; p < t; ++p) {
-      hd[(size_t)i * t + p] = delta[(size_t)i * t + p];
-      if (i + 1 < nld) he[(size_t)i * t + p] = beta[(size_t)(i + 1) * t + p];
-    }
-  DevBuf dd, de, dz, df;
-  dd.ensure(hd.size() * sizeof(double));
-  de.ensure(he.size() * sizeof(double));
-  dz.ensure(hd.size() * sizeof(double));
-  df.ensure(sizeof(int));
-  CUDA_TRY(cudaMemcpy(dd.p, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(de.p, he.data(), he.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemset(df.p, 0, sizeof(int)));
-  tridiag_ql_kernel<<<(unsigned)ceil_div(t, 32), 32>>>(dd.as<double>(), de.as<double>(), dz.as<double>(), t, nld,
-                                                       df.as<int>());
-  LAUNCH_CHECK();
-  std::vector<double> hz(hd.size());
-  int fail = 0;
-  CUDA_TRY(cudaMemcpy(hd.data(), dd.p, hd.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(hz.data(), dz.p, hz.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(&fail, df.p, sizeof(int), cudaMemcpyDeviceToHost));
-  if (fail) SLEMM_THROW(SLEMM_ERR_NUMERIC, "tridiagonal QL did not converge in 64 sweeps");
-  // sort eigenvalues ascending per probe (column-major t×nld output)
+  std::vector<double> d(nld), e(nld), z(nld);
   std::vector<int> idx(nld);
   for (int p = 0; p < t; ++p) {
-    for (int i = 0; i < nld; ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return hd[(size_t)a * t + p] < hd[(size_t)b * t + p]; });
     for (int i = 0; i < nld; ++i) {
-      D[(size_t)i * t + p] = hd[(size_t)idx[i] * t + p];
-      const double zz = hz[(size_t)idx[i] * t + p];
-      W2[(size_t)i * t + p] = zz * zz;
+      d[i] = delta[(size_t)i * t + p];
+      e[i] = (i + 1 < nld) ? beta[(size_t)(i + 1) * t + p] : 0.0;
+    }
+    if (!tridiag_ql(d.data(), e.data(), z.data(), nld))
+      SLEMM_THROW(SLEMM_ERR_NUMERIC, "tridiagonal QL did not converge in 64 sweeps");
+    for (int i = 0; i < nld; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return d[a] < d[b]; });
+    for (int i = 0; i < nld; ++i) {
+      D[(size_t)i * t + p] = d[idx[i]];
+      W2[(size_t)i * t + p] = z[idx[i]] * z[idx[i]];
     }
   }
 }

@@ -12,6 +12,7 @@
 // All reductions are two-stage (per-block FP64 partials, then a fixed-order sum), so results
 // are bit-reproducible run to run.
 #include "internal.h"
+#include "reduce.cuh"
 
 #include <cuda_bf16.h>
 
@@ -20,112 +21,144 @@ namespace slemm {
 constexpr int kRedThreads = 256;
 constexpr int kRowsPerBlock = 4096;   // rows handled by one block of the row-wise kernels
 
-__device__ __forceinline__ double block_sum(double v, double* sh)
+// 4-wide accesses need rows % 4 == 0 (a vector never straddles the end), ld % 4 == 0 and a
+// 16-byte aligned base.
+static bool vec4_ok(int64_t rows, int64_t ld, const void* p)
 {
-  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
-  }
-  return r;   // valid in thread 0
+  return rows % 4 == 0 && ld % 4 == 0 && ((uintptr_t)p & 15u) == 0;
 }
 
-// red[q][nblk] → out[q] (fixed order)
+// out[q] = Σ_b red[q][b] in block order
 __global__ void reduce_partials_kernel(const double* __restrict__ red, int nblk, int nq,
                                        double* __restrict__ out)
 {
-  const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (q >= nq) return;
-  double s = 0.0;
-  for (int b = lane; b < nblk; b += 32) s += red[(int64_t)q * nblk + b];
-  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) out[q] = s;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) out[q] = sum_partials(red + (int64_t)q * nblk, nblk);
 }
 
 static void reduce_partials(const double* red, int nblk, int nq, double* out, cudaStream_t st)
 {
-  const int per_block = 8;
-  reduce_partials_kernel<<<(unsigned)ceil_div(nq, per_block), 32 * per_block, 0, st>>>(red, nblk, nq, out);
+  reduce_partials_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(red, nblk, nq, out);
   LAUNCH_CHECK();
 }
 
 // ---- projections ---------------------------------------------------------------------------------
 // red[(l*k + c)][blk] = Σ_{i in block} Q[i,l]·X[i,c]
-__global__ void proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, int cq,
-                                    const float* __restrict__ X, int64_t ldx, int64_t n, int k,
-                                    double* __restrict__ red, int nblk)
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __restrict__ X, int64_t ldx,
+                    int64_t n, int k, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
   const int c = blockIdx.y % k, l = blockIdx.y / k;
-  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int64_t i1 = min64(n, i0 + kRowsPerBlock);
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
-    acc += (double)Q[(int64_t)l * ldq + i] * (double)X[(int64_t)c * ldx + i];
-  const double s = block_sum(acc, sh);
+  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n, i0 + kRowsPerBlock);
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
+    float q[V], x[V];
+    ldv<V>(Q + (int64_t)l * ldq + i, q);
+    ldv<V>(X + (int64_t)c * ldx + i, x);
+#pragma unroll
+    for (int u = 0; u < V; ++u) df_fma(acc, q[u], x[u]);
+  }
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.x] = s;
-  (void)cq;
 }
 
-// X[i,c] += −Σ_l Q[i,l]·QtX[l,c] (+ tau0·V[i,c] when V != nullptr)
-__global__ void proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq,
-                                  float* __restrict__ X, int64_t ldx, int64_t n, int k,
-                                  const double* __restrict__ QtX, const float* __restrict__ V,
-                                  int64_t ldv, float tau0)
+// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ 64
+__device__ __forceinline__ void load_qt(const double* __restrict__ parts, int nblk, int cq, int k, int c, double* qt)
 {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int)threadIdx.x < cq) qt[threadIdx.x] = sum_partials(parts + (int64_t)(threadIdx.x * k + c) * nblk, nblk);
+  __syncthreads();
+}
+
+// X[i,c] −= Σ_l Q[i,l]·QtX[l,c] (+ tau0·Vin[i,c] when Vin != nullptr)
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq, float* __restrict__ X, int64_t ldx,
+                  int64_t n, int k, const double* __restrict__ qparts, int nblkq,
+                  const float* __restrict__ Vin, int64_t ld_v, float tau0)
+{
+  __shared__ double qt[64];
   const int c = blockIdx.y;
+  load_qt(qparts, nblkq, cq, k, c, qt);
+  const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
   if (i >= n) return;
-  double acc = 0.0;
-  for (int l = 0; l < cq; ++l) acc += (double)Q[(int64_t)l * ldq + i] * QtX[l * k + c];
-  float x = X[(int64_t)c * ldx + i];
-  x = x - (float)acc;
-  if (V) x += tau0 * V[(int64_t)c * ldv + i];
-  X[(int64_t)c * ldx + i] = x;
+  float x[V];
+  ldv<V>(X + (int64_t)c * ldx + i, x);
+#pragma unroll
+  for (int u = 0; u < V; ++u) {
+    double a = 0.0;
+    for (int l = 0; l < cq; ++l) a += (double)Q[(int64_t)l * ldq + i + u] * qt[l];
+    x[u] = x[u] - (float)a;
+    if (Vin) x[u] = __fmaf_rn(tau0, Vin[(int64_t)c * ld_v + i + u], x[u]);
+  }
+  stv<V>(X + (int64_t)c * ldx + i, x);
+}
+
+template <int V>
+static void launch_proj_partial(slemm_geno* g, const float* X, int64_t ldx, int k, double* red, int nblk)
+{
+  proj_partial_kernel<V><<<dim3(nblk, g->c * k), kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, X, ldx,
+                                                                               g->n, k, red, nblk);
+  LAUNCH_CHECK();
+}
+
+static void proj_partials(slemm_geno* g, const float* X, int64_t ldx, int k, double* red, int nblk)
+{
+  if (vec4_ok(g->n, ldx, X)) launch_proj_partial<4>(g, X, ldx, k, red, nblk);
+  else launch_proj_partial<1>(g, X, ldx, k, red, nblk);
+}
+
+static void proj_apply_parts(slemm_geno* g, float* X, int64_t ldx, int k, const double* qparts, int nblkq,
+                             const float* Vin, int64_t ld_v, float tau0)
+{
+  const bool v4 = vec4_ok(g->n, ldx, X) && (!Vin || vec4_ok(g->n, ld_v, Vin));
+  if (v4) {
+    dim3 grid((unsigned)ceil_div(g->n, 4 * kRedThreads), k);
+    proj_apply_kernel<4><<<grid, kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, g->c, X, ldx, g->n, k,
+                                                              qparts, nblkq, Vin, ld_v, tau0);
+  } else {
+    dim3 grid((unsigned)ceil_div(g->n, kRedThreads), k);
+    proj_apply_kernel<1><<<grid, kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, g->c, X, ldx, g->n, k,
+                                                              qparts, nblkq, Vin, ld_v, tau0);
+  }
+  LAUNCH_CHECK();
 }
 
 void proj_coeffs(slemm_geno* g, const float* X, int64_t ldx, int k, double* d_QtX)
 {
   if (g->c == 0) return;
+  CHECK_ARG(g->c <= 64, "more than 64 covariates");
   const int nblk = (int)ceil_div(g->n, kRowsPerBlock);
   double* red = (double*)g->ws_red.ensure((size_t)nblk * g->c * k * sizeof(double));
-  dim3 grid(nblk, g->c * k);
-  proj_partial_kernel<<<grid, kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, g->c, X, ldx,
-                                                           g->n, k, red, nblk);
-  LAUNCH_CHECK();
+  proj_partials(g, X, ldx, k, red, nblk);
   reduce_partials(red, nblk, g->c * k, d_QtX, g->stream);
 }
 
 void proj_apply(slemm_geno* g, float* X, int64_t ldx, int k, const double* d_QtX)
 {
   if (g->c == 0) return;
-  dim3 grid((unsigned)ceil_div(g->n, 256), k);
-  proj_apply_kernel<<<grid, 256, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, g->c, X, ldx, g->n, k,
-                                                 d_QtX, nullptr, 0, 0.f);
-  LAUNCH_CHECK();
+  proj_apply_parts(g, X, ldx, k, d_QtX, 1, nullptr, 0, 0.f);
 }
 
 // ---- column dots ------------------------------------------------------------------------------------
-__global__ void col_dots_partial_kernel(const float* __restrict__ a, int64_t lda,
-                                        const float* __restrict__ b, int64_t ldb, int64_t n,
-                                        double* __restrict__ red, int nblk)
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+col_dots_partial_kernel(const float* __restrict__ a, int64_t lda, const float* __restrict__ b, int64_t ldb,
+                        int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
   const int c = blockIdx.y;
-  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int64_t i1 = min64(n, i0 + kRowsPerBlock);
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const double x = a[(int64_t)c * lda + i];
-    const double y = b ? (double)b[(int64_t)c * ldb + i] : x;
-    acc += x * y;
+  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n, i0 + kRowsPerBlock);
+  DF acc;
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
+    float x[V], y[V];
+    ldv<V>(a + (int64_t)c * lda + i, x);
+    if (b) ldv<V>(b + (int64_t)c * ldb + i, y);
+#pragma unroll
+    for (int u = 0; u < V; ++u) df_fma(acc, x[u], b ? y[u] : x[u]);
   }
-  const double s = block_sum(acc, sh);
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
@@ -135,145 +168,231 @@ void col_dots(slemm_geno* g, const float* a, int64_t lda, const float* b, int64_
   const int nblk = (int)ceil_div(n, kRowsPerBlock);
   double* red = (double*)g->ws_red.ensure((size_t)nblk * k * sizeof(double));
   dim3 grid(nblk, k);
-  col_dots_partial_kernel<<<grid, kRedThreads, 0, g->stream>>>(a, lda, b, ldb, n, red, nblk);
+  if (vec4_ok(n, lda, a) && (!b || vec4_ok(n, ldb, b)))
+    col_dots_partial_kernel<4><<<grid, kRedThreads, 0, g->stream>>>(a, lda, b, ldb, n, red, nblk);
+  else
+    col_dots_partial_kernel<1><<<grid, kRedThreads, 0, g->stream>>>(a, lda, b, ldb, n, red, nblk);
   LAUNCH_CHECK();
   reduce_partials(red, nblk, k, d_out, g->stream);
 }
 
 // ---- dense-operand builders ------------------------------------------------------------------------
-// Writes x into the dense operand: FP32 row c (npieces == 0) or BF16 pieces p·k + c, and returns
-// the exact value the products will see.
-__device__ __forceinline__ double store_operand(float x, int npieces, void* Bv, int64_t K_pad,
-                                                int k, int c, int64_t kidx)
+// Writes x[0 … V−1] (rows kidx …) into the dense operand — FP32 row c (npieces == 0) or BF16
+// pieces p·k + c — and adds exactly what the products will see to acc (weighted by wt when
+// kWeighted).
+template <int V, bool kWeighted>
+__device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, void* Bv, int64_t K_pad, int k,
+                                              int c, int64_t kidx, DF& acc, const float (&wt)[V])
 {
   if (npieces == 0) {
-    static_cast<float*>(Bv)[(int64_t)c * K_pad + kidx] = x;
-    return (double)x;
+    stv<V>(static_cast<float*>(Bv) + (int64_t)c * K_pad + kidx, x);
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      if (kWeighted) df_fma(acc, wt[u], x[u]);
+      else df_add(acc, x[u]);
+    }
+    return;
   }
   __nv_bfloat16* B = static_cast<__nv_bfloat16*>(Bv);
-  double sum = 0.0;
-  float r = x;
+  float r[V];
+#pragma unroll
+  for (int u = 0; u < V; ++u) r[u] = x[u];
   for (int p = 0; p < npieces; ++p) {
-    const __nv_bfloat16 h = __float2bfloat16_rn(r);
-    const float hf = __bfloat162float(h);
-    B[(int64_t)(p * k + c) * K_pad + kidx] = h;
-    sum += (double)hf;
-    r = r - hf;   // exact in FP32
+    __nv_bfloat16 h[V];
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      h[u] = __float2bfloat16_rn(r[u]);
+      const float hf = __bfloat162float(h[u]);
+      r[u] = __fsub_rn(r[u], hf);   // exact in FP32
+      if (kWeighted) df_fma(acc, wt[u], hf);
+      else df_add(acc, hf);
+    }
+    __nv_bfloat16* dst = B + (int64_t)(p * k + c) * K_pad + kidx;
+    if constexpr (V == 4) {
+      __nv_bfloat162 lo2, hi2;
+      lo2.x = h[0], lo2.y = h[1], hi2.x = h[2], hi2.y = h[3];
+      uint2 pk;
+      pk.x = *reinterpret_cast<uint32_t*>(&lo2);
+      pk.y = *reinterpret_cast<uint32_t*>(&hi2);
+      *reinterpret_cast<uint2*>(dst) = pk;
+    } else {
+      dst[0] = h[0];
+    }
   }
-  return sum;
+}
+
+// Zeroes BF16 padding row `row` (rows pieces·k … N−1 of the operand) over K-range [k0, k1).
+__device__ __forceinline__ void zero_pad_row(void* Bv, int64_t K_pad, int row, int64_t k0, int64_t k1)
+{
+  uint2* dst = reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(Bv) + (int64_t)row * K_pad);
+  for (int64_t q = k0 / 4 + threadIdx.x; q < k1 / 4; q += blockDim.x) dst[q] = make_uint2(0u, 0u);
 }
 
 // Direction-1 operand (K = individuals): x = in[i,c]; for the first nq columns
-// x −= Σ_l Q[i,l]·QtV[l,c]; optionally x *= rr[i]; rows i ≥ n are 0.
-// red[c][blk] = Σ_i stored(x).
-__global__ void prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n,
-                                      int64_t n_pad, int k, const float* __restrict__ Q,
-                                      int64_t ldq, int cq, const double* __restrict__ QtV, int nq,
-                                      const float* __restrict__ rr, int npieces, void* B,
-                                      double* __restrict__ red, int nblk)
+// x −= Σ_l Q[i,l]·QtV[l,c] (QtV from its partials); optionally x *= rr[i]; rows i ≥ n are 0.
+// red[c][blk] = Σ_i stored(x).  Blocks with c ≥ k zero BF16 padding row npieces·k + (c − k).
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64_t n_pad, int k,
+                      const float* __restrict__ Q, int64_t ldq, int cq, const double* __restrict__ qparts,
+                      int nblkq, int nq, const float* __restrict__ rr, int npieces, void* B,
+                      double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
+  __shared__ double qt[64];
   const int c = blockIdx.y;
-  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int64_t i1 = min64(n_pad, i0 + kRowsPerBlock);
-  double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    float x = 0.f;
-    if (i < n) {
-      x = in[(int64_t)c * ld + i];
-      if (QtV && c < nq) {
-        double p = 0.0;
-        for (int l = 0; l < cq; ++l) p += (double)Q[(int64_t)l * ldq + i] * QtV[l * nq + c];
-        x = x - (float)p;
-      }
-      if (rr) x *= rr[i];
-    }
-    acc += store_operand(x, npieces, B, n_pad, k, c, i);
+  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n_pad, i0 + kRowsPerBlock);
+  if (c >= k) {
+    zero_pad_row(B, n_pad, npieces * k + (c - k), i0, i1);
+    return;
   }
-  const double s = block_sum(acc, sh);
+  const bool proj = qparts != nullptr && c < nq;
+  if (proj) load_qt(qparts, nblkq, cq, nq, c, qt);
+  DF acc;
+  const float one[V] = {};
+  for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
+    float x[V] = {};
+    if (i < n) {
+      ldv<V>(in + (int64_t)c * ld + i, x);
+      if (proj) {
+#pragma unroll
+        for (int u = 0; u < V; ++u) {
+          double p = 0.0;
+          for (int l = 0; l < cq; ++l) p += (double)Q[(int64_t)l * ldq + i + u] * qt[l];
+          x[u] = x[u] - (float)p;
+        }
+      }
+      if (rr) {
+        float r[V];
+        ldv<V>(rr + i, r);
+#pragma unroll
+        for (int u = 0; u < V; ++u) x[u] = __fmul_rn(x[u], r[u]);
+      }
+    }
+    store_operand<V, false>(x, npieces, B, n_pad, k, c, i, acc, one);
+  }
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// Sum over split-K partials and BF16 pieces of column c, row r.
-__device__ __forceinline__ float gather_D(const float* __restrict__ D, int splits, int N,
-                                          int64_t M_pad, int pieces, int k, int c, int64_t r)
+// Sum over split-K partials and BF16 pieces of column c, rows r … r+V−1.
+template <int V>
+__device__ __forceinline__ void gather_D(const float* __restrict__ D, int splits, int N, int64_t M_pad,
+                                         int pieces, int k, int c, int64_t r, float (&acc)[V])
 {
-  float acc = 0.f;
+#pragma unroll
+  for (int u = 0; u < V; ++u) acc[u] = 0.f;
   for (int s = 0; s < splits; ++s)
-    for (int p = 0; p < pieces; ++p) acc += D[((int64_t)s * N + p * k + c) * M_pad + r];
-  return acc;
+    for (int p = 0; p < pieces; ++p) {
+      float t[V];
+      ldv<V>(D + ((int64_t)s * N + p * k + c) * M_pad + r, t);
+#pragma unroll
+      for (int u = 0; u < V; ++u) acc[u] = __fadd_rn(acc[u], t[u]);
+    }
 }
 
-// Direction-1 finalize (rows = SNPs): val = raw − gm_j·colsum_c, times w_j when use_w.
-// mode 0: out[j,c] = val (j < m).  mode 1: val becomes the direction-2 operand (K = SNPs) and
-// red[c][blk] = Σ_j gm_j·stored(val).
-__global__ void finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pad,
-                                    int pieces, int k, int64_t m, const float* __restrict__ gm,
-                                    const float* __restrict__ w, const double* __restrict__ colsum,
-                                    int mode, float* __restrict__ out, int64_t ldo, int npieces2,
-                                    void* B2, double* __restrict__ red, int nblk)
+// Direction-1 finalize (rows = SNPs): val = raw − gm_j·colsum_c (colsum from the prologue's
+// partials), times w_j when w != nullptr.  mode 0: out[j,c] = val (j < m).  mode 1: val becomes
+// the direction-2 operand (K = SNPs) and red[c][blk] = Σ_j gm_j·stored(val); blocks with c ≥ k
+// zero BF16 padding row npieces2·k + (c − k).
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pad, int pieces, int k,
+                    int64_t m, const float* __restrict__ gm, const float* __restrict__ w,
+                    const double* __restrict__ cparts, int nblkc, int mode, float* __restrict__ out,
+                    int64_t ldo, int npieces2, void* B2, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
+  __shared__ float sb[2];
   const int c = blockIdx.y;
-  const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int64_t j1 = min64(m_pad, j0 + kRowsPerBlock);
-  const double cs = colsum[c];
-  double acc = 0.0;
-  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    float val = 0.f;
+  const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
+  if (c >= k) {
+    zero_pad_row(B2, m_pad, npieces2 * k + (c - k), j0, j1);
+    return;
+  }
+  float ch, cl;
+  block_scalar([&] { return sum_partials(cparts + (int64_t)c * nblkc, nblkc); }, sb, ch, cl);
+  DF acc;
+  for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
+    float val[V] = {}, g[V];
+    ldv<V>(gm + j, g);   // gm is zero-padded to m_pad
     if (j < m) {
-      const float raw = gather_D(D, splits, N, m_pad, pieces, k, c, j);
-      val = (float)((double)raw - (double)gm[j] * cs);
-      if (w) val *= w[j];
+      gather_D<V>(D, splits, N, m_pad, pieces, k, c, j, val);
+      float ws[V];
+      if (w) ldv<V>(w + j, ws);
+#pragma unroll
+      for (int u = 0; u < V; ++u) {
+        float v = __fmaf_rn(-g[u], cl, __fmaf_rn(-g[u], ch, val[u]));
+        if (w) v = __fmul_rn(v, ws[u]);
+        val[u] = v;
+      }
     }
     if (mode == 0) {
-      if (j < m) out[(int64_t)c * ldo + j] = val;
+      if (j < m) stv<V>(out + (int64_t)c * ldo + j, val);
     } else {
-      const double st = store_operand(val, npieces2, B2, m_pad, k, c, j);
-      acc += (double)gm[j] * st;
+      store_operand<V, true>(val, npieces2, B2, m_pad, k, c, j, acc, g);
     }
   }
   if (mode == 1) {
-    const double s = block_sum(acc, sh);
+    const double s = block_sum_d(df_value(acc), sh);
     if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
   }
 }
 
-// Direction-2 operand straight from an m×k input (matvec): stored(in) and red = Σ gm·stored.
-__global__ void prologue_snp_kernel(const float* __restrict__ in, int64_t ld, int64_t m,
-                                    int64_t m_pad, int k, const float* __restrict__ gm,
-                                    int npieces, void* B, double* __restrict__ red, int nblk)
+// Direction-2 operand straight from an m×k input (matvec): stored(in) and red = Σ gm·stored;
+// blocks with c ≥ k zero BF16 padding rows.
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+prologue_snp_kernel(const float* __restrict__ in, int64_t ld, int64_t m, int64_t m_pad, int k,
+                    const float* __restrict__ gm, int npieces, void* B, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
   const int c = blockIdx.y;
-  const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int64_t j1 = min64(m_pad, j0 + kRowsPerBlock);
-  double acc = 0.0;
-  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    const float x = (j < m) ? in[(int64_t)c * ld + j] : 0.f;
-    const double st = store_operand(x, npieces, B, m_pad, k, c, j);
-    acc += (double)gm[j] * st;
+  const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
+  if (c >= k) {
+    zero_pad_row(B, m_pad, npieces * k + (c - k), j0, j1);
+    return;
   }
-  const double s = block_sum(acc, sh);
+  DF acc;
+  for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
+    float x[V] = {}, g[V];
+    if (j < m) ldv<V>(in + (int64_t)c * ld + j, x);
+    ldv<V>(gm + j, g);
+    store_operand<V, true>(x, npieces, B, m_pad, k, c, j, acc, g);
+  }
+  const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// Direction-2 finalize (rows = individuals) of columns c0 + blockIdx.y: val = raw − t_c, times
-// rr_i when rr != nullptr, plus tau0·v when V != nullptr.  out[i,c] = val for i < n.
-__global__ void finalize_indiv_kernel(const float* __restrict__ D, int splits, int N,
-                                      int64_t n_pad, int pieces, int k, int64_t n,
-                                      const double* __restrict__ tsum, const float* __restrict__ rr,
-                                      const float* __restrict__ V, int64_t ldv, float tau0,
-                                      float* __restrict__ out, int64_t ldo, int c0)
+// Direction-2 finalize (rows = individuals): val = raw − t_c (t from the direction-1 partials),
+// times rr_i when rr != nullptr, plus tau0·Vin for columns c ≥ nq when Vin != nullptr.
+template <int V>
+__global__ void __launch_bounds__(kRedThreads)
+finalize_indiv_kernel(const float* __restrict__ D, int splits, int N, int64_t n_pad, int pieces, int k,
+                      int64_t n, const double* __restrict__ tparts, int nblkt, const float* __restrict__ rr,
+                      const float* __restrict__ Vin, int64_t ld_v, float tau0, int nq, float* __restrict__ out,
+                      int64_t ldo)
 {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = c0 + blockIdx.y;
+  __shared__ float sb[2];
+  const int c = blockIdx.y;
+  float th, tl;
+  block_scalar([&] { return sum_partials(tparts + (int64_t)c * nblkt, nblkt); }, sb, th, tl);
+  const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
   if (i >= n) return;
-  const float raw = gather_D(D, splits, N, n_pad, pieces, k, c, i);
-  float val = (float)((double)raw - tsum[c]);
-  if (rr) val *= rr[i];
-  if (V) val += tau0 * V[(int64_t)c * ldv + i];
-  out[(int64_t)c * ldo + i] = val;
+  float val[V];
+  gather_D<V>(D, splits, N, n_pad, pieces, k, c, i, val);
+  float r[V], v[V];
+  if (rr) ldv<V>(rr + i, r);
+  const bool addv = Vin != nullptr && c >= nq;
+  if (addv) ldv<V>(Vin + (int64_t)c * ld_v + i, v);
+#pragma unroll
+  for (int u = 0; u < V; ++u) {
+    float x = __fsub_rn(__fsub_rn(val[u], th), tl);
+    if (rr) x = __fmul_rn(x, r[u]);
+    if (addv) x = __fmaf_rn(tau0, v[u], x);
+    val[u] = x;
+  }
+  stv<V>(out + (int64_t)c * ldo + i, val);
 }
 
 // ---- one packed pass ---------------------------------------------------------------------------------
@@ -356,42 +475,25 @@ static void run_gemm(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t
   }
 }
 
-// Device scratch: small FP64 vectors + error word.
-struct Small {
-  double* colsum;   // k
-  double* tsum;     // k
-  double* QtV;      // 64·k
-  double* QtT;      // 64·k
-  int* err;         // the handle's error word
-};
-
-static Small small_ws(slemm_geno* g, int k)
-{
-  const size_t nd = (size_t)k * 2 + (size_t)64 * k * 2;
-  uint8_t* base = (uint8_t*)g->ws_small.ensure(nd * sizeof(double));
-  Small s;
-  s.colsum = (double*)base;
-  s.tsum = s.colsum + k;
-  s.QtV = s.tsum + k;
-  s.QtT = s.QtV + (size_t)64 * k;
-  s.err = g->err.as<int>();
-  return s;
-}
-
 // One operator application on a column group (k ≤ max_group).  For the H0 operators (kind
 // LDET, or QUADFORM) the first nq columns get the projections of H0_quadform_mv and the others
 // are plain H0_ldet_mv columns, so one block can carry both kinds of seed systems.
+//
+// Launches: [QᵀV partials] → prologue (operand 1 + its column sums) → packed pass 1 → finalize 1
+// (operand 2 + its centring sums) → packed pass 2 → finalize 2 → [QᵀT partials → projection].
+// Each kernel sums the partials it needs itself, in a fixed order.
 static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                      float* out, int64_t ld_out, int nq)
 {
   if (kind == SLEMM_OP_QUADFORM) kind = SLEMM_OP_LDET;   // nq carries the projected columns
   cudaStream_t st = g->stream;
-  Small sm = small_ws(g, k);
   const bool dir1 = kind != SLEMM_OP_MATVEC;                          // needs Zᵀ pass
   const bool dir2 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET || kind == SLEMM_OP_MATVEC;
   const PassPlan p1 = plan_pass(g, k, g->m_pad, g->n_pad);             // M = SNPs, K = indiv
   const PassPlan p2 = plan_pass(g, k, g->n_pad, g->m_pad);             // M = indiv, K = SNPs
   const int np1 = p1.tc ? p1.pieces : 0, np2 = p2.tc ? p2.pieces : 0;
+  const int pad1 = p1.tc ? p1.N - p1.pieces * k : 0;                   // BF16 padding rows
+  const int pad2 = p2.tc ? p2.N - p2.pieces * k : 0;
   const size_t b1 = dir1 ? (p1.tc ? (size_t)p1.N * g->n_pad * 2 : (size_t)k * g->n_pad * 4) : 0;
   const size_t b2 = dir2 ? (p2.tc ? (size_t)p2.N * g->m_pad * 2 : (size_t)k * g->m_pad * 4) : 0;
   uint8_t* Bbuf = (uint8_t*)g->ws_B.ensure(b1 + b2);
@@ -402,85 +504,93 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   float* D = (float*)g->ws_D.ensure(std::max(d1, d2) * sizeof(float));
   const int nblk_n = (int)ceil_div(g->n_pad, kRowsPerBlock);
   const int nblk_m = (int)ceil_div(g->m_pad, kRowsPerBlock);
-  double* red = (double*)g->ws_red.ensure((size_t)std::max(nblk_n, nblk_m) * k * sizeof(double) +
-                                          (size_t)ceil_div(g->n, kRowsPerBlock) * 64 * k * sizeof(double));
-  // zero the BF16 padding rows (pieces·k … N) of both operands
-  if (p1.tc && dir1 && p1.N > p1.pieces * k)
-    CUDA_TRY(cudaMemsetAsync((uint16_t*)B1 + (size_t)p1.pieces * k * g->n_pad, 0,
-                             (size_t)(p1.N - p1.pieces * k) * g->n_pad * 2, st));
-  if (p2.tc && dir2 && p2.N > p2.pieces * k)
-    CUDA_TRY(cudaMemsetAsync((uint16_t*)B2 + (size_t)p2.pieces * k * g->m_pad, 0,
-                             (size_t)(p2.N - p2.pieces * k) * g->m_pad * 2, st));
+  const int nblk_q = (int)ceil_div(g->n, kRowsPerBlock);
+  // partials: colsum [k][nblk_n] | tsum [k][nblk_m] | QᵀV [c·nq][nblk_q] | QᵀT [c·nq][nblk_q]
+  const int cq = g->c;
+  CHECK_ARG(cq <= 64, "more than 64 covariates");
+  const size_t nred = (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q;
+  double* r_col = (double*)g->ws_red.ensure(nred * sizeof(double));
+  double* r_t = r_col + (size_t)k * nblk_n;
+  double* r_qv = r_t + (size_t)k * nblk_m;
+  double* r_qt = r_qv + (size_t)std::max(cq, 1) * k * nblk_q;
+  int* err = g->err.as<int>();
 
   // H0 operators: the first nq columns are projected (H0_quadform_mv), the rest are not (H0_ldet_mv)
   const bool h0 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET;
+  const bool vin = vec4_ok(g->n, ld_in, in);
 
   if (dir1) {
     // ---- prologue 1: v_adj = rr∘(v − QQᵀv) (quadform), rr∘v (ldet), v (rmatvec) ----
-    const double* QtV = nullptr;
-    if (h0 && nq > 0 && g->c > 0) {
-      proj_coeffs(g, in, ld_in, nq, sm.QtV);
-      QtV = sm.QtV;
-    }
-    dim3 grid(nblk_n, k);
-    prologue_indiv_kernel<<<grid, kRedThreads, 0, st>>>(
-        in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad, g->c, QtV, nq,
-        h0 ? g->rr.as<float>() : nullptr, np1, B1, red, nblk_n);
+    const bool proj = h0 && nq > 0 && cq > 0;
+    if (proj) proj_partials(g, in, ld_in, nq, r_qv, nblk_q);
+    dim3 grid(nblk_n, k + pad1);
+    const float* rr = h0 ? g->rr.as<float>() : nullptr;
+    if (vin)
+      prologue_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad,
+                                                             cq, proj ? r_qv : nullptr, nblk_q, nq, rr, np1, B1,
+                                                             r_col, nblk_n);
+    else
+      prologue_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad,
+                                                             cq, proj ? r_qv : nullptr, nblk_q, nq, rr, np1, B1,
+                                                             r_col, nblk_n);
     LAUNCH_CHECK();
-    reduce_partials(red, nblk_n, k, sm.colsum, st);
     // ---- pass 1: Cntᵀ over individuals ----
-    run_gemm(g, p1, g->G.as<uint8_t>(), g->m_pad, g->n_pad, B1, D, sm.err, k, 1);
+    run_gemm(g, p1, g->G.as<uint8_t>(), g->m_pad, g->n_pad, B1, D, err, k, 1);
     // ---- finalize 1 ----
-    dim3 gridm(nblk_m, k);
     const float* wsc = (kind == SLEMM_OP_RMATVEC) ? nullptr : g->w.as<float>();
     if (h0) {
-      finalize_snp_kernel<<<gridm, kRedThreads, 0, st>>>(
-          D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, sm.colsum, 1,
-          nullptr, 0, np2, B2, red, nblk_m);
+      finalize_snp_kernel<4><<<dim3(nblk_m, k + pad2), kRedThreads, 0, st>>>(
+          D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 1, nullptr, 0,
+          np2, B2, r_t, nblk_m);
       LAUNCH_CHECK();
-      reduce_partials(red, nblk_m, k, sm.tsum, st);
     } else {
-      finalize_snp_kernel<<<gridm, kRedThreads, 0, st>>>(
-          D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, sm.colsum, 0,
-          out, ld_out, 0, nullptr, nullptr, 0);
+      if (vec4_ok(g->m, ld_out, out))
+        finalize_snp_kernel<4><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
+            D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
+            0, nullptr, nullptr, 0);
+      else
+        finalize_snp_kernel<1><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
+            D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
+            0, nullptr, nullptr, 0);
       LAUNCH_CHECK();
       return;
     }
   } else {
     // matvec: operand straight from the m×k input
-    dim3 gridm(nblk_m, k);
-    prologue_snp_kernel<<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k,
-                                                       g->gm.as<float>(), np2, B2, red, nblk_m);
+    dim3 gridm(nblk_m, k + pad2);
+    if (vec4_ok(g->m, ld_in, in))
+      prologue_snp_kernel<4><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, g->gm.as<float>(), np2, B2,
+                                                            r_t, nblk_m);
+    else
+      prologue_snp_kernel<1><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, g->gm.as<float>(), np2, B2,
+                                                            r_t, nblk_m);
     LAUNCH_CHECK();
-    reduce_partials(red, nblk_m, k, sm.tsum, st);
   }
   // ---- pass 2: Cnt over SNPs ----
-  run_gemm(g, p2, g->GT.as<uint8_t>(), g->n_pad, g->m_pad, B2, D, sm.err, k, 2);
+  run_gemm(g, p2, g->GT.as<uint8_t>(), g->n_pad, g->m_pad, B2, D, err, k, 2);
   // ---- finalize 2 ----
-  const unsigned gx = (unsigned)ceil_div(g->n, 256);
-  if (kind == SLEMM_OP_MATVEC) {
-    finalize_indiv_kernel<<<dim3(gx, k), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n,
-                                                       sm.tsum, nullptr, nullptr, 0, 0.f, out, ld_out, 0);
-    LAUNCH_CHECK();
-    return;
+  // matvec: out = raw − t.  H0: out = rr∘(raw − t) (+ τ0·v for the ldet columns nq … k−1)
+  const float* rr2 = (kind == SLEMM_OP_MATVEC) ? nullptr : g->rr.as<float>();
+  const float* v2 = (kind == SLEMM_OP_MATVEC) ? nullptr : in;
+  const int nq2 = (kind == SLEMM_OP_MATVEC) ? 0 : nq;
+  if (vec4_ok(g->n, ld_out, out) && (!v2 || vin)) {
+    dim3 grid((unsigned)ceil_div(g->n, 4 * kRedThreads), k);
+    finalize_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n, r_t,
+                                                           nblk_m, rr2, v2, ld_in, tau0, nq2, out, ld_out);
+  } else {
+    dim3 grid((unsigned)ceil_div(g->n, kRedThreads), k);
+    finalize_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n, r_t,
+                                                           nblk_m, rr2, v2, ld_in, tau0, nq2, out, ld_out);
   }
-  // ldet columns nq … k−1: out = rr∘(Z_c W Z_cᵀ rr∘v) + τ0 v
-  if (nq < k) {
-    finalize_indiv_kernel<<<dim3(gx, k - nq), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k,
-                                                            g->n, sm.tsum, g->rr.as<float>(), in, ld_in,
-                                                            tau0, out, ld_out, nq);
-    LAUNCH_CHECK();
-  }
-  // quadform columns 0 … nq−1: T = rr∘(Z_c W Z_cᵀ v_adj); out = T + τ0 v − QQᵀT
-  if (nq > 0) {
-    finalize_indiv_kernel<<<dim3(gx, nq), 256, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k,
-                                                        g->n, sm.tsum, g->rr.as<float>(), nullptr, 0, 0.f,
-                                                        out, ld_out, 0);
-    LAUNCH_CHECK();
-    if (g->c > 0) proj_coeffs(g, out, ld_out, nq, sm.QtT);
-    proj_apply_kernel<<<dim3(gx, nq), 256, 0, st>>>(g->Q.as<float>(), g->n_pad, g->c, out, ld_out, g->n,
-                                                    nq, sm.QtT, in, ld_in, tau0);
-    LAUNCH_CHECK();
+  LAUNCH_CHECK();
+  // quadform columns 0 … nq−1: out = T + τ0 v − QQᵀT
+  if (kind != SLEMM_OP_MATVEC && nq > 0) {
+    if (cq > 0) {
+      proj_partials(g, out, ld_out, nq, r_qt, nblk_q);
+      proj_apply_parts(g, out, ld_out, nq, r_qt, nblk_q, in, ld_in, tau0);
+    } else {
+      proj_apply_parts(g, out, ld_out, nq, nullptr, 1, in, ld_in, tau0);
+    }
   }
 }
 

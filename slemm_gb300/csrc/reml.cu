@@ -319,7 +319,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   std::vector<float> QV((size_t)n * (1 + c));
   std::copy(yproj.begin(), yproj.end(), QV.begin());
   for (size_t i = 0; i < (size_t)n * c; ++i) QV[(size_t)n + i] = (float)S.qr.Q[i];
-  DevBuf d_y, d_QV, d_X, d_tmp;
+  DevBuf d_y(g->stream), d_QV(g->stream), d_X(g->stream), d_tmp(g->stream);
   d_y.ensure((size_t)n * sizeof(float));
   d_QV.ensure((size_t)n * tQV * sizeof(float));
   d_X.ensure((size_t)n * tQV * sizeof(float));
@@ -436,7 +436,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   proj_apply(g, d_Py, n, 1, d_scal);
   scale_rows(g, d_Py, n, n, 1, g->rr.as<float>());
   // snp_blup = W Z_cᵀ Py  (src/reml.cpp:662)
-  DevBuf d_b;
+  DevBuf d_b(g->stream);
   d_b.ensure((size_t)m * sizeof(float));
   op_device(g, SLEMM_OP_WRMATVEC, 0.f, d_Py, n, 1, d_b.as<float>(), m);
   CUDA_TRY(cudaMemcpyAsync(Py_out, d_Py, n * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -546,7 +546,8 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
       for (int64_t i = 0; i < n; ++i) V[(size_t)j * n + i] = rnorm(rng);
   }
   for (int64_t i = 0; i < n; ++i) V[i] = y[i];
-  DevBuf d_V, d_u, d_PV, d_Py, d_ub, d_tmp, d_aux;
+  DevBuf d_V(g->stream), d_u(g->stream), d_PV(g->stream), d_Py(g->stream), d_ub(g->stream),
+      d_tmp(g->stream), d_aux(g->stream);
   d_V.ensure((size_t)n * tV * sizeof(float));
   d_u.ensure((size_t)m * n_MC * sizeof(float));
   d_PV.ensure((size_t)n * tV * sizeof(float));

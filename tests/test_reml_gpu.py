@@ -145,9 +145,14 @@ def test_score_terms_vs_reference_script(gpu):
     assert np.max(np.abs(np.log10(p[ok]) - np.log10(rp[ok]))) <= 1e-3
 
 
-@pytest.mark.parametrize("seed,n,n_V", [(0, 37, 3), (1, 1000, 5), (42, 2049, 2), (7, 100003, 1)])
+@pytest.mark.parametrize("seed,n,n_V", [(0, 37, 3), (1, 1000, 5), (42, 2049, 2), (7, 100003, 1),
+                                        (5, 1, 1000), (9, 200, 3000), (11, 79872, 4), (3, 100000, 64)])
 def test_gpu_probes_match_reference_draws(gpu, seed, n, n_V):
-    """The GPU MT19937 probe block equals the libstdc++ draws of src/reml.cpp:597-605 bit for bit."""
+    """The GPU MT19937 probe block equals the libstdc++ draws of src/reml.cpp:597-605 bit for bit.
+
+    The cases cover one chunk (no jump), several doubling levels, a column shorter than one
+    generator phase (n < 227), chunk boundaries that fall on column boundaries, and the
+    64-probe block of the n = 100,000 benchmark (21 chunks)."""
     import ctypes
     V = np.zeros((n, n_V), np.float32, order="F")
     _lib.check(gpu.slemm_gpu_rademacher(seed, n, n_V, V.ctypes.data_as(ctypes.c_void_p), n, 0))
