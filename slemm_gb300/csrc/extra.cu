@@ -163,7 +163,7 @@ int slemm_gpu_gebv(slemm_geno* g, const double* alpha, const uint8_t* flip, doub
     const int64_t M_tiles = g->n_pad / kTileM, K_tiles = g->m_pad / kTileK;
     const int splits = choose_splits(M_tiles, K_tiles, 8, num_sms());
     const int tps = (int)ceil_div(K_tiles, splits);
-    DevBuf d_a, d_part, d_out;
+    DevBuf d_a(st), d_part(st), d_out(st);
     d_a.ensure(a.size() * sizeof(double));
     d_part.ensure((size_t)splits * g->n_pad * sizeof(double));
     d_out.ensure((size_t)g->n * sizeof(double));
@@ -224,7 +224,7 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
     const int64_t M_tiles = g->m_pad / kTileM, K_tiles = n_pad / kTileK;
     const int splits = choose_splits(M_tiles, K_tiles, 8, num_sms());
     const int tps = (int)ceil_div(K_tiles, splits);
-    DevBuf dB, dpart, dsrq, dxy, dxx, dpc;
+    DevBuf dB(st), dpart(st), dsrq(st), dxy(st), dxx(st), dpc(st);
     dB.ensure(B.size() * sizeof(float));
     dpart.ensure((size_t)splits * (C + 1) * g->m_pad * sizeof(double));
     dsrq.ensure(sum_rq.size() * sizeof(double));
@@ -252,7 +252,7 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
         const int Cp = C <= 8 ? 8 : 16;
         std::vector<float> Bp((size_t)Cp * n_pad, 0.f);
         std::copy(B.begin(), B.end(), Bp.begin());
-        DevBuf dBp, dpp;
+        DevBuf dBp(st), dpp(st);
         dBp.ensure(Bp.size() * sizeof(float));
         dpp.ensure((size_t)splits * (Cp + 1) * g->m_pad * sizeof(double));
         CUDA_TRY(cudaMemcpyAsync(dBp.p, Bp.data(), Bp.size() * sizeof(float), cudaMemcpyHostToDevice, st));

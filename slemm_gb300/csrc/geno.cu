@@ -131,6 +131,109 @@ __global__ void pack_GT_kernel(const uint8_t* __restrict__ raw, int64_t row_byte
   GT[((mt * K_tiles_T + kt) * 128 + r) * 4 + wr] = word;
 }
 
+// ---- tiled pack (no individual subset) -----------------------------------------------------------
+// One CTA turns a block of 128 SNP rows × 128 raw bytes (512 individuals) into the 8 G tiles and
+// 8 GT tiles that cover it: the raw bytes are read row-contiguously (from device memory, or from
+// the caller's host buffer over NVLink-C2C where the device can address pageable memory), the
+// codes become 2-bit counts with four bit operations per 16 calls, and both copies are written
+// tile-contiguously through shared memory.
+constexpr int kPackThreads = 256;
+
+// 16 PLINK codes (code e at bits 2e) → 16 counts in the same positions: count = bit0 + bit1
+// (00 → 0, 10 → 1, 11 → 2, missing 01 → 1).
+__device__ __forceinline__ uint32_t counts_of_codes(uint32_t w)
+{
+  const uint32_t lo = w & 0x55555555u, hi = (w >> 1) & 0x55555555u;
+  return (lo ^ hi) | ((lo & hi) << 1);
+}
+
+// Natural order (field e at bits 2e) → tile word order (even e = 2q at bits 2q, odd e = 2q+1 at
+// bits 16+2q): an inverse perfect shuffle of 2-bit units in three exchange steps.
+__device__ __forceinline__ uint32_t unshuffle2(uint32_t x)
+{
+  uint32_t t = (x ^ (x >> 2)) & 0x0C0C0C0Cu;
+  x ^= t ^ (t << 2);
+  t = (x ^ (x >> 4)) & 0x00F000F0u;
+  x ^= t ^ (t << 4);
+  t = (x ^ (x >> 8)) & 0x0000FF00u;
+  x ^= t ^ (t << 8);
+  return x;
+}
+
+// raw row j (global SNP index) is at raw + (j − j0)·row_stride; rows j0 … j0 + rows − 1 are present.
+// blockIdx.x: SNP group (G M-tile, GT K-tiles 2·sg, 2·sg+1); blockIdx.y: 512-individual group.
+__global__ void __launch_bounds__(kPackThreads)
+pack_tiles_kernel(const uint8_t* __restrict__ raw, int64_t row_stride, int64_t row_bytes, int64_t j0,
+                  int64_t rows, int64_t m, int64_t n, int64_t Kt_G, int64_t Mt_T, int64_t Kt_T, bool aligned4,
+                  uint32_t* __restrict__ G, uint32_t* __restrict__ GT)
+{
+  __shared__ uint32_t cnt[128][33];    // [SNP row][16-individual word], natural order
+  __shared__ uint32_t outT[512][9];    // [individual][GT word 0 … 7 (2 K-tiles × 4)]
+  const int tid = threadIdx.x;
+  const int64_t sg = (int64_t)blockIdx.x + j0 / 128;
+  const int64_t ig = blockIdx.y;
+  for (int idx = tid; idx < 128 * 32; idx += kPackThreads) {
+    const int r = idx >> 5, q = idx & 31;
+    const int64_t j = sg * 128 + r;
+    const int64_t b0 = ig * 128 + 4 * q;
+    uint32_t w = 0;
+    if (j < m && j - j0 < rows && b0 < row_bytes) {
+      const uint8_t* p = raw + (j - j0) * row_stride + b0;
+      if (aligned4 && b0 + 4 <= row_bytes) {
+        w = *reinterpret_cast<const uint32_t*>(p);
+      } else {
+        for (int k = 0; k < 4 && b0 + k < row_bytes; ++k) w |= (uint32_t)p[k] << (8 * k);
+      }
+    }
+    const int64_t i0 = 4 * b0;   // first individual of the word
+    const uint32_t valid = (i0 + 16 <= n) ? 0xFFFFFFFFu : (i0 >= n ? 0u : ((1u << (2 * (n - i0))) - 1u));
+    cnt[r][q] = counts_of_codes(w) & valid;
+  }
+  __syncthreads();
+  // G: tile (sg, 8·ig + t), row r = SNP, words 0 … 3 = local words 4t … 4t+3 of that row
+  for (int idx = tid; idx < 8 * 128; idx += kPackThreads) {
+    const int t = idx >> 7, r = idx & 127;
+    const int64_t kt = ig * 8 + t;
+    if (kt >= Kt_G) continue;
+    uint4 o;
+    o.x = unshuffle2(cnt[r][4 * t]);
+    o.y = unshuffle2(cnt[r][4 * t + 1]);
+    o.z = unshuffle2(cnt[r][4 * t + 2]);
+    o.w = unshuffle2(cnt[r][4 * t + 3]);
+    *reinterpret_cast<uint4*>(G + ((sg * Kt_G + kt) * 128 + r) * 4) = o;
+  }
+  // GT: individuals in quads (one count byte of a word), SNP rows 16·hw … 16·hw + 15
+  for (int idx = tid; idx < 128 * 8; idx += kPackThreads) {
+    const int iq = idx & 127, hw = idx >> 7;   // quad, GT word (K-tile hw/4, word hw%4)
+    uint32_t o0 = 0, o1 = 0, o2 = 0, o3 = 0;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const uint32_t b = (cnt[16 * hw + e][iq >> 2] >> (8 * (iq & 3))) & 0xFFu;
+      o0 |= (b & 3u) << (2 * e);
+      o1 |= ((b >> 2) & 3u) << (2 * e);
+      o2 |= ((b >> 4) & 3u) << (2 * e);
+      o3 |= ((b >> 6) & 3u) << (2 * e);
+    }
+    outT[4 * iq][hw] = unshuffle2(o0);
+    outT[4 * iq + 1][hw] = unshuffle2(o1);
+    outT[4 * iq + 2][hw] = unshuffle2(o2);
+    outT[4 * iq + 3][hw] = unshuffle2(o3);
+  }
+  __syncthreads();
+  // GT tiles (4·ig + i/128, 2·sg + h), row i % 128, words 4h … 4h+3
+  for (int idx = tid; idx < 512 * 2; idx += kPackThreads) {
+    const int i = idx & 511, h = idx >> 9;
+    const int64_t mt = ig * 4 + (i >> 7), kt = sg * 2 + h;
+    if (mt >= Mt_T || kt >= Kt_T) continue;
+    uint4 o;
+    o.x = outT[i][4 * h];
+    o.y = outT[i][4 * h + 1];
+    o.z = outT[i][4 * h + 2];
+    o.w = outT[i][4 * h + 3];
+    *reinterpret_cast<uint4*>(GT + ((mt * Kt_T + kt) * 128 + (i & 127)) * 4) = o;
+  }
+}
+
 // Per-row integer counts over the G copy: n1 = fields 01, n2 = fields 10, allele count n1 + 2·n2.
 __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int64_t K_tiles,
                                   int64_t* __restrict__ pc, int32_t* __restrict__ c1,
@@ -213,6 +316,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       configure_pool(g->device);
       CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
       g->own_stream = true;
+      g->bind_stream();
       g->n = n;
       g->m = m;
       // rows padded to 256 so every tensor-core CTA (two 128-row tiles) is full
@@ -225,47 +329,72 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       g->GT.ensure(bytes_GT);
       g->err.ensure(sizeof(int));
       CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));
-      CUDA_TRY(cudaMemsetAsync(g->G.p, 0, bytes_G, g->stream));
-      CUDA_TRY(cudaMemsetAsync(g->GT.p, 0, bytes_GT, g->stream));
-
-      DevBuf d_keep;
-      if (keep_idx) {
-        d_keep.ensure(n * sizeof(int64_t));
-        CUDA_TRY(cudaMemcpyAsync(d_keep.p, keep_idx, n * sizeof(int64_t), cudaMemcpyHostToDevice,
-                                 g->stream));
-      }
-      // stream SNP chunks of 4096 rows (multiple of 128) through a device staging buffer
-      const int64_t chunk = 4096;
-      DevBuf d_raw;
-      d_raw.ensure((size_t)chunk * row_bytes);
-      for (int64_t j0 = 0; j0 < m; j0 += chunk) {
-        const int64_t rows = std::min(chunk, m - j0);
-        if (row_stride == row_bytes) {
-          CUDA_TRY(cudaMemcpyAsync(d_raw.p, bed_rows + j0 * row_stride, rows * row_bytes,
-                                   cudaMemcpyHostToDevice, g->stream));
+      const int64_t Mt_T = g->n_pad / kTileM;
+      if (!keep_idx) {
+        // tiled pack of both copies, padding included; the raw rows are read in place when the
+        // device can address pageable host memory, else through a device staging buffer
+        int pageable = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, g->device));
+        const unsigned gy = (unsigned)ceil_div(g->n_pad, 512);
+        if (pageable) {
+          const bool al = ((uintptr_t)bed_rows % 4 == 0) && (row_stride % 4 == 0);
+          pack_tiles_kernel<<<dim3((unsigned)(g->m_pad / 128), gy), kPackThreads, 0, g->stream>>>(
+              bed_rows, row_stride, row_bytes, 0, m, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
+              g->GT.as<uint32_t>());
+          LAUNCH_CHECK();
         } else {
-          CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride,
-                                     row_bytes, rows, cudaMemcpyHostToDevice, g->stream));
+          const int64_t chunk = 4096;
+          DevBuf d_raw;
+          d_raw.ensure((size_t)chunk * row_bytes);
+          const bool al = (row_bytes % 4 == 0);
+          for (int64_t j0 = 0; j0 < g->m_pad; j0 += chunk) {
+            const int64_t rows = std::max<int64_t>(0, std::min(chunk, m - j0));
+            if (rows > 0)
+              CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes,
+                                         rows, cudaMemcpyHostToDevice, g->stream));
+            const unsigned gx = (unsigned)(std::min(chunk, g->m_pad - j0) / 128);
+            pack_tiles_kernel<<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
+                d_raw.as<uint8_t>(), row_bytes, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al,
+                g->G.as<uint32_t>(), g->GT.as<uint32_t>());
+            LAUNCH_CHECK();
+          }
+          CUDA_TRY(cudaStreamSynchronize(g->stream));   // d_raw is released on return
         }
-        {
-          const int64_t total = rows * (Kt_G * 4);
-          const int th = 256;
-          pack_G_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
-              d_raw.as<uint8_t>(), row_bytes, j0, rows, d_keep.as<int64_t>(), n, Kt_G,
-              g->G.as<uint32_t>());
-          LAUNCH_CHECK();
+      } else {
+        CUDA_TRY(cudaMemsetAsync(g->G.p, 0, bytes_G, g->stream));
+        CUDA_TRY(cudaMemsetAsync(g->GT.p, 0, bytes_GT, g->stream));
+        DevBuf d_keep;
+        d_keep.ensure(n * sizeof(int64_t));
+        CUDA_TRY(cudaMemcpyAsync(d_keep.p, keep_idx, n * sizeof(int64_t), cudaMemcpyHostToDevice, g->stream));
+        // stream SNP chunks of 4096 rows (multiple of 128) through a device staging buffer
+        const int64_t chunk = 4096;
+        DevBuf d_raw;
+        d_raw.ensure((size_t)chunk * row_bytes);
+        for (int64_t j0 = 0; j0 < m; j0 += chunk) {
+          const int64_t rows = std::min(chunk, m - j0);
+          CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
+                                     cudaMemcpyHostToDevice, g->stream));
+          {
+            const int64_t total = rows * (Kt_G * 4);
+            const int th = 256;
+            pack_G_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
+                d_raw.as<uint8_t>(), row_bytes, j0, rows, d_keep.as<int64_t>(), n, Kt_G, g->G.as<uint32_t>());
+            LAUNCH_CHECK();
+          }
+          {
+            const int64_t total = ceil_div(rows, 16) * g->n_pad;
+            const int th = 256;
+            pack_GT_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
+                d_raw.as<uint8_t>(), row_bytes, j0, rows, m, d_keep.as<int64_t>(), n, g->n_pad, Kt_GT,
+                g->GT.as<uint32_t>());
+            LAUNCH_CHECK();
+          }
         }
-        {
-          const int64_t total = ceil_div(rows, 16) * g->n_pad;
-          const int th = 256;
-          pack_GT_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
-              d_raw.as<uint8_t>(), row_bytes, j0, rows, m, d_keep.as<int64_t>(), n, g->n_pad,
-              Kt_GT, g->GT.as<uint32_t>());
-          LAUNCH_CHECK();
-        }
+        CUDA_TRY(cudaStreamSynchronize(g->stream));   // staging buffers are released on return
       }
       CUDA_TRY(cudaStreamSynchronize(g->stream));
     } catch (...) {
+      g->for_each_buf([](DevBuf& b) { b.release(); });
       if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
       delete g;
       throw;
@@ -278,6 +407,7 @@ int slemm_gpu_genotype_destroy(slemm_geno* g)
 {
   return guarded([&] {
     if (!g) return;
+    g->for_each_buf([](DevBuf& b) { b.release(); });   // stream-ordered frees before the stream goes
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
@@ -306,6 +436,7 @@ int slemm_gpu_set_stream(slemm_geno* g, void* stream)
       CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
       g->own_stream = true;
     }
+    g->bind_stream();   // the old stream was synchronised: later frees may run on the new one
   });
 }
 
@@ -322,7 +453,7 @@ int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
-    DevBuf d_pc, d_c1, d_c2;
+    DevBuf d_pc(g->stream), d_c1(g->stream), d_c2(g->stream);
     d_pc.ensure(g->m * sizeof(int64_t));
     d_c1.ensure(g->m * sizeof(int32_t));
     d_c2.ensure(g->m * sizeof(int32_t));

@@ -37,6 +37,21 @@ struct slemm_geno {
     double ms;
   };
   std::vector<GemmStat> prof_stats;
+  // Every device buffer of the handle: all are stream-ordered on `stream` (the pool keeps freed
+  // blocks cached, so building and dropping handles costs no device-wide synchronisation).
+  template <class F>
+  void for_each_buf(F&& f)
+  {
+    for (slemm::DevBuf* b : {&G, &GT, &gm, &w, &rr, &Q, &ws_B, &ws_D, &ws_red, &ws_small, &ws_T, &ws_in, &ws_out, &err})
+      f(*b);
+  }
+  void bind_stream()
+  {
+    for_each_buf([&](slemm::DevBuf& b) {
+      b.stream = stream;
+      b.ordered = true;
+    });
+  }
 };
 
 namespace slemm {

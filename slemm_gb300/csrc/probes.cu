@@ -180,7 +180,9 @@ __device__ __forceinline__ uint32_t mt_temper(uint32_t y)
 
 // Runs the recurrence from the window held in x (positions 0 … 623, indices taken & kMask):
 // at phase t thread tid < 227 produces word 624 + 227·t + tid, stores it and passes it to
-// emit(t, word).  Every thread of the CTA must call this (it contains barriers).
+// emit(t, word).  Two phases run between barriers: their cross-thread operands are at least two
+// phases old, so all four are loaded up front.  `phases` must be even.  Every thread of the CTA
+// must call this (it contains barriers).
 template <uint32_t kMask, class Emit>
 __device__ __forceinline__ void mt_pipeline(uint32_t* x, int64_t phases, Emit&& emit)
 {
@@ -188,17 +190,21 @@ __device__ __forceinline__ void mt_pipeline(uint32_t* x, int64_t phases, Emit&& 
   const bool act = tid < kMtLag;
   uint32_t prev = act ? x[(kMtM + tid) & kMask] : 0u;   // x_{j−227} for j = 624 + tid
   uint32_t j = (uint32_t)(kMtN + tid);                  // wraps harmlessly: only j & kMask is used
-  for (int64_t t = 0; t < phases; ++t) {
+  for (int64_t t = 0; t < phases; t += 2) {
     if (act) {
-      const uint32_t w = mt_step(prev, x[(j - kMtN) & kMask], x[(j - kMtN + 1) & kMask]);
-      x[j & kMask] = w;
-      prev = w;
-      emit(t, w);
+      const uint32_t a0 = x[(j - kMtN) & kMask], b0 = x[(j - kMtN + 1) & kMask];
+      const uint32_t a1 = x[(j + kMtLag - kMtN) & kMask], b1 = x[(j + kMtLag - kMtN + 1) & kMask];
+      const uint32_t w0 = mt_step(prev, a0, b0);
+      const uint32_t w1 = mt_step(w0, a1, b1);
+      x[j & kMask] = w0;
+      x[(j + kMtLag) & kMask] = w1;
+      prev = w1;
+      emit(t, w0);
+      emit(t + 1, w1);
     }
-    j += kMtLag;
-    if (t & 1) __syncthreads();   // cross-thread operands are ≥ 2 phases old
+    j += 2 * kMtLag;
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // Window 0: the seeded state of std::mt19937(seed).
@@ -246,20 +252,24 @@ mt_chunk_kernel(const uint32_t* __restrict__ states, int64_t L0, int64_t total, 
   const int64_t d0 = (int64_t)k * L0;
   const int64_t len = min64(L0, total - d0);
   const int tid = threadIdx.x;
-  int64_t c = 0, i = 0;
+  int64_t i = 0;
+  float* dst = V;
   if (tid < kMtLag) {
-    c = (d0 + tid) / n;
+    const int64_t c = (d0 + tid) / n;
     i = d0 + tid - c * n;
+    dst = V + c * ld + i;
   }
-  mt_pipeline<kMtRing - 1>(x, ceil_div(len, kMtLag), [&](int64_t t, uint32_t w) {
+  const int64_t phases = ceil_div(len, kMtLag);
+  mt_pipeline<kMtRing - 1>(x, phases + (phases & 1), [&](int64_t t, uint32_t w) {
     if (kMtLag * t + tid < len) {
       const bool neg = __uint2float_rn(mt_temper(w)) < 2147483648.0f;   // float(x)/2^32 < 0.5
-      V[c * ld + i] = neg ? -value : value;
+      *dst = neg ? -value : value;
     }
     i += kMtLag;
+    dst += kMtLag;
     while (i >= n) {
       i -= n;
-      ++c;
+      dst += ld - n;
     }
   });
 }
@@ -269,8 +279,8 @@ void rademacher_device(int seed, int64_t n, int n_V, float* dV, int64_t ld, cuda
 {
   const float value = 1.0f / std::sqrt((float)n);   // ±1 / ‖±1‖, both IEEE-rounded in FP32
   const int64_t total = n * (int64_t)n_V;
-  // chunk count ≈ √(total / 6000): the doubling levels cost ∝ P, the chunk pass ∝ total / P
-  const int64_t target = std::max<int64_t>(1, std::min<int64_t>(512, (int64_t)std::sqrt((double)total / 6000.0)));
+  // chunk count ≈ √(total / 1500): the doubling levels cost ∝ P, the chunk pass ∝ total / P
+  const int64_t target = std::max<int64_t>(1, std::min<int64_t>(512, (int64_t)std::sqrt((double)total / 1500.0)));
   int e = 0;
   while (((int64_t)kMtN << e) * target < total) ++e;
   const int64_t L0 = (int64_t)kMtN << e;
