@@ -90,6 +90,22 @@ int slemm_gpu_get_stream(const slemm_geno* g, void** stream);
 int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32_t* n1,
                               int32_t* n2);
 
+/* Marker QC (src/input.cpp:388-394; replaces cal_maf_from_genobits, src/weight.cpp:3-15, and
+ * cal_hwep_from_genobits, src/input.cpp:10-22): per SNP, maf = |[f>0.5] − f| with
+ * f = popcount/float(2n) (FP32), and hwep = float(SNPHWE2(n1, n0, n2, midp)) — the exact HWE test
+ * (src/snphwe.cpp:18).  Host pointers, length m each. */
+int slemm_gpu_marker_qc(slemm_geno* g, int hwe_midp, float* maf, float* hwep);
+
+/* The exact HWE test alone (SNPHWE2(obs_hets, obs_hom1, obs_hom2, midp), src/snphwe.cpp:18) for m
+ * count triples; host pointers; p in FP64. */
+int slemm_gpu_hwe_exact(const int32_t* het, const int32_t* hom1, const int32_t* hom2, int64_t m,
+                        int midp, double* p);
+
+/* Decoded allele-2 counts (missing = 1) of SNP rows `rows[0 … cnt−1]` for the kept individuals:
+ * out[c·ld + i], i < n (the kmat[j][2i] + kmat[j][2i+1] reads of src/option.cpp:471-472). */
+int slemm_gpu_genotype_rows(slemm_geno* g, const int64_t* rows, int cnt, float* out, int64_t ld,
+                            int mem);
+
 /* gm (m), w (m), rr (n) — host pointers.  gm is the per-SNP mean count, w the per-SNP
  * weight (gw in the reference, src/reml.cpp:622), rr = R^{-1/2} (NULL = all ones). */
 int slemm_gpu_set_weights(slemm_geno* g, const float* gm, const float* w, const float* rr);
@@ -168,6 +184,31 @@ int slemm_gpu_reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_
 int slemm_gpu_reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
                        const float* y, const float* persnp, const slemm_reml_opts* opts,
                        float* Py, float* snp_blup, float* blue, slemm_reml_result* res);
+
+/* Iterative window weighting (`--iter_weighting`, src/option.cpp:437-530): equal-weight GREML
+ * (DF-REML when lrt and n < 5000, else MC-REML with n_MC samples), per-SNP variance
+ * 2·maf(1−maf)·b² normalised to mean 1, fixed-effect SNPs by clumping (largest variance above
+ * sig_chisq, kept when independent at indep_r2), window weights over window_size+1 SNPs, then the
+ * window-weighted GREML (DF-REML when lrt, else MC-REML with n_MC_final samples) with the fixed
+ * SNPs appended to the covariates; their snp_blup entries are their BLUE.  maf is per SNP (the
+ * marker QC values).  Outputs (host): Py (n), snp_blup (m), blue (c + max_fixed; the first
+ * c + n_fixed used), var_blue ((c+n_fixed)², DF-REML only, may be NULL), persnp_out (m, the final
+ * weights, may be NULL), fixed_idx (max_fixed, may be NULL), n_fixed. */
+typedef struct {
+  int   window_size;  /* --window_size, even (20 unless given, src/option.cpp:303-307)     */
+  float sig_chisq;    /* --sig_chisq (1e6)                                                */
+  float indep_r2;     /* --indep_r2 (0.5)                                                 */
+  int   lrt;          /* --lrt                                                            */
+  int   n_MC;         /* MC samples of an MC-REML first stage (0: max(min(4e9/n², 30), 3))  */
+  int   n_MC_final;   /* MC samples of an MC-REML second stage (0: n_MC; --using_nr_opt: n_V) */
+  int   max_fixed;    /* capacity of blue / fixed_idx beyond the c covariates              */
+} slemm_window_opts;
+int slemm_gpu_reml_iter_weighting(slemm_geno* g, const float* rvec, const float* X, int64_t ldx,
+                                  int c, const float* y, const float* persnp, const float* maf,
+                                  const slemm_reml_opts* opts, const slemm_window_opts* wopts,
+                                  float* Py, float* snp_blup, float* blue, float* var_blue,
+                                  float* persnp_out, int64_t* fixed_idx, int* n_fixed,
+                                  slemm_reml_result* res);
 
 /* ---- prediction and GWAS score statistics ------------------------------------------------- */
 /* GEBV: tgv_i = Σ_j (flip_j ? 2−count_ij : count_ij)·alpha_j, FP64 accumulation of exact

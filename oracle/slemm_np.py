@@ -95,6 +95,64 @@ def maf(pc: np.ndarray, n: int) -> np.ndarray:
     return out
 
 
+def hwe_exact(het: int, hom1: int, hom2: int, midp: int = 0) -> float:
+    """src/snphwe.cpp:18 SNPHWE2 (called as SNPHWE2(n1, n0, n2, midp) at src/input.cpp:20): exact
+    Hardy–Weinberg test (Wigginton, Cutler & Abecasis 2005).  Under HWE the het count h (parity of
+    the rare-allele count) has P(h+2)/P(h) = 4·hom_r·hom_c / ((h+2)(h+1)); p = Σ P(h) over
+    P(h) ≤ P(obs) (relative tie tolerance 1e-7), normalised; mid-p subtracts P(obs)/2.  Terms are
+    taken relative to the mode and summed outward with math.fsum."""
+    import math
+    n = het + hom1 + hom2
+    if n == 0:
+        return 0.5 if midp else 1.0
+    rare = 2 * min(hom1, hom2) + het
+    hmax = min(rare, 2 * n - rare)
+    par = rare & 1
+
+    def up(h):
+        hr = (rare - h) // 2
+        hc = n - h - hr
+        return 4.0 * hr * hc / ((h + 2) * (h + 1))
+
+    h = int(rare * (2 * n - rare) / (2 * n - 1))
+    if (h & 1) != par:
+        h += 1 if h + 1 <= hmax else -1
+    h = max(par, min(h, hmax))
+    while h + 2 <= hmax and up(h) > 1.0:
+        h += 2
+    while h >= 2 and up(h - 2) < 1.0:
+        h -= 2
+    probs = {h: 1.0}
+    p, k = 1.0, h
+    while k + 2 <= hmax and p > 0.0:
+        p *= up(k)
+        k += 2
+        probs[k] = p
+    p, k = 1.0, h
+    while k >= 2 and p > 0.0:
+        p /= up(k - 2)
+        k -= 2
+        probs[k] = p
+    pobs = probs[het]
+    tot = math.fsum(probs.values())
+    tail = math.fsum(v for v in probs.values() if v <= pobs * (1.0 + 1e-7))
+    if midp:
+        tail -= 0.5 * pobs
+    return min(1.0, tail / tot)
+
+
+def marker_qc(counts: np.ndarray, midp: int = 0):
+    """src/input.cpp:388-394 — per-SNP MAF (src/weight.cpp:3-15, FP32) and HWE p-value stored as
+    FP32 (src/input.cpp:10-22: n2 = both bits, n1 = one bit incl. missing, n0 = neither)."""
+    counts = np.ascontiguousarray(counts, dtype=np.uint8)
+    m, n = counts.shape
+    pc = popcounts(counts)
+    n0, n1, n2 = hwe_counts(counts)
+    maf_v = maf(pc, n)
+    hwep = np.array([hwe_exact(int(a), int(b), int(c), midp) for a, b, c in zip(n1, n0, n2)], np.float32)
+    return maf_v, hwep
+
+
 def genotype_mean(pc: np.ndarray, n: int) -> np.ndarray:
     """src/reml.cpp:620 — gm = nz_bits/float(n)."""
     pc = np.ascontiguousarray(pc, dtype=np.int64)
@@ -576,6 +634,73 @@ def window_weights(maf_vals, snp_blup, window_size, sig_idx=()):
     for j in sig_idx:
         out[j] = 0
     return snpvar, out
+
+
+def clump_fixed_snps(counts, snpvar, sig_chisq, indep_r2):
+    """src/option.cpp:466-497 — repeatedly take the SNP with the largest snpvar (first maximum)
+    while it exceeds sig_chisq; its centred count vector joins the fixed effects when it is the
+    first, or when its residual after regression on the ones already taken keeps more than
+    indep_r2 of its squared norm.  Returns the indices taken and the n×s centred columns."""
+    f32 = np.float32
+    tmp = np.asarray(snpvar, f32).copy()
+    idx, cols = [], []
+    while True:
+        j = int(np.argmax(tmp))
+        if not tmp[j] > sig_chisq:
+            break
+        tmp[j] = 0
+        yv = np.asarray(counts[j], f32)
+        yv = yv - f32(yv.astype(np.float64).mean())
+        if not idx:
+            idx.append(j)
+            cols.append(yv)
+            continue
+        Xs = np.column_stack(cols).astype(np.float64)
+        y64 = yv.astype(np.float64)
+        coef = np.linalg.solve(Xs.T @ Xs, Xs.T @ y64)
+        res = y64 - Xs @ coef
+        if (res @ res) / (y64 @ y64) > indep_r2:
+            idx.append(j)
+            cols.append(yv)
+    Xs = np.column_stack(cols).astype(f32) if cols else np.zeros((counts.shape[1], 0), f32)
+    return idx, Xs
+
+
+def REML_iter_weighting(counts, rvec, X, y, persnp, maf_vals, lrt=True, seed=0, n_V=30, n_MC=None,
+                        n_MC_final=None, tol_L=5e-4, s2max=0.7, window_size=20, sig_chisq=1e6,
+                        indep_r2=0.5, dtype=np.float32):
+    """src/option.cpp:437-530 — equal-weight GREML (DF-REML when --lrt and n < 5000, else MC-REML),
+    per-SNP variance 2·maf(1−maf)·b² normalised to mean 1, fixed-effect SNPs by clumping, window
+    weights, then the window-weighted GREML with those SNPs as covariates; their SNP-BLUP entries
+    become their BLUE."""
+    f32 = np.float32
+    n = y.size
+    m = counts.shape[0]
+    n_MC = n_mc_rule(n) if n_MC is None else n_MC
+    n_MC_final = n_MC if n_MC_final is None else n_MC_final
+    ones = np.ones(m, f32)
+    if lrt and n < 5000:
+        r1 = SLDF_REML(counts, rvec, X, y, ones, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype)
+    else:
+        r1 = LMC_REML(counts, rvec, X, y, ones, seed=seed, n_MC=n_MC, tol_L=tol_L, s2max=s2max, dtype=dtype)
+    snpvar, _ = window_weights(maf_vals, r1["snp_blup"], window_size)
+    sig, Xs = clump_fixed_snps(counts, snpvar, sig_chisq, indep_r2)
+    _, w = window_weights(maf_vals, r1["snp_blup"], window_size, sig)
+    p2 = np.asarray(persnp, f32) * w
+    p2 = (p2 / f32(p2.astype(np.float64).mean())).astype(f32)
+    X2 = np.column_stack([np.asarray(X, f32).reshape(n, -1), Xs])
+    if lrt:
+        r2 = SLDF_REML(counts, rvec, X2, y, p2, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype)
+    else:
+        r2 = LMC_REML(counts, rvec, X2, y, p2, seed=seed, n_MC=n_MC_final, tol_L=tol_L, s2max=s2max,
+                      dtype=dtype)
+    c = np.asarray(X).reshape(n, -1).shape[1]
+    blup = np.asarray(r2["snp_blup"], f32).copy()
+    for i, j in enumerate(sig):
+        blup[j] = r2["blue"][c + i]
+    r2 = dict(r2)
+    r2.update(snp_blup=blup, fixed=sig, persnp=p2, stage1=r1)
+    return r2
 
 
 # ------------------------------------------------------------------------------------------

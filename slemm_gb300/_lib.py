@@ -35,6 +35,11 @@ class RemlResult(ctypes.Structure):
                 ("t_final", ctypes.c_double)]
 
 
+class WindowOpts(ctypes.Structure):
+    _fields_ = [("window_size", I32), ("sig_chisq", F32), ("indep_r2", F32), ("lrt", I32), ("n_MC", I32),
+                ("n_MC_final", I32), ("max_fixed", I32)]
+
+
 _SIGS = {
     "slemm_gpu_last_error": (ctypes.c_char_p, []),
     "slemm_gpu_version": (I32, []),
@@ -46,6 +51,9 @@ _SIGS = {
     "slemm_gpu_set_stream": (I32, [P, P]),
     "slemm_gpu_get_stream": (I32, [P, ctypes.POINTER(P)]),
     "slemm_gpu_genotype_counts": (I32, [P, P, P, P, P]),
+    "slemm_gpu_marker_qc": (I32, [P, I32, P, P]),
+    "slemm_gpu_hwe_exact": (I32, [P, P, P, I64, I32, P]),
+    "slemm_gpu_genotype_rows": (I32, [P, P, I32, P, I64, I32]),
     "slemm_gpu_set_weights": (I32, [P, P, P, P]),
     "slemm_gpu_set_projection": (I32, [P, P, I64, I32]),
     "slemm_gpu_set_precision": (I32, [P, I32]),
@@ -61,6 +69,9 @@ _SIGS = {
                                   ctypes.POINTER(RemlResult)]),
     "slemm_gpu_reml_lmc": (I32, [P, P, P, I64, I32, P, P, ctypes.POINTER(RemlOpts), P, P, P,
                                  ctypes.POINTER(RemlResult)]),
+    "slemm_gpu_reml_iter_weighting": (I32, [P, P, P, I64, I32, P, P, P, ctypes.POINTER(RemlOpts),
+                                            ctypes.POINTER(WindowOpts), P, P, P, P, P, P,
+                                            ctypes.POINTER(I32), ctypes.POINTER(RemlResult)]),
     "slemm_gpu_gebv": (I32, [P, P, P, P]),
     "slemm_gpu_score_terms": (I32, [P, P, I32, P, P]),
     "slemm_gpu_profile": (I32, [P, I32, I32, ctypes.POINTER(I32), P, P, P]),

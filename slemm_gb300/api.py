@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import (MEM_DEVICE, MEM_HOST, OP_LDET, OP_MATVEC, OP_QUADFORM, OP_RMATVEC,
+from ._lib import (WindowOpts, MEM_DEVICE, MEM_HOST, OP_LDET, OP_MATVEC, OP_QUADFORM, OP_RMATVEC,
                    OP_WRMATVEC, RemlOpts, RemlResult, check)
 
 _OP_OF_NAME = {"quadform": OP_QUADFORM, "ldet": OP_LDET}
@@ -83,6 +83,21 @@ class Genotypes:
         n2 = np.zeros(self.m, np.int32)
         check(self._lib.slemm_gpu_genotype_counts(self.h, _ptr(pc), _ptr(n0), _ptr(n1), _ptr(n2)))
         return pc, n0, n1, n2
+
+    def marker_qc(self, hwe_midp: int = 0):
+        """(maf, hwep) float32 per SNP — cal_maf_from_genobits / cal_hwep_from_genobits
+        (src/weight.cpp:3-15, src/input.cpp:10-22)."""
+        maf = np.zeros(self.m, np.float32)
+        hwep = np.zeros(self.m, np.float32)
+        check(self._lib.slemm_gpu_marker_qc(self.h, int(hwe_midp), _ptr(maf), _ptr(hwep)))
+        return maf, hwep
+
+    def genotype_rows(self, rows):
+        """n×len(rows) float32 allele-2 counts (missing = 1) of the given SNP rows."""
+        rows = np.ascontiguousarray(rows, np.int64).reshape(-1)
+        out = np.zeros((self.n, rows.size), np.float32, order="F")
+        check(self._lib.slemm_gpu_genotype_rows(self.h, _ptr(rows), rows.size, _ptr(out), self.n, MEM_HOST))
+        return out
 
     # ---- configuration -----------------------------------------------------------------------
     def set_weights(self, gm, w, rr=None):
@@ -202,6 +217,36 @@ class Genotypes:
                     n_criterion=r.n_criterion, seconds=r.seconds,
                     phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
+    def REML_iter_weighting(self, rvec, X, y, persnp, maf, lrt=True, seed=0, n_V=30, n_MC=0,
+                            n_MC_final=0, tol_L=5e-4, s2max=0.7, window_size=20, sig_chisq=1e6,
+                            indep_r2=0.5, max_fixed=64, verbose=False):
+        """`--iter_weighting` (src/option.cpp:437-530): equal-weight GREML, window weights from the
+        SNP-BLUP, fixed-effect SNPs by clumping, window-weighted GREML."""
+        rv, Xf, c, yv, ps = self._reml_args(rvec, X, y, persnp)
+        mf = np.ascontiguousarray(maf, np.float32)
+        o = RemlOpts(n_V, seed, tol_L, s2max, 1e-4, 1e-4, 600, int(verbose))
+        w = WindowOpts(int(window_size), float(sig_chisq), float(indep_r2), int(bool(lrt)), int(n_MC),
+                       int(n_MC_final), int(max_fixed))
+        Py = np.zeros(self.n, np.float32)
+        b = np.zeros(self.m, np.float32)
+        blue = np.zeros(c + max_fixed, np.float32)
+        vb = np.zeros((c + max_fixed) ** 2, np.float32)
+        p2 = np.zeros(self.m, np.float32)
+        fixed = np.zeros(max(max_fixed, 1), np.int64)
+        nf = ctypes.c_int(0)
+        r = RemlResult()
+        check(self._lib.slemm_gpu_reml_iter_weighting(self.h, _ptr(rv), _ptr(Xf), self.n, c, _ptr(yv), _ptr(ps),
+                                                      _ptr(mf), ctypes.byref(o), ctypes.byref(w), _ptr(Py),
+                                                      _ptr(b), _ptr(blue), _ptr(vb), _ptr(p2), _ptr(fixed),
+                                                      ctypes.byref(nf), ctypes.byref(r)))
+        k = nf.value
+        cc = c + k
+        out = dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue[:cc],
+                   fixed=list(fixed[:k]), persnp=p2, iters=(r.iters_y, r.iters_Q, r.iters_V))
+        if lrt:
+            out["var_blue"] = vb[:cc * cc].reshape(cc, cc, order="F")
+        return out
+
     def gebv(self, alpha, flip=None):
         """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""
         a = np.ascontiguousarray(alpha, np.float64)
@@ -247,6 +292,16 @@ class LSeed:
             self.close()
         except Exception:
             pass
+
+
+def hwe_exact(het, hom1, hom2, midp: int = 0) -> np.ndarray:
+    """SNPHWE2(het, hom1, hom2, midp) (src/snphwe.cpp:18) for arrays of count triples, FP64."""
+    het = np.ascontiguousarray(het, np.int32).reshape(-1)
+    hom1 = np.ascontiguousarray(hom1, np.int32).reshape(-1)
+    hom2 = np.ascontiguousarray(hom2, np.int32).reshape(-1)
+    p = np.zeros(het.size, np.float64)
+    check(_lib.load().slemm_gpu_hwe_exact(_ptr(het), _ptr(hom1), _ptr(hom2), het.size, int(midp), _ptr(p)))
+    return p
 
 
 def tridiag_eig(delta, beta):

@@ -264,6 +264,16 @@ __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int
 
 }  // namespace slemm
 
+namespace slemm {
+void row_counts_device(slemm_geno* g, int64_t* pc, int32_t* c1, int32_t* c2)
+{
+  const int th = 256;
+  row_counts_kernel<<<(unsigned)ceil_div(g->m * 32, th), th, 0, g->stream>>>(g->G.as<uint32_t>(), g->m,
+                                                                             g->n_pad / kTileK, pc, c1, c2);
+  LAUNCH_CHECK();
+}
+}  // namespace slemm
+
 using namespace slemm;
 
 // =================================================================================================
@@ -457,12 +467,7 @@ int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32
     d_pc.ensure(g->m * sizeof(int64_t));
     d_c1.ensure(g->m * sizeof(int32_t));
     d_c2.ensure(g->m * sizeof(int32_t));
-    const int th = 256;
-    const int64_t warps = g->m;
-    row_counts_kernel<<<(unsigned)ceil_div(warps * 32, th), th, 0, g->stream>>>(
-        g->G.as<uint32_t>(), g->m, g->n_pad / kTileK, d_pc.as<int64_t>(), d_c1.as<int32_t>(),
-        d_c2.as<int32_t>());
-    LAUNCH_CHECK();
+    row_counts_device(g, d_pc.as<int64_t>(), d_c1.as<int32_t>(), d_c2.as<int32_t>());
     std::vector<int64_t> pc(g->m);
     std::vector<int32_t> c1(g->m), c2(g->m);
     CUDA_TRY(cudaMemcpyAsync(pc.data(), d_pc.p, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost,

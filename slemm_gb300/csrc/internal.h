@@ -96,6 +96,9 @@ void lseed_free(slemm_lseed* S);
 // probes.cu — the reference's normalised Rademacher block (n×n_V, ld) on the device.
 void rademacher_device(int seed, int64_t n, int n_V, float* dV, int64_t ld, cudaStream_t st);
 
+// geno.cu — per-SNP popcounts (missing = 1) and class counts n1 (fields 01), n2 (fields 10).
+void row_counts_device(slemm_geno* g, int64_t* pc, int32_t* c1, int32_t* c2);
+
 int64_t workspace_bytes(const slemm_geno* g);
 // Reads (and clears) the device error word; throws if a kernel gave up a bounded wait.
 void check_device_error(slemm_geno* g);

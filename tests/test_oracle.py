@@ -62,6 +62,15 @@ def test_rng_draws_match_golden():
         assert np.array_equal(e.T, np.array(g[f"lmc_seed{seed}_m11_n7_nmc2_e"], np.float32))
 
 
+def test_hwe_exact_matches_reference_snphwe2():
+    """The oracle's exact HWE test reproduces every SNPHWE2 output of the reference (compiled
+    from src/snphwe.cpp) in tests/golden/hwe_ref.json, including mid-p and p ~ 1e-305."""
+    g = json.load(open(os.path.join(GOLD, "hwe_ref.json")))["cases"]
+    for het, h1, h2, midp, p in g:
+        v = orc.hwe_exact(het, h1, h2, midp)
+        assert abs(v - p) <= 1e-12 * p, (het, h1, h2, midp, p, v)
+
+
 def test_hwe_golden_fixture_sane():
     """The fixture holds the reference SNPHWE2 outputs; p-values lie in (0, 1] and mid-p ≤ p."""
     g = json.load(open(os.path.join(GOLD, "hwe_ref.json")))["cases"]

@@ -158,3 +158,37 @@ def test_gpu_probes_match_reference_draws(gpu, seed, n, n_V):
     _lib.check(gpu.slemm_gpu_rademacher(seed, n, n_V, V.ctypes.data_as(ctypes.c_void_p), n, 0))
     ref = orc.rademacher(seed, n, n_V)
     assert np.array_equal(V, ref)
+
+
+def _strong_problem(n=1500, m=2000, seed=43):
+    """A polygenic trait plus three large-effect SNPs (their per-SNP variance is >100× the mean;
+    the next largest is ~14×), so the fixed-SNP selection is clear-cut."""
+    counts, _ = synth.simulate_counts(n, m, seed=seed)
+    rows = synth.encode_bed(counts)
+    y, _, _ = synth.simulate_phenotype(counts, 0.3, n_causal=200, seed=seed)
+    for j in (300, 301, 1200):
+        x = counts[j].astype(np.float64)
+        y = y + 0.35 * (x - x.mean()) / x.std()
+    X = np.ones((n, 1), np.float32)
+    return counts, rows, y.astype(np.float32), X
+
+
+@pytest.mark.parametrize("lrt", [True, False])
+def test_iter_weighting_vs_oracle(gpu, lrt):
+    """--iter_weighting (src/option.cpp:437-530): same fixed SNPs, final weights, h² and BLUE as
+    the oracle's restatement of the two-stage flow."""
+    counts, rows, y, X = _strong_problem()
+    n, m = counts.shape[1], counts.shape[0]
+    persnp = np.ones(m, np.float32)
+    maf = orc.maf(orc.popcounts(counts), n)
+    kw = dict(lrt=lrt, seed=1, n_V=12, n_MC=4, window_size=20, sig_chisq=30.0, indep_r2=0.5)
+    r64 = orc.REML_iter_weighting(counts, None, X, y, persnp, maf, dtype=np.float64, **kw)
+    with api.Genotypes(rows, n) as g:
+        gmaf, _ = g.marker_qc()
+        assert np.array_equal(gmaf, maf)
+        r = g.REML_iter_weighting(None, X, y, persnp, gmaf, **kw)
+    assert r["fixed"] == r64["fixed"] == [1200, 300, 301]
+    assert np.allclose(r["persnp"], r64["persnp"], rtol=2e-3, atol=1e-4)
+    assert abs(r["h2"] - r64["h2"]) <= (2e-4 if lrt else 1e-4)
+    assert np.allclose(r["blue"], r64["blue"], rtol=5e-3, atol=5e-3)
+    assert np.corrcoef(r["snp_blup"], r64["snp_blup"])[0, 1] >= 0.9999
