@@ -210,6 +210,16 @@ int slemm_gpu_reml_iter_weighting(slemm_geno* g, const float* rvec, const float*
                                   float* persnp_out, int64_t* fixed_idx, int* n_fixed,
                                   slemm_reml_result* res);
 
+/* GWAS step 1 quadratic forms (`--lmm` with real markers, src/reml.cpp:919-981) for the
+ * .gstat.txt file: samples min(num_qf, #eligible) markers with gm·n > 20 and (2−gm)·n > 20 in
+ * the reference's order (std::random_shuffle on the C library's unseeded rand(), restated) and
+ * returns per marker xPy, xPx, xBx (window of window_size markers, even, ≤ 5000) and xSx.
+ * Uses the handle's weights (gm, gw, rr) and projection Q, as left by the REML driver; Py (n) and
+ * tau1 = ve/vg are that fit's.  Host pointers; variants/x* hold num_qf entries; *count = sampled. */
+int slemm_gpu_lmm_quadforms(slemm_geno* g, const float* Py, float tau1, float tol_L, int num_qf,
+                            int window_size, int64_t* variants, float* xPy, float* xPx, float* xBx,
+                            float* xSx, int* count);
+
 /* ---- prediction and GWAS score statistics ------------------------------------------------- */
 /* GEBV: tgv_i = Σ_j (flip_j ? 2−count_ij : count_ij)·alpha_j, FP64 accumulation of exact
  * integer counts (src/pred.cpp:112-130).  Uses the handle's genotypes (no centring). flip: m

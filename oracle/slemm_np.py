@@ -40,6 +40,9 @@ def _lib():
             lib.oracle_bed_decode.argtypes = [P, I64, I64, I64, P, P, I64]
             lib.oracle_popcounts.argtypes = [P, I64, I64, P]
             lib.oracle_hwe_counts.argtypes = [P, I64, I64, P, P, P]
+            lib.oracle_lmm_variants.argtypes = [P, I64, I64, ctypes.c_int, P]
+            lib.oracle_lmm_variants.restype = ctypes.c_int
+            lib.oracle_libc_rand.argtypes = [ctypes.c_uint, ctypes.c_int, P]
             lib.oracle_maf.argtypes = [P, I64, I64, P]
             lib.oracle_gm.argtypes = [P, I64, I64, P]
             lib.oracle_gebv.argtypes = [P, I64, I64, P, P, P]
@@ -599,6 +602,55 @@ def LMC_REML(counts, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, 
     blue = np.linalg.solve(Xd64.T @ Xd64, Xd64.T @ v0.astype(np.float64))
     return dict(vg=vg, ve=ve, h2=float(s2), Py=Py, snp_blup=snp_blup, blue=blue,
                 iters=seed_V["iters"], secant=trace, gm=gm, gw=gw, n_MC=n_MC)
+
+
+def lmm_variants(gm, n: int, num_qf: int = 30) -> list:
+    """src/reml.cpp:919-925 — markers with MAC > 20 on both alleles in file order, shuffled by
+    libstdc++ std::random_shuffle on the C library's unseeded rand(); the first num_qf."""
+    gm = np.ascontiguousarray(gm, np.float32)
+    out = np.zeros(max(num_qf, 1), np.int64)
+    k = _lib().oracle_lmm_variants(_p(gm), gm.size, n, num_qf, _p(out))
+    return [int(v) for v in out[:k]]
+
+
+def LMM_quadforms(counts, Py, rr, Q, gm, gw, tau1, num_qf=30, window_size=1000, tol_L=5e-4,
+                  dtype=np.float64):
+    """src/reml.cpp:919-981 (--lmm, real markers): for the sampled markers x (centred counts),
+    xPy = xᵀPy; with v = (I − QQᵀ)(rr∘x): xPx = vᵀ(H0 + τ1)⁻¹v by one Lanczos seed and solve,
+    xSx = ‖v‖², and xBx = (xSx − zᵀ(ZᵀZ + τ1·diag(1/gw))⁻¹z)/τ1 with Z the projected, rr-scaled
+    centred counts of the window_size markers around x (clamped at the ends) and z = Zᵀv."""
+    dt = dtype
+    counts = np.asarray(counts)
+    m, n = counts.shape
+    gm = np.asarray(gm, np.float32)
+    variants = lmm_variants(gm, n, num_qf)
+    rr = np.asarray(rr, dt)
+    Q = np.asarray(Q, dt).reshape(n, -1)
+    V = counts[variants].T.astype(dt) - gm[variants].astype(dt)
+    xPy = V.T @ np.asarray(Py, dt)
+    V = rr[:, None] * V
+    V = V - Q @ (Q.T @ V)
+    ops = Operators(counts, gm, gw, rr, Q, dtype=dt)
+    seed_V = L_Seed(ops, "quadform", tau1, V, tol_L)
+    X = L_Solve(seed_V, V, 0.0)
+    xPx = np.einsum("ij,ij->j", V, X)
+    xSx = np.einsum("ij,ij->j", V, V)
+    xBx = np.zeros(len(variants), dt)
+    gw = np.asarray(gw, dt)
+    for i, j in enumerate(variants):
+        if j < window_size // 2:
+            wds = 0
+        elif j > m - window_size // 2:
+            wds = m - window_size
+        else:
+            wds = j - window_size // 2
+        Z = counts[wds:wds + window_size].T.astype(dt) - gm[wds:wds + window_size].astype(dt)
+        Z = rr[:, None] * Z
+        Z = Z - Q @ (Q.T @ Z)
+        G = Z.T @ Z + np.diag(tau1 / gw[wds:wds + window_size])
+        z = Z.T @ V[:, i]
+        xBx[i] = (xSx[i] - z @ np.linalg.solve(G, z)) / tau1
+    return dict(variants=variants, xPy=xPy, xPx=xPx, xBx=xBx, xSx=xSx, iters=seed_V["iters"])
 
 
 def n_mc_rule(n: int) -> int:

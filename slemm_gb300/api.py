@@ -247,6 +247,20 @@ class Genotypes:
             out["var_blue"] = vb[:cc * cc].reshape(cc, cc, order="F")
         return out
 
+    def LMM_quadforms(self, Py, tau1, num_qf=30, window_size=1000, tol_L=5e-4):
+        """--lmm quadratic forms (src/reml.cpp:919-981): dict of variants, xPy, xPx, xBx, xSx."""
+        py = np.ascontiguousarray(Py, np.float32)
+        var = np.zeros(num_qf, np.int64)
+        out = {k: np.zeros(num_qf, np.float32) for k in ("xPy", "xPx", "xBx", "xSx")}
+        cnt = ctypes.c_int(0)
+        check(self._lib.slemm_gpu_lmm_quadforms(self.h, _ptr(py), float(tau1), float(tol_L), int(num_qf),
+                                                int(window_size), _ptr(var), _ptr(out["xPy"]), _ptr(out["xPx"]),
+                                                _ptr(out["xBx"]), _ptr(out["xSx"]), ctypes.byref(cnt)))
+        k = cnt.value
+        res = {key: v[:k] for key, v in out.items()}
+        res["variants"] = [int(v) for v in var[:k]]
+        return res
+
     def gebv(self, alpha, flip=None):
         """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""
         a = np.ascontiguousarray(alpha, np.float64)

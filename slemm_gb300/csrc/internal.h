@@ -64,6 +64,10 @@ void op_device(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_
 void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                      float* out, int64_t ld_out, int nq);
 
+// Centred Z_cᵀU over SNP rows [r0, r0 + rows) (multiples of 256) with `pieces` BF16 pieces (ops.cu).
+void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64_t ldu, int k, float* out,
+                  int64_t ldo, int pieces);
+
 // Column reductions with FP64 accumulation, deterministic two-stage (ops.cu).
 // dots[c] = Σ_i a[i,c]·b[i,c] over i < n for c < k (b == nullptr → Σ a²).  Result on device.
 void col_dots(slemm_geno* g, const float* a, int64_t lda, const float* b, int64_t ldb,

@@ -594,6 +594,54 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   }
 }
 
+// out[j, c] = Σ_i (count_ij − gm_j)·U[i, c] for SNP rows j ∈ [r0, r0 + rows) of the G copy (the
+// centred Z_cᵀU of a window of SNPs), with `pieces` BF16 pieces on the tensor cores (3: about
+// FP32 accuracy).  r0 and rows must be multiples of 256; U is n×k (ld ldu), out rows×k (ld ldo).
+void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64_t ldu, int k, float* out,
+                  int64_t ldo, int pieces)
+{
+  CHECK_ARG(r0 % kPadRows == 0 && rows % kPadRows == 0 && r0 + rows <= g->m_pad, "row range not aligned");
+  CHECK_ARG(pieces >= 2 && pieces <= 3, "pieces must be 2 or 3");
+  cudaStream_t st = g->stream;
+  const int grp = pieces == 3 ? 80 : 128;
+  const int64_t K_pad = g->n_pad, K_tiles = K_pad / kTileK;
+  const uint8_t* A = g->G.as<uint8_t>() + (size_t)(r0 / kTileM) * K_tiles * kTileBytes;
+  const int nblk_n = (int)ceil_div(g->n_pad, kRowsPerBlock);
+  const int nblk_m = (int)ceil_div(rows, kRowsPerBlock);
+  const int64_t m_valid = std::max<int64_t>(0, std::min<int64_t>(rows, g->m - r0));
+  for (int c0 = 0; c0 < k; c0 += grp) {
+    const int kc = std::min(grp, k - c0);
+    PassPlan p;
+    p.tc = true;
+    p.pieces = pieces;
+    p.N = (int)round_up((int64_t)pieces * kc, 16);
+    p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms());
+    const int pad = p.N - pieces * kc;
+    void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
+    float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.N * rows * sizeof(float));
+    double* r_col = (double*)g->ws_red.ensure((size_t)kc * nblk_n * sizeof(double));
+    const float* in = U + (int64_t)c0 * ldu;
+    if (vec4_ok(g->n, ldu, in))
+      prologue_indiv_kernel<4><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
+          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n);
+    else
+      prologue_indiv_kernel<1><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
+          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n);
+    LAUNCH_CHECK();
+    run_gemm(g, p, A, rows, K_pad, B1, D, g->err.as<int>(), kc, 1);
+    float* o = out + (int64_t)c0 * ldo;
+    if (vec4_ok(m_valid, ldo, o))
+      finalize_snp_kernel<4><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
+          D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
+          nullptr, nullptr, 0);
+    else
+      finalize_snp_kernel<1><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
+          D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
+          nullptr, nullptr, 0);
+    LAUNCH_CHECK();
+  }
+}
+
 void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                      float* out, int64_t ld_out, int nq)
 {

@@ -71,6 +71,18 @@ def test_hwe_exact_matches_reference_snphwe2():
         assert abs(v - p) <= 1e-12 * p, (het, h1, h2, midp, p, v)
 
 
+def test_lmm_variant_sample_is_libstdcxx_random_shuffle():
+    """The --lmm marker sample uses std::random_shuffle on the unseeded C rand(): the oracle calls
+    the real library; check its first draws and the MAC > 20 filter."""
+    import ctypes
+    out = np.zeros(3, np.int32)
+    orc._lib().oracle_libc_rand(1, 3, out.ctypes.data_as(ctypes.c_void_p))
+    assert list(out) == [1804289383, 846930886, 1681692777]   # glibc's documented initial sequence
+    gm = np.array([0.01, 0.5, 1.0, 1.99, 0.3, 1.5], np.float32)
+    v = orc.lmm_variants(gm, 1000, 30)
+    assert sorted(v) == [1, 2, 4, 5]
+
+
 def test_hwe_golden_fixture_sane():
     """The fixture holds the reference SNPHWE2 outputs; p-values lie in (0, 1] and mid-p ≤ p."""
     g = json.load(open(os.path.join(GOLD, "hwe_ref.json")))["cases"]

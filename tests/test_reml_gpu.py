@@ -192,3 +192,26 @@ def test_iter_weighting_vs_oracle(gpu, lrt):
     assert abs(r["h2"] - r64["h2"]) <= (2e-4 if lrt else 1e-4)
     assert np.allclose(r["blue"], r64["blue"], rtol=5e-3, atol=5e-3)
     assert np.corrcoef(r["snp_blup"], r64["snp_blup"])[0, 1] >= 0.9999
+
+
+@pytest.mark.parametrize("window_size,c", [(100, 2), (1000, 1)])
+def test_lmm_quadforms_vs_oracle(gpu, window_size, c):
+    """--lmm quadratic forms (src/reml.cpp:919-981): the reference's marker sample, and xPy, xPx,
+    xBx, xSx against the FP64 oracle (relative tolerance 1e-4 on xPy, xSx; 5e-4 on xPx, xBx)."""
+    counts, rows, y, rvec, X, persnp = _problem(n=1500, m=2600, seed=47, c=c)
+    n, m = counts.shape[1], counts.shape[0]
+    pc = orc.popcounts(counts)
+    gm = orc.genotype_mean(pc, n)
+    gw = orc.snp_weights(gm, persnp)
+    rr = (1 / np.sqrt(rvec)).astype(np.float32)
+    Q, _, _ = orc.qr_colpiv(rr[:, None] * X)
+    Py = np.random.default_rng(3).standard_normal(n).astype(np.float32)
+    tau1 = 1.7
+    ref = orc.LMM_quadforms(counts, Py, rr, Q, gm, gw, tau1, num_qf=30, window_size=window_size)
+    with api.Genotypes(rows, n) as g:
+        g.set_weights(gm, gw, rr)
+        g.set_projection(Q.astype(np.float32))
+        r = g.LMM_quadforms(Py, tau1, num_qf=30, window_size=window_size)
+    assert r["variants"] == ref["variants"]
+    for key, tol in (("xPy", 1e-4), ("xSx", 1e-4), ("xPx", 5e-4), ("xBx", 5e-4)):
+        assert np.allclose(r[key], ref[key], rtol=tol, atol=tol * np.max(np.abs(ref[key]))), key
