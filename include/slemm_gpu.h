@@ -220,6 +220,20 @@ int slemm_gpu_lmm_quadforms(slemm_geno* g, const float* Py, float tau1, float to
                             int window_size, int64_t* variants, float* xPy, float* xPx, float* xBx,
                             float* xSx, int* count);
 
+/* Windowed MLMA of slemm_gwa.py (bin/slemm_gwa.py:259-434) for the variants test_begin …
+ * test_end (handle indices, one chromosome).  The handle holds every variant of the .bed for the
+ * GWA samples.  y = the Py column of .reml.py.txt, R its last column (NULL = ones), covar its
+ * covariates (n×c, ldc); model_idx = increasing handle indices of the chromosome's model SNPs
+ * (.reml.snp.csv); block_size = the .gstat.txt WindowSize; tau = Ve/Vg; model_snp_ct, snp_var
+ * from .reml.vc.csv; cfactor = mean(xBx/xPx) of .gstat.txt; mac the final minor-allele-count
+ * filter.  Outputs per tested variant (host): beta, se, chisq (FP32, allele 1 = the .bim's
+ * allele 1 as pgenlib counts it) and pval (FP64); NaN where filtered. */
+int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float* R, const float* covar,
+                          int64_t ldc, int c, const int64_t* model_idx, int64_t n_model,
+                          int64_t test_begin, int64_t test_end, int block_size, float tau,
+                          int64_t model_snp_ct, float cfactor, float snp_var, int mac,
+                          float* beta, float* se, float* chisq, double* pval);
+
 /* ---- prediction and GWAS score statistics ------------------------------------------------- */
 /* GEBV: tgv_i = Σ_j (flip_j ? 2−count_ij : count_ij)·alpha_j, FP64 accumulation of exact
  * integer counts (src/pred.cpp:112-130).  Uses the handle's genotypes (no centring). flip: m

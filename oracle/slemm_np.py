@@ -653,6 +653,93 @@ def LMM_quadforms(counts, Py, rr, Q, gm, gw, tau1, num_qf=30, window_size=1000, 
     return dict(variants=variants, xPy=xPy, xPx=xPx, xBx=xBx, xSx=xSx, iters=seed_V["iters"])
 
 
+def gwa_blocks(ksnp_idx, block_size, chr_start, chr_end):
+    """bin/slemm_gwa.py:322-345 — overlapping blocks of model SNPs (step block_size/2) and the
+    range of tested variants each block serves."""
+    ksnp_idx = np.asarray(ksnp_idx, np.int64)
+    ksnp_ct = ksnp_idx.size
+    if block_size > ksnp_ct:
+        block_size = int(ksnp_ct / 2) * 2
+    step = int(block_size / 2)
+    ext = int(step / 2)
+    block_ct = int((ksnp_ct - step) / step)
+    blocks = [ksnp_idx[i * step:i * step + block_size] for i in range(block_ct)]
+    if (ksnp_ct - step) % step != 0:
+        blocks.append(ksnp_idx[ksnp_ct - block_size:ksnp_ct])
+    bounds = np.empty((len(blocks), 2), np.int64)
+    bounds[0, 0] = chr_start
+    bounds[0, 1] = blocks[0][block_size - ext]
+    for i in range(1, len(blocks)):
+        bounds[i, 0] = bounds[i - 1, 1]
+        bounds[i, 1] = blocks[i][block_size - ext]
+    bounds[-1, 1] = chr_end + 1
+    return blocks, bounds, block_size
+
+
+def gwa_windows(a1_counts, y, R, covar, ksnp_idx, chr_start, chr_end, block_size, tau, model_snp_ct,
+                cfactor, snp_var, mac):
+    """bin/slemm_gwa.py:259-431 — windowed MLMA for the variants chr_start … chr_end.  a1_counts is
+    m×n allele-1 counts (pgenlib's convention, 2 − the .bed A2 count); y the Py column of
+    .reml.py.txt; R its last column; covar its covariates.  FP32 as the script (numpy float32).
+    Returns beta, se, chisq, p (FP32, p FP64) over the tested range; NaN where MAC ≤ mac."""
+    from scipy import linalg
+    from scipy.stats import chi2
+    f32 = np.float32
+    n = y.size
+    vec_y = np.asarray(y, f32)
+    vec_rr = np.asarray(R, f32)
+    mat_covar = np.asarray(covar, f32).reshape(n, -1)
+    is_one_rr = bool(np.min(vec_rr) > 0.99999 and np.max(vec_rr) < 1.00001)
+    is_const_covar = bool(mat_covar.shape[1] == 1 and np.max(mat_covar) == np.min(mat_covar))
+    vec_rr = (1.0 / np.sqrt(vec_rr)).astype(f32)
+    mat_covar = np.transpose(np.transpose(mat_covar) * vec_rr)
+    Q = linalg.qr(mat_covar, mode="economic")[0]
+    blocks, bounds, block_size = gwa_blocks(ksnp_idx, block_size, chr_start, chr_end)
+    step = int(block_size / 2)
+    tested = chr_end - chr_start + 1
+    st_xx = np.empty(tested, f32)
+    st_xy = np.empty(tested, f32)
+    A = np.asarray(a1_counts)
+
+    def prep(rows):
+        b = A[rows].astype(f32)
+        mean = b.mean(axis=1, keepdims=True)
+        rv = ((2. - mean) * mean / 2.)[:, 0]
+        b = b - mean
+        if not is_one_rr:
+            b = b * vec_rr
+        if not (is_one_rr and is_const_covar):
+            b = b - np.matmul(np.matmul(b, Q), np.transpose(Q))
+        return b.astype(f32), rv.astype(f32)
+
+    for i, blk in enumerate(blocks):
+        buf2, rvars = prep(blk)
+        mat_h = np.matmul(buf2, np.transpose(buf2))
+        mat_h.ravel()[::mat_h.shape[1] + 1] += model_snp_ct * tau * rvars
+        cf = linalg.cho_factor(mat_h)
+        for j in range(bounds[i, 0], bounds[i, 1]):
+            x = A[j].astype(f32)
+            sx = x.sum()
+            if sx <= mac or (2 * n - sx) <= mac:
+                st_xx[j - chr_start] = np.nan
+                st_xy[j - chr_start] = np.nan
+                continue
+            x = x - sx / n
+            st_xy[j - chr_start] = np.dot(x, vec_y)
+            if not is_one_rr:
+                x = x * vec_rr
+            if not (is_one_rr and is_const_covar):
+                x = x - np.dot(Q, np.dot(np.transpose(Q), x))
+            zx = np.dot(buf2, x)
+            st_xx[j - chr_start] = np.dot(x, x) - np.dot(zx, linalg.cho_solve(cf, zx))
+    st_xx /= tau
+    beta = st_xy / st_xx * cfactor
+    serr = np.sqrt((snp_var * cfactor) / st_xx)
+    chisq = np.square(beta / serr)
+    pval = chi2.sf(chisq, 1)
+    return beta, serr, chisq, pval
+
+
 def n_mc_rule(n: int) -> int:
     """src/option.cpp:381,414 — n_MC = max(min(int(4e9/n/n), 30), 3)."""
     return max(min(int(4e9 / n / n), 30), 3)

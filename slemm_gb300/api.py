@@ -261,6 +261,23 @@ class Genotypes:
         res["variants"] = [int(v) for v in var[:k]]
         return res
 
+    def gwa_windows(self, y, R, covar, model_idx, test_begin, test_end, block_size, tau, model_snp_ct,
+                    cfactor, snp_var, mac=20):
+        """slemm_gwa.py windowed MLMA (bin/slemm_gwa.py:259-434): beta, se, chisq, p per tested
+        variant test_begin … test_end (allele 1 orientation)."""
+        yv = np.ascontiguousarray(y, np.float32)
+        Rv = None if R is None else np.ascontiguousarray(R, np.float32)
+        cv = np.asfortranarray(np.asarray(covar, np.float32).reshape(self.n, -1))
+        mi = np.ascontiguousarray(model_idx, np.int64)
+        t = test_end - test_begin + 1
+        beta, se, chisq = (np.zeros(t, np.float32) for _ in range(3))
+        p = np.zeros(t, np.float64)
+        check(self._lib.slemm_gpu_gwa_windows(self.h, _ptr(yv), _ptr(Rv), _ptr(cv), self.n, cv.shape[1], _ptr(mi),
+                                              mi.size, int(test_begin), int(test_end), int(block_size), float(tau),
+                                              int(model_snp_ct), float(cfactor), float(snp_var), int(mac),
+                                              _ptr(beta), _ptr(se), _ptr(chisq), _ptr(p)))
+        return beta, se, chisq, p
+
     def gebv(self, alpha, flip=None):
         """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""
         a = np.ascontiguousarray(alpha, np.float64)

@@ -68,6 +68,9 @@ void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64
 void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64_t ldu, int k, float* out,
                   int64_t ldo, int pieces);
 
+// reml.cu — orthonormal basis (FP64 column-pivoted QR) of an n×c matrix; returns the rank.
+int orthonormal_columns(const std::vector<double>& A, int64_t n, int c, std::vector<double>& Q);
+
 // Column reductions with FP64 accumulation, deterministic two-stage (ops.cu).
 // dots[c] = Σ_i a[i,c]·b[i,c] over i < n for c < k (b == nullptr → Σ a²).  Result on device.
 void col_dots(slemm_geno* g, const float* a, int64_t lda, const float* b, int64_t ldb,

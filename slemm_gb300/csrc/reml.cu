@@ -269,6 +269,15 @@ static Setup reml_setup(slemm_geno* g, const float* rvec, const float* X, int64_
   return S;
 }
 
+// Orthonormal basis of the columns of an n×c matrix (column-pivoted Householder QR, FP64); returns
+// the numerical rank and Q (n×rank).
+int orthonormal_columns(const std::vector<double>& A, int64_t n, int c, std::vector<double>& Q)
+{
+  QRHost r = qr_colpiv(A, n, c);
+  Q = std::move(r.Q);
+  return r.rank;
+}
+
 static void upload(slemm_geno* g, float* d, const float* h, size_t cnt)
 {
   CUDA_TRY(cudaMemcpyAsync(d, h, cnt * sizeof(float), cudaMemcpyHostToDevice, g->stream));

@@ -44,3 +44,38 @@ def make_case(n_fam, m, seed=1, missing=0.0, keep_frac=1.0):
         keep_idx = np.nonzero(keep_mask)[0].astype(np.int64)
     dec = orc.bed_decode(rows, n_fam, keep_mask)
     return rows, keep_idx, dec
+
+
+def load_gwa_case(d):
+    """Inputs of bin/slemm_gwa.py for a golden case, parsed as the script does (:137-260): Py,
+    covariates and R from .reml.py.txt; model SNPs of chromosome 1 (.reml.snp.csv order mapped to
+    .bim indices); block size and cfactor = mean(xBx/xPx) from .gstat.txt; Vg/Ve and the model SNP
+    count from .reml.vc.csv; the .bed rows and decoded A2 counts.  Returns a dict."""
+    import os
+    from oracle import slemm_np as orc
+    fam = [l.split() for l in open(os.path.join(d, "geno.fam"))]
+    bim = [l.split() for l in open(os.path.join(d, "geno.bim"))]
+    n_fam = len(fam)
+    raw = np.fromfile(os.path.join(d, "geno.bed"), dtype=np.uint8)[3:]
+    rows = raw.reshape(-1, (n_fam + 3) // 4)
+    py = [l.split() for l in open(os.path.join(d, "s1.reml.py.txt")).read().splitlines()[1:]]
+    y = np.array([float(r[1]) for r in py], np.float32)
+    covar = np.array([[float(v) for v in r[2:-1]] for r in py], np.float32)
+    R = np.array([float(r[-1]) for r in py], np.float32)
+    gs = [l.split() for l in open(os.path.join(d, "s1.gstat.txt")).read().splitlines()[1:]]
+    cfactor = sum(float(r[8]) / float(r[7]) for r in gs) / len(gs)
+    block_size = int(gs[-1][10])
+    vc = open(os.path.join(d, "s1.reml.vc.csv")).read().splitlines()
+    model_snp_ct = int(vc[1].split(",")[1])
+    snp_var = float(vc[2].split(",")[1])
+    err_var = float(vc[3].split(",")[1])
+    ksnp = {l.split(",")[0] for l in open(os.path.join(d, "s1.reml.snp.csv")).read().splitlines()[1:]
+            if l.split(",")[1] == "1"}
+    ksnp_idx = [j for j, b in enumerate(bim) if b[1] in ksnp]
+    chr_idx = [j for j, b in enumerate(bim) if b[0] == "1"]
+    dec = orc.bed_decode(rows, n_fam)
+    out = [l.split("\t") for l in open(os.path.join(d, "gwa.txt")).read().splitlines()[1:]]
+    ref = {k: np.array([float(r[i]) for r in out]) for k, i in (("beta", 6), ("se", 7), ("chisq", 8), ("p", 9))}
+    return dict(rows=rows, n_fam=n_fam, a2=dec, y=y, covar=covar, R=R, cfactor=cfactor, block_size=block_size,
+                model_snp_ct=model_snp_ct, snp_var=snp_var, tau=err_var / snp_var, ksnp_idx=ksnp_idx,
+                chr_start=min(chr_idx), chr_end=max(chr_idx), ref=ref, mac=20)

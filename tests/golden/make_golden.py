@@ -10,7 +10,9 @@ oracle/_ref exist; the fixtures are committed and the tests read only them).
   gamma_case/        a small synthetic .bed/.bim/.fam with SLEMM step-1 style inputs and the
                      output of the reference's bin/slemm_gamma.py run on it (pgenlib replaced
                      by tests/golden/pgenlib_shim, which reads PLINK1 .bed files).
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+  gwa_case/          the same kind of case for the reference's bin/slemm_gwa.py (windowed
+                     MLMA on chromosome 1), with step-1 files from the oracle.
+Usage: python tests/golden/make_golden.py [/path/to/reference] [gwa]
 """
 import ctypes
 import json
@@ -109,9 +111,65 @@ def gamma_case():
                     os.path.join(d, "gamma.txt")], check=True, env=env, capture_output=True)
 
 
+def gwa_case():
+    """Runs the reference's bin/slemm_gwa.py (windowed MLMA) on a synthetic two-chromosome case.
+    Step-1 files come from the oracle: MC-REML on the model SNPs (every chromosome-2 SNP and all
+    chromosome-1 SNPs but every 7th), and real --lmm quadratic forms for .gstat.txt."""
+    from oracle import slemm_np as orc
+    from slemm_gb300 import synth
+    d = os.path.join(HERE, "gwa_case")
+    os.makedirs(d, exist_ok=True)
+    n, m = 500, 420
+    counts, _ = synth.simulate_counts(n, m, seed=33)
+    rows = synth.encode_bed(counts, 0.0)
+    chrom = [1] * 360 + [2] * 60
+    ids, iids = synth.write_plink(os.path.join(d, "geno"), rows, n, chrom=chrom)
+    y, _, _ = synth.simulate_phenotype(counts, 0.5, n_causal=40, seed=33)
+    rng = np.random.default_rng(12)
+    rvec = rng.uniform(0.8, 1.5, n).astype(np.float32)
+    X = np.column_stack([np.ones(n), rng.standard_normal(n)]).astype(np.float32)
+    model = [j for j in range(m) if chrom[j] == 2 or j % 7 != 3]
+    cm = counts[model]
+    res = orc.LMC_REML(cm, rvec, X, y.astype(np.float32), np.ones(len(model), np.float32), seed=5,
+                       n_MC=4, dtype=np.float32)
+    pc = orc.popcounts(cm)
+    gm = orc.genotype_mean(pc, n)
+    gw = orc.snp_weights(gm, np.ones(len(model), np.float32))
+    rr = (1.0 / np.sqrt(rvec)).astype(np.float32)
+    Q, _, _ = orc.qr_colpiv(rr[:, None].astype(np.float64) * X, dtype=np.float32)
+    tau1 = res["ve"] / res["vg"]
+    ws = 60
+    qf = orc.LMM_quadforms(cm, res["Py"], rr, Q, gm, gw, tau1, num_qf=30, window_size=ws)
+    with open(os.path.join(d, "s1.reml.py.txt"), "w") as f:
+        f.write("IID Py intercept x1 R\n")
+        for i in range(n):
+            f.write(f"{iids[i]} {res['Py'][i]:.6g} {X[i,0]:.6g} {X[i,1]:.6g} {rvec[i]:.6g}\n")
+    with open(os.path.join(d, "s1.reml.vc.csv"), "w") as f:
+        f.write(f"pop_size,{n}\nnum_markers,{len(model)}\nVg,{res['vg']:.6g}\nVe,{res['ve']:.6g}\n")
+    with open(os.path.join(d, "s1.reml.snp.csv"), "w") as f:
+        f.write("SNP,Chr,Pos,Allele1,Allele2,MAF,HWE_Pval,Group,Weight,Effect\n")
+        for k, j in enumerate(model):
+            f.write(f"{ids[j]},{chrom[j]},{1000 * (j + 1)},2,1,0.1,0.5,NULL,1,{res['snp_blup'][k]:.6g}\n")
+    with open(os.path.join(d, "s1.gstat.txt"), "w") as f:
+        f.write("variant\tChr\tPos\tMAC\tMAF\tHWEP\txPy\txPx\txBx\txSx\tWindowSize\tChiSq\tPval\n")
+        for k, j in enumerate(qf["variants"]):
+            jj = model[j]
+            f.write(f"{ids[jj]}\t{chrom[jj]}\t{1000 * (jj + 1)}\t50\t0.1\t0.5\t{qf['xPy'][k]:.6g}\t"
+                    f"{qf['xPx'][k]:.6g}\t{qf['xBx'][k]:.6g}\t{qf['xSx'][k]:.6g}\t{ws}\t0.1\t0.7\n")
+    env = dict(os.environ, PYTHONPATH=os.path.join(HERE, "pgenlib_shim"))
+    subprocess.run([sys.executable, os.path.join(REF, "bin", "slemm_gwa.py"), "--pfile",
+                    os.path.join(d, "geno"), "--slemm", os.path.join(d, "s1"), "--out",
+                    os.path.join(d, "gwa.txt"), "--chr", "1"], check=True, env=env, capture_output=True)
+
+
 if __name__ == "__main__":
+    only = sys.argv[2] if len(sys.argv) > 2 else None
+    if only == "gwa":
+        gwa_case()
+        sys.exit(0)
     hwe()
     rng_draws()
     formats()
     gamma_case()
+    gwa_case()
     print("golden fixtures written to", HERE)

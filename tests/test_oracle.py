@@ -83,6 +83,21 @@ def test_lmm_variant_sample_is_libstdcxx_random_shuffle():
     assert sorted(v) == [1, 2, 4, 5]
 
 
+def test_gwa_windows_oracle_matches_reference_script():
+    """The oracle restatement of bin/slemm_gwa.py:259-431 reproduces the reference script's output
+    on the golden case (tests/golden/gwa_case, run with a PLINK1 stand-in for pgenlib)."""
+    from conftest import load_gwa_case
+    c = load_gwa_case(os.path.join(GOLD, "gwa_case"))
+    beta, se, chisq, p = orc.gwa_windows(2 - c["a2"], c["y"], c["R"], c["covar"], c["ksnp_idx"], c["chr_start"],
+                                         c["chr_end"], c["block_size"], c["tau"], c["model_snp_ct"], c["cfactor"],
+                                         c["snp_var"], c["mac"])
+    ref = c["ref"]
+    ok = np.isfinite(ref["p"])
+    assert np.array_equal(ok, np.isfinite(p))
+    assert np.allclose(beta[ok], ref["beta"][ok], rtol=1e-4, atol=1e-6)
+    assert np.max(np.abs(np.log10(p[ok]) - np.log10(ref["p"][ok]))) <= 1e-4
+
+
 def test_hwe_golden_fixture_sane():
     """The fixture holds the reference SNPHWE2 outputs; p-values lie in (0, 1] and mid-p ≤ p."""
     g = json.load(open(os.path.join(GOLD, "hwe_ref.json")))["cases"]

@@ -215,3 +215,19 @@ def test_lmm_quadforms_vs_oracle(gpu, window_size, c):
     assert r["variants"] == ref["variants"]
     for key, tol in (("xPy", 1e-4), ("xSx", 1e-4), ("xPx", 5e-4), ("xBx", 5e-4)):
         assert np.allclose(r[key], ref[key], rtol=tol, atol=tol * np.max(np.abs(ref[key]))), key
+
+
+def test_gwa_windows_vs_reference_script(gpu):
+    """Windowed MLMA (bin/slemm_gwa.py:259-434) on the golden case produced by the reference's own
+    script: same NaN pattern, beta within 1e-3 relative, −log10 p within 2e-3."""
+    from conftest import load_gwa_case
+    c = load_gwa_case(os.path.join(GOLD, "gwa_case"))
+    with api.Genotypes(c["rows"], c["n_fam"]) as g:
+        beta, se, chisq, p = g.gwa_windows(c["y"], c["R"], c["covar"], c["ksnp_idx"], c["chr_start"], c["chr_end"],
+                                           c["block_size"], c["tau"], c["model_snp_ct"], c["cfactor"], c["snp_var"],
+                                           c["mac"])
+    ref = c["ref"]
+    ok = np.isfinite(ref["p"])
+    assert np.array_equal(ok, np.isfinite(p))
+    assert np.allclose(beta[ok], ref["beta"][ok], rtol=1e-3, atol=1e-5)
+    assert np.max(np.abs(np.log10(p[ok]) - np.log10(ref["p"][ok]))) <= 2e-3
