@@ -234,6 +234,15 @@ int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float* R, const f
                           int64_t model_snp_ct, float cfactor, float snp_var, int mac,
                           float* beta, float* se, float* chisq, double* pval);
 
+/* SNP effects by weighted least squares (`--wls`, src/wls.cpp:4-129): with
+ * Z̃ = (I − QQᵀ)(rr∘(Cnt − gm)), rr = rvec^(−1/2), Q an orthonormal basis of rr∘X,
+ * snp_blup = (Z̃ᵀZ̃ + 1e-4·mean(diag)·I)⁻¹ Z̃ᵀ(I − QQᵀ)(rr∘y), Cholesky in FP32 like the reference.
+ * Sets the handle's weights (gm = popcount/n, rr) and projection.  Needs 4·m² bytes of device
+ * memory for the m×m system.  Host pointers: rvec (n, NULL = ones), X (n×c, ldx), y (n),
+ * snp_blup (m). */
+int slemm_gpu_wls(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
+                  const float* y, float* snp_blup);
+
 /* ---- prediction and GWAS score statistics ------------------------------------------------- */
 /* GEBV: tgv_i = Σ_j (flip_j ? 2−count_ij : count_ij)·alpha_j, FP64 accumulation of exact
  * integer counts (src/pred.cpp:112-130).  Uses the handle's genotypes (no centring). flip: m

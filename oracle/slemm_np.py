@@ -740,6 +740,28 @@ def gwa_windows(a1_counts, y, R, covar, ksnp_idx, chr_start, chr_end, block_size
     return beta, serr, chisq, pval
 
 
+def WLS(counts, rvec, X, y, dtype=np.float64):
+    """src/wls.cpp:4-129 — SNP effects by weighted least squares: with Z̃ = (I − QQᵀ)(rr∘(Cnt − gm)),
+    solve (Z̃ᵀZ̃ + 1e-4·mean(diag(Z̃ᵀZ̃))·I) b = Z̃ᵀ(I − QQᵀ)(rr∘y)."""
+    dt = dtype
+    counts = np.asarray(counts)
+    m, n = counts.shape
+    rvec = np.ones(n) if rvec is None else np.asarray(rvec, np.float64)
+    rr = (1.0 / np.sqrt(rvec)).astype(dt)
+    Xd = np.asarray(X, dt).reshape(n, -1)
+    Q, _, rank = qr_colpiv(rr[:, None].astype(np.float64) * Xd, dtype=dt)
+    y_proj = rr * np.asarray(y, dt)
+    y_proj = y_proj - Q @ (Q.T @ y_proj)
+    gm = genotype_mean(popcounts(counts), n).astype(dt)
+    Z = counts.T.astype(dt) - gm
+    Z = rr[:, None] * Z
+    Z = Z - Q @ (Q.T @ Z)
+    XtX = Z.T @ Z
+    Xty = Z.T @ y_proj
+    XtX[np.diag_indices(m)] += 1e-4 * np.mean(np.diag(XtX))
+    return np.linalg.solve(XtX, Xty)
+
+
 def n_mc_rule(n: int) -> int:
     """src/option.cpp:381,414 — n_MC = max(min(int(4e9/n/n), 30), 3)."""
     return max(min(int(4e9 / n / n), 30), 3)

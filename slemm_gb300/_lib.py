@@ -75,6 +75,7 @@ _SIGS = {
     "slemm_gpu_lmm_quadforms": (I32, [P, P, F32, F32, I32, I32, P, P, P, P, P, ctypes.POINTER(I32)]),
     "slemm_gpu_gwa_windows": (I32, [P, P, P, P, I64, I32, P, I64, I64, I64, I32, F32, I64, F32, F32, I32,
                                     P, P, P, P]),
+    "slemm_gpu_wls": (I32, [P, P, P, I64, I32, P, P]),
     "slemm_gpu_gebv": (I32, [P, P, P, P]),
     "slemm_gpu_score_terms": (I32, [P, P, I32, P, P]),
     "slemm_gpu_profile": (I32, [P, I32, I32, ctypes.POINTER(I32), P, P, P]),

@@ -278,6 +278,13 @@ class Genotypes:
                                               _ptr(beta), _ptr(se), _ptr(chisq), _ptr(p)))
         return beta, se, chisq, p
 
+    def weighted_least_squares(self, rvec, X, y):
+        """`--wls` SNP effects (src/wls.cpp:4-129), float32 per SNP."""
+        rv, Xf, c, yv, _ = self._reml_args(rvec, X, y, np.ones(self.m, np.float32))
+        b = np.zeros(self.m, np.float32)
+        check(self._lib.slemm_gpu_wls(self.h, _ptr(rv), _ptr(Xf), self.n, c, _ptr(yv), _ptr(b)))
+        return b
+
     def gebv(self, alpha, flip=None):
         """GEBV Σ_j (flip ? 2−count : count)·alpha_j in FP64 (src/pred.cpp:154-172)."""
         a = np.ascontiguousarray(alpha, np.float64)

@@ -231,3 +231,15 @@ def test_gwa_windows_vs_reference_script(gpu):
     assert np.array_equal(ok, np.isfinite(p))
     assert np.allclose(beta[ok], ref["beta"][ok], rtol=1e-3, atol=1e-5)
     assert np.max(np.abs(np.log10(p[ok]) - np.log10(ref["p"][ok]))) <= 2e-3
+
+
+@pytest.mark.parametrize("n,m,tol", [(900, 500, 1e-4), (600, 1100, 2e-2)])
+def test_wls_vs_oracle(gpu, n, m, tol):
+    """--wls (src/wls.cpp:4-129) against the FP64 oracle: ‖b − b_ref‖/‖b_ref‖ ≤ 1e-4 when m < n;
+    when m > n the system is ridge-regularised (1e-4·mean(diag)) and its FP32 Cholesky — the
+    reference's precision — loses digits in proportion to the condition number, bound 2e-2."""
+    counts, rows, y, rvec, X, _ = _problem(n=n, m=m, seed=53)
+    ref = orc.WLS(counts, rvec, X, y)
+    with api.Genotypes(rows, n) as g:
+        b = g.weighted_least_squares(rvec, X, y)
+    assert np.linalg.norm(b - ref) / np.linalg.norm(ref) <= tol
