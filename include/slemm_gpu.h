@@ -55,6 +55,9 @@ extern "C" {
 #define SLEMM_MEM_HOST     0
 #define SLEMM_MEM_DEVICE   1
 
+/* ---- genotype_create flags ---------------------------------------------------------------- */
+#define SLEMM_ROWS_DEVICE  1  /* bed_rows is a device pointer on the current device             */
+
 typedef struct slemm_geno  slemm_geno;   /* packed genotypes resident in HBM + weights         */
 typedef struct slemm_lseed slemm_lseed;  /* Lanczos seed system (basis, Jacobi coefficients)  */
 
@@ -74,7 +77,9 @@ int64_t slemm_gpu_launch_count(void);
  *   (NULL = all n_fam individuals; then n must equal n_fam).
  * Codes follow PLINK: 00→0, 10(het)→1, 11→2, 01(missing)→1 allele-2 copies, exactly like the
  * reference's bit decode (missing counts as one copy).  The handle keeps two packed 2-bit
- * copies (SNP-major and individual-major) in HBM.  flags: reserved, pass 0. */
+ * copies (SNP-major and individual-major) in HBM.  flags: 0, or SLEMM_ROWS_DEVICE when bed_rows
+ * is already in device memory (keep_idx stays a host pointer).  Host rows are read in place over
+ * NVLink-C2C where the device can address pageable memory, else staged. */
 int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
                               int64_t row_stride, const int64_t* keep_idx, int64_t n,
                               int flags, slemm_geno** out);

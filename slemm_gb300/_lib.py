@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libslemm_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "slemm_gpu.h")
 
 OP_QUADFORM, OP_LDET, OP_MATVEC, OP_RMATVEC, OP_WRMATVEC = range(5)
+ROWS_DEVICE = 1
 PREC_FP32, PREC_BF16X2, PREC_BF16X3 = range(3)
 MEM_HOST, MEM_DEVICE = 0, 1
 

@@ -47,12 +47,19 @@ class Genotypes:
 
     def __init__(self, bed_rows, n_fam: int, keep_idx=None):
         self._lib = _lib.load()
-        rows = np.ascontiguousarray(bed_rows, dtype=np.uint8)
+        flags = 0
+        if getattr(bed_rows, "is_cuda", False):   # a CUDA tensor of .bed rows: read in HBM
+            rows = bed_rows.contiguous()
+            ptr = ctypes.c_void_p(rows.data_ptr())
+            flags = _lib.ROWS_DEVICE
+        else:
+            rows = np.ascontiguousarray(bed_rows, dtype=np.uint8)
+            ptr = _ptr(rows)
         m, rb = rows.shape
         keep = None if keep_idx is None else np.ascontiguousarray(keep_idx, dtype=np.int64)
         n = n_fam if keep is None else keep.size
         h = ctypes.c_void_p()
-        check(self._lib.slemm_gpu_genotype_create(_ptr(rows), n_fam, m, rb, _ptr(keep), n, 0,
+        check(self._lib.slemm_gpu_genotype_create(ptr, n_fam, m, rb, _ptr(keep), n, flags,
                                                   ctypes.byref(h)))
         self.h = h
         self.n, self.m = int(n), int(m)

@@ -318,7 +318,8 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
     if (keep_idx)
       for (int64_t i = 0; i < n; ++i)
         CHECK_ARG(keep_idx[i] >= 0 && keep_idx[i] < n_fam, "keep_idx entry out of range");
-    (void)flags;
+    CHECK_ARG((flags & ~SLEMM_ROWS_DEVICE) == 0, "unknown flags");
+    const bool rows_on_device = (flags & SLEMM_ROWS_DEVICE) != 0;
 
     auto* g = new slemm_geno();
     try {
@@ -346,7 +347,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
         int pageable = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, g->device));
         const unsigned gy = (unsigned)ceil_div(g->n_pad, 512);
-        if (pageable) {
+        if (pageable || rows_on_device) {
           const bool al = ((uintptr_t)bed_rows % 4 == 0) && (row_stride % 4 == 0);
           pack_tiles_kernel<<<dim3((unsigned)(g->m_pad / 128), gy), kPackThreads, 0, g->stream>>>(
               bed_rows, row_stride, row_bytes, 0, m, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
@@ -361,7 +362,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
             const int64_t rows = std::max<int64_t>(0, std::min(chunk, m - j0));
             if (rows > 0)
               CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes,
-                                         rows, cudaMemcpyHostToDevice, g->stream));
+                                         rows, cudaMemcpyDefault, g->stream));
             const unsigned gx = (unsigned)(std::min(chunk, g->m_pad - j0) / 128);
             pack_tiles_kernel<<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
                 d_raw.as<uint8_t>(), row_bytes, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al,
@@ -383,7 +384,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
         for (int64_t j0 = 0; j0 < m; j0 += chunk) {
           const int64_t rows = std::min(chunk, m - j0);
           CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
-                                     cudaMemcpyHostToDevice, g->stream));
+                                     cudaMemcpyDefault, g->stream));
           {
             const int64_t total = rows * (Kt_G * 4);
             const int th = 256;

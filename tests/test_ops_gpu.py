@@ -158,3 +158,15 @@ def test_errors_are_status_codes(gpu):
         with pytest.raises(_lib.SlemmError) as e:
             g.set_precision(9)
         assert e.value.code == -1
+
+
+def test_create_from_device_rows(gpu):
+    """SLEMM_ROWS_DEVICE: .bed rows already in HBM build the same tiles as host rows."""
+    import torch
+    rows, _, dec = make_case(1001, 257, seed=61, missing=0.02)
+    v = np.random.default_rng(3).standard_normal((1001, 3)).astype(np.float32)
+    with api.Genotypes(rows, 1001) as g:
+        a = (g.counts()[0], g.rmatvec(v))
+    with api.Genotypes(torch.from_numpy(np.ascontiguousarray(rows)).cuda(), 1001) as g:
+        b = (g.counts()[0], g.rmatvec(v))
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
