@@ -33,21 +33,32 @@
 
 namespace slemm {
 
-constexpr int kPk = 8;                 // packed-tile stages
-constexpr int kS = 3;                  // A (TMEM) + B (smem) stages
-constexpr int kNG = 2;                 // decoder groups
+// Ring depths, a template triple <PK, S, SB>: PK packed slots of kPkg K-tiles each, S A (TMEM)
+// stages and SB B (smem) stages of one K-tile.  B has its own, deeper ring: its tiles come from
+// L2 (every row tile of a split reads the same B) with a latency of ~1500 cycles under load, so
+// they are requested SB stages ahead instead of only as far ahead as the TMEM-bound A ring
+// allows; one decoder warp of each stage waits for its B tile before arriving, so the MMA thread
+// still waits on one barrier per stage.  The K-tiles of a row tile are contiguous in HBM, so one bulk copy
+// moves a whole slot: issuing one 2 KB copy per K-tile paced the kernel at ~750 cycles per
+// K-tile (the copies, not the MMAs, were the bottleneck), four K-tiles per copy take a quarter of
+// that.  Wide blocks use <4, 3, 6> (16 K-tiles in flight); narrow ones (N ≤ 64), whose MMAs are
+// short and whose B tiles are small, use <6, 6, 0>: SB = 0 puts B on the A stages' own full
+// barrier (the B producer's expect_tx), which measured faster there than a separate B ring.
+constexpr int kPkg = 4;                // K-tiles per packed slot
+constexpr int kNG = 3;                 // decoder groups (each keeps one stage in flight)
 constexpr int kMaxThreads = 64 + 2 * 32 + kNG * 2 * 128;   // SUB = 2
 constexpr uint64_t kWaitBudgetNs = 2000000000ull;   // 2 s per wait
 constexpr size_t kSmemBudget = 227 * 1024;
 
+template <int PK, int S, int SB>
 struct TcPlan {
   int N, sub;
   size_t b_off, pk_off, bar_off, total;
   __host__ __device__ TcPlan(int N_, int sub_) : N(N_), sub(sub_)
   {
-    b_off = 0;                                         // kS × N·128 B (1024-aligned, N%8==0)
-    pk_off = b_off + (size_t)kS * N * 128;             // kPk × sub × 2 KB
-    bar_off = pk_off + (size_t)kPk * sub * kTileBytes;
+    b_off = 0;                                         // BS × N·128 B (1024-aligned, N%8==0)
+    pk_off = b_off + (size_t)(SB > 0 ? SB : S) * N * 128;   // PK × sub × kPkg × 2 KB
+    bar_off = pk_off + (size_t)PK * sub * kPkg * kTileBytes;
     total = bar_off + 512 + 1024;                      // barriers/slots + 1024-B base alignment
   }
   __host__ __device__ int mma_warp0() const { return 2; }
@@ -57,12 +68,14 @@ struct TcPlan {
   __host__ __device__ uint32_t acol() const { return (uint32_t)(((sub * N + 31) / 32) * 32); }
 };
 
-// Two tiles when their accumulators and kS A-stages fit the 512 TMEM columns, else one.
-static TcPlan plan_tc(int N)
+// Two tiles when their accumulators and S A-stages fit the 512 TMEM columns, else one.
+template <int PK, int S, int SB>
+static TcPlan<PK, S, SB> plan_tc(int N)
 {
-  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * kS <= 512) return TcPlan(N, 2);
-  return TcPlan(N, 1);
+  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * S <= 512) return TcPlan<PK, S, SB>(N, 2);
+  return TcPlan<PK, S, SB>(N, 1);
 }
+constexpr int kNarrowN = 64;   // N ≤ 64 uses the deep ring
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
 {
@@ -222,6 +235,7 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32
       : "memory");
 }
 
+template <int PK, int S, int SB>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
                float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
@@ -230,14 +244,17 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment of the shared-window address (SWIZZLE_128B tiles need it)
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  const TcPlan P(N, sub);
+  const TcPlan<PK, S, SB> P(N, sub);
   uint8_t* sB = smem + P.b_off;
   uint8_t* sPk = smem + P.pk_off;
   uint64_t* pk_full = (uint64_t*)(smem + P.bar_off);
-  uint64_t* pk_empty = pk_full + kPk;
-  uint64_t* st_full = pk_empty + kPk;
-  uint64_t* st_empty = st_full + kS;
-  uint64_t* accum = st_empty + kS;
+  uint64_t* pk_empty = pk_full + PK;
+  uint64_t* st_full = pk_empty + PK;
+  uint64_t* st_empty = st_full + S;
+  constexpr int BS = SB > 0 ? SB : S;          // B stages (SB = 0: B rides on the A stages)
+  uint64_t* b_full = st_empty + S;
+  uint64_t* b_empty = b_full + BS;
+  uint64_t* accum = b_empty + BS;
   uint32_t* tmem_slot = (uint32_t*)(accum + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
@@ -251,13 +268,17 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   const int nk = max(0, kt1 - kt0);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kPk; ++s) {
+    for (int s = 0; s < PK; ++s) {
       mbar_init(&pk_full[s], 1);
-      mbar_init(&pk_empty[s], dec_warps);
+      mbar_init(&pk_empty[s], dec_warps * kPkg);   // the decoders of each of the slot's K-tiles
     }
-    for (int s = 0; s < kS; ++s) {
-      mbar_init(&st_full[s], dec_warps + 1);   // decoder warps + the B producer's expect_tx
-      mbar_init(&st_empty[s], sub);            // one commit per MMA warp
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&st_full[s], dec_warps + (SB > 0 ? 0 : 1));   // decoder warps (+ B's expect_tx if SB = 0)
+      mbar_init(&st_empty[s], sub);            // one commit per MMA-issuing thread
+    }
+    for (int s = 0; s < (SB > 0 ? SB : 0); ++s) {
+      mbar_init(&b_full[s], 1);                // the B producer's expect_tx
+      mbar_init(&b_empty[s], sub);             // one commit per MMA-issuing thread
     }
     mbar_init(accum, sub);
     *abort_flag = 0;
@@ -280,22 +301,25 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     // ---------------- packed-tile producer (DRAM) ----------------
     if (lane == 0) {
       int issued = 0;
-      for (int i = 0; i < nk; ++i) {
-        const int s = i % kPk;
-        const uint32_t round = (uint32_t)(i / kPk);
-        if (i >= kPk && !mbar_wait(&pk_empty[s], (round - 1) & 1, err, 1, abort_flag, 128)) break;
+      const int nslots = (nk + kPkg - 1) / kPkg;
+      for (int j = 0; j < nslots; ++j) {
+        const int s = j % PK;
+        const uint32_t round = (uint32_t)(j / PK);
+        if (j >= PK && !mbar_wait(&pk_empty[s], (round - 1) & 1, err, 1, abort_flag, 128)) break;
         if (*abort_flag) break;
-        mbar_arrive_expect_tx(&pk_full[s], (uint32_t)(sub * kTileBytes));
-        const int kt = kt0 + i;
-        uint8_t* dst = sPk + (size_t)s * sub * kTileBytes;
+        const int cnt = min(kPkg, nk - j * kPkg);   // K-tiles in this slot
+        const uint32_t bytes = (uint32_t)(cnt * kTileBytes);
+        mbar_arrive_expect_tx(&pk_full[s], (uint32_t)sub * bytes);
+        const int kt = kt0 + j * kPkg;
+        uint8_t* dst = sPk + (size_t)s * sub * kPkg * kTileBytes;
         for (int t = 0; t < sub; ++t)
-          bulk_copy_g2s(dst + t * kTileBytes, A + ((size_t)(mt0 + t) * K_tiles + kt) * kTileBytes, kTileBytes,
+          bulk_copy_g2s(dst + (size_t)t * kPkg * kTileBytes, A + ((size_t)(mt0 + t) * K_tiles + kt) * kTileBytes, bytes,
                         &pk_full[s]);
         ++issued;
       }
       if (*abort_flag)   // let issued copies land before the CTA's shared memory is released
-        for (int i = max(0, issued - kPk); i < issued; ++i)
-          mbar_wait_drain(&pk_full[i % kPk], (uint32_t)(i / kPk) & 1);
+        for (int j = max(0, issued - PK); j < issued; ++j)
+          mbar_wait_drain(&pk_full[j % PK], (uint32_t)(j / PK) & 1);
     }
   } else if (warp == 1) {
     // ---------------- B producer (L2) ----------------
@@ -303,20 +327,25 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       const uint32_t bytes = (uint32_t)N * 128u;
       int issued = 0;
       for (int i = 0; i < nk; ++i) {
-        const int s = i % kS;
-        const uint32_t round = (uint32_t)(i / kS);
-        if (i >= kS && !mbar_wait(&st_empty[s], (round - 1) & 1, err, 16, abort_flag, 128)) break;
+        const int s = i % BS;
+        const uint32_t round = (uint32_t)(i / BS);
+        uint64_t* empty = (SB > 0) ? &b_empty[s] : &st_empty[s];
+        uint64_t* full = (SB > 0) ? &b_full[s] : &st_full[s];
+        if (i >= BS && !mbar_wait(empty, (round - 1) & 1, err, 16, abort_flag, 128)) break;
         if (*abort_flag) break;
-        mbar_arrive_expect_tx(&st_full[s], bytes);
-        tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, &st_full[s]);
+        mbar_arrive_expect_tx(full, bytes);
+        tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, full);
         ++issued;
       }
       if (*abort_flag)
-        for (int i = max(0, issued - kS); i < issued; ++i)
-          mbar_wait_drain(&st_full[i % kS], (uint32_t)(i / kS) & 1);
+        for (int i = max(0, issued - BS); i < issued; ++i)
+          mbar_wait_drain((SB > 0) ? &b_full[i % BS] : &st_full[i % BS], (uint32_t)(i / BS) & 1);
     }
   } else if (warp < P.dec_warp0()) {
     // ---------------- MMA issuer for tile t ----------------
+    // One issuing thread per tile: MMA issue is effectively blocking, and while one thread
+    // waits, fences and commits, the other tile's MMAs keep the tensor pipe fed (one thread for
+    // both tiles, or four column-group issuers, measured slower).
     const int t = warp - P.mma_warp0();
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16(N);
@@ -325,22 +354,24 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       const uint32_t d_tmem = tmem_base + (uint32_t)(t * N);
       const uint32_t a_base = tmem_base + acol + (uint32_t)(t * 32);
       const uint32_t a_step = (uint32_t)(sub * 32);             // columns per A stage
-      int s = 0;
+      int s = 0, sb = 0;
       uint32_t phase = 0;
       for (int i = 0; i < nk; ++i) {
         if (!mbar_wait(&st_full[s], phase, err, 2, abort_flag)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint64_t bd = bdesc0 + (uint64_t)(s * bstep);
+        const uint64_t bd = bdesc0 + (uint64_t)(sb * bstep);
         const uint32_t ad = a_base + (uint32_t)s * a_step;
         mma_bf16_ts(d_tmem, ad, bd, idesc, i > 0 ? 1u : 0u);
         mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
         mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
         mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
         mma_commit(&st_empty[s]);
-        if (++s == kS) {
+        if (SB > 0) mma_commit(&b_empty[sb]);
+        if (++s == S) {
           s = 0;
           phase ^= 1u;
         }
+        if (++sb == BS) sb = 0;
       }
       mma_commit(accum);   // arrives once every MMA this thread issued has completed
     }
@@ -352,10 +383,10 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     const int lq = warp & 3;                 // TMEM lane quarter = row quarter
     const int r = lq * 32 + lane;            // row within the tile
     for (int i = grp; i < nk; i += kNG) {
-      const int sp = i % kPk, s = i % kS;
-      bool got = mbar_wait(&pk_full[sp], (uint32_t)(i / kPk) & 1, err, 4, abort_flag, 64);
+      const int slot = i / kPkg, sp = slot % PK, u = i % kPkg, s = i % S;
+      bool got = mbar_wait(&pk_full[sp], (uint32_t)(slot / PK) & 1, err, 4, abort_flag, 64);
       if (!__all_sync(0xffffffffu, got)) break;   // warp-uniform exit
-      const uint4 pk = *reinterpret_cast<const uint4*>(sPk + ((size_t)sp * sub + tsub) * kTileBytes + r * 16);
+      const uint4 pk = *reinterpret_cast<const uint4*>(sPk + (((size_t)sp * sub + tsub) * kPkg + u) * kTileBytes + r * 16);
       __syncwarp();
       if (lane == 0) mbar_arrive(&pk_empty[sp]);
       uint32_t v[32];
@@ -364,14 +395,18 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       for (int w = 0; w < 4; ++w)
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
-      if (i >= kS) {
-        got = mbar_wait(&st_empty[s], (uint32_t)(i / kS - 1) & 1, err, 64, abort_flag, 64);
+      if (i >= S) {
+        got = mbar_wait(&st_empty[s], (uint32_t)(i / S - 1) & 1, err, 64, abort_flag, 64);
         if (!__all_sync(0xffffffffu, got)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
       tmem_st32(tmem_base + ((uint32_t)(lq * 32) << 16) + acol + (uint32_t)((s * sub + tsub) * 32), v);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      if (SB > 0 && (dw % dec_warps) == 0) {   // this stage's B tile has landed before the stage is full
+        got = mbar_wait(&b_full[i % BS], (uint32_t)(i / BS) & 1, err, 32, abort_flag, 64);
+        if (!__all_sync(0xffffffffu, got)) break;
+      }
       __syncwarp();
       if (lane == 0) mbar_arrive(&st_full[s]);
     }
@@ -427,15 +462,18 @@ static PFN_encodeTiled get_encode()
   return fn;
 }
 
-int gemm_tc_rows_per_cta(int N) { return plan_tc(N).sub * kTileM; }
-
-void gemm_tc(const GemmArgs& a, cudaStream_t st)
+int gemm_tc_rows_per_cta(int N)
 {
-  CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
-  const TcPlan P = plan_tc(a.N);
+  return (N <= kNarrowN ? plan_tc<6, 6, 0>(N).sub : plan_tc<4, 3, 6>(N).sub) * kTileM;
+}
+
+template <int PK, int S, int SB>
+static void launch_tc(const GemmArgs& a, cudaStream_t st)
+{
+  const TcPlan<PK, S, SB> P = plan_tc<PK, S, SB>(a.N);
   CHECK_ARG(a.M_pad % (P.sub * kTileM) == 0 && a.K_pad % 128 == 0, "unpadded operand");
   CHECK_ARG(((uintptr_t)a.A % 16) == 0 && ((uintptr_t)a.B % 16) == 0, "misaligned operand");
-  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * kS <= 512, "no TMEM/shared-memory plan for this N");
+  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * S <= 512, "no TMEM/shared-memory plan for this N");
   const int64_t Mc = a.M_pad / (P.sub * kTileM);
   const int K_tiles = (int)(a.K_pad / kTileK);
   const int tps = (int)ceil_div(K_tiles, a.splits);
@@ -453,15 +491,23 @@ void gemm_tc(const GemmArgs& a, cudaStream_t st)
 
   static bool configured = false;
   if (!configured) {
-    CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+    CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<PK, S, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kSmemBudget));
     configured = true;
   }
   // Each CTA allocates all 512 TMEM columns: request enough shared memory that only one CTA is
   // resident per SM, so no allocation ever has to wait for another CTA's release.
   const size_t smem = std::max<size_t>(P.total, 120 * 1024);
   dim3 grid((unsigned)Mc, (unsigned)a.splits);
-  gemm_tc_kernel<<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub, a.err);
+  gemm_tc_kernel<PK, S, SB><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub, a.err);
   LAUNCH_CHECK();
+}
+
+void gemm_tc(const GemmArgs& a, cudaStream_t st)
+{
+  CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
+  if (a.N <= kNarrowN) launch_tc<6, 6, 0>(a, st);
+  else launch_tc<4, 3, 6>(a, st);
 }
 
 }  // namespace slemm

@@ -464,20 +464,26 @@ int slemm_gpu_genotype_counts(slemm_geno* g, int64_t* popcnt, int32_t* n0, int32
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
-    DevBuf d_pc(g->stream), d_c1(g->stream), d_c2(g->stream);
-    d_pc.ensure(g->m * sizeof(int64_t));
-    d_c1.ensure(g->m * sizeof(int32_t));
-    d_c2.ensure(g->m * sizeof(int32_t));
-    row_counts_device(g, d_pc.as<int64_t>(), d_c1.as<int32_t>(), d_c2.as<int32_t>());
-    std::vector<int64_t> pc(g->m);
-    std::vector<int32_t> c1(g->m), c2(g->m);
-    CUDA_TRY(cudaMemcpyAsync(pc.data(), d_pc.p, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost,
-                             g->stream));
-    CUDA_TRY(cudaMemcpyAsync(c1.data(), d_c1.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                             g->stream));
-    CUDA_TRY(cudaMemcpyAsync(c2.data(), d_c2.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                             g->stream));
-    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    // exact integer counts of the immutable packed copy: computed on first use, then kept
+    if (g->counts_pc.empty()) {
+      DevBuf d_pc(g->stream), d_c1(g->stream), d_c2(g->stream);
+      d_pc.ensure(g->m * sizeof(int64_t));
+      d_c1.ensure(g->m * sizeof(int32_t));
+      d_c2.ensure(g->m * sizeof(int32_t));
+      row_counts_device(g, d_pc.as<int64_t>(), d_c1.as<int32_t>(), d_c2.as<int32_t>());
+      std::vector<int64_t> hpc(g->m);
+      std::vector<int32_t> hc1(g->m), hc2(g->m);
+      CUDA_TRY(cudaMemcpyAsync(hpc.data(), d_pc.p, g->m * sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+      CUDA_TRY(cudaMemcpyAsync(hc1.data(), d_c1.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost, g->stream));
+      CUDA_TRY(cudaMemcpyAsync(hc2.data(), d_c2.p, g->m * sizeof(int32_t), cudaMemcpyDeviceToHost, g->stream));
+      CUDA_TRY(cudaStreamSynchronize(g->stream));
+      g->counts_pc = std::move(hpc);
+      g->counts_c1 = std::move(hc1);
+      g->counts_c2 = std::move(hc2);
+    }
+    const std::vector<int64_t>& pc = g->counts_pc;
+    const std::vector<int32_t>& c1 = g->counts_c1;
+    const std::vector<int32_t>& c2 = g->counts_c2;
     for (int64_t j = 0; j < g->m; ++j) {
       if (popcnt) popcnt[j] = pc[j];
       if (n1) n1[j] = c1[j];

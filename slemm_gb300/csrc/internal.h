@@ -23,6 +23,9 @@ struct slemm_geno {
   slemm::DevBuf ws_B, ws_D, ws_red, ws_small, ws_T, ws_in, ws_out;
   slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
   slemm::HostScal scal;           // mapped host scalars of the Lanczos steps
+  // per-SNP popcount and class counts of the packed copy (immutable): filled on first request
+  std::vector<int64_t> counts_pc;
+  std::vector<int32_t> counts_c1, counts_c2;
   // optional per-launch timing of the packed products (CUDA events on `stream`)
   struct GemmRecord {
     cudaEvent_t start, stop;

@@ -302,10 +302,24 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   const int64_t n = g->n, m = g->m;
   const bool verbose = o.verbose != 0;
   if (verbose) printf("\nStarted stochastic Lanczos DF-REML.\n");
-  Setup S = reml_setup(g, rvec, X, ldx, c, persnp);
   cudaStream_t st = g->stream;
   const int n_V = o.n_V;
   CHECK_ARG(n_V >= 1, "n_V must be >= 1");
+  CHECK_ARG(c >= 1 && c <= 64, "number of covariates must be in [1, 64]");
+  // One block [y_proj | Q | V] (t = 1 + c + n_V) through one Lanczos recurrence: column 0 uses
+  // the projected operator (seed_y, H0_quadform_mv), the rest the plain one (seed_Q and seed_V,
+  // H0_ldet_mv); each of the three groups keeps its own stopping rule, as the reference's three
+  // L_Seed calls do (src/reml.cpp:627-631).
+  const int tQV = 1 + c + n_V;
+  DevBuf d_y(g->stream), d_QV(g->stream), d_X(g->stream), d_tmp(g->stream);
+  d_y.ensure((size_t)n * sizeof(float));
+  d_QV.ensure((size_t)n * tQV * sizeof(float));
+  d_X.ensure((size_t)n * tQV * sizeof(float));
+  d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + 64 * 64 * sizeof(double));
+  // Rademacher probes (src/reml.cpp:597-605), the reference's mt19937 draws generated on the GPU;
+  // launched first so that the host set-up below runs while they are drawn
+  rademacher_device(o.seed, n, n_V, d_QV.as<float>() + (size_t)(1 + c) * n, n, g->stream);
+  Setup S = reml_setup(g, rvec, X, ldx, c, persnp);
   // y_proj = (I − QQᵀ)(rr∘y)   (src/reml.cpp:591-592), FP64 on the host
   std::vector<float> yproj(n);
   {
@@ -320,23 +334,11 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     for (int64_t i = 0; i < n; ++i) yproj[i] = (float)ry[i];
   }
   if (verbose) printf("Projected covariates out of phenotypes.\nGenerating %d Rademacher probing vectors.\n", n_V);
-  // One block [y_proj | Q | V] (t = 1 + c + n_V) through one Lanczos recurrence: column 0 uses
-  // the projected operator (seed_y, H0_quadform_mv), the rest the plain one (seed_Q and seed_V,
-  // H0_ldet_mv); each of the three groups keeps its own stopping rule, as the reference's three
-  // L_Seed calls do (src/reml.cpp:627-631).
-  const int tQV = 1 + c + n_V;
   std::vector<float> QV((size_t)n * (1 + c));
   std::copy(yproj.begin(), yproj.end(), QV.begin());
   for (size_t i = 0; i < (size_t)n * c; ++i) QV[(size_t)n + i] = (float)S.qr.Q[i];
-  DevBuf d_y(g->stream), d_QV(g->stream), d_X(g->stream), d_tmp(g->stream);
-  d_y.ensure((size_t)n * sizeof(float));
-  d_QV.ensure((size_t)n * tQV * sizeof(float));
-  d_X.ensure((size_t)n * tQV * sizeof(float));
-  d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + 64 * 64 * sizeof(double));
   upload(g, d_y.as<float>(), yproj.data(), n);
   upload(g, d_QV.as<float>(), QV.data(), (size_t)n * (1 + c));
-  // Rademacher probes (src/reml.cpp:597-605), the reference's mt19937 draws generated on the GPU
-  rademacher_device(o.seed, n, n_V, d_QV.as<float>() + (size_t)(1 + c) * n, n, g->stream);
   const double t_a = stamp();
   double* d_scal = d_tmp.as<double>();
 

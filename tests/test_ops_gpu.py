@@ -165,8 +165,12 @@ def test_create_from_device_rows(gpu):
     import torch
     rows, _, dec = make_case(1001, 257, seed=61, missing=0.02)
     v = np.random.default_rng(3).standard_normal((1001, 3)).astype(np.float32)
+    gm = orc.genotype_mean(orc.popcounts(dec), 1001)
+    w = np.full(257, 1.0 / 257, np.float32)
     with api.Genotypes(rows, 1001) as g:
+        g.set_weights(gm, w)
         a = (g.counts()[0], g.rmatvec(v))
     with api.Genotypes(torch.from_numpy(np.ascontiguousarray(rows)).cuda(), 1001) as g:
+        g.set_weights(gm, w)
         b = (g.counts()[0], g.rmatvec(v))
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
