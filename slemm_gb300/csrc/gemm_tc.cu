@@ -6,22 +6,28 @@
 // turn their row's 16 packed bytes into 32 BF16 pairs in registers and write them into tensor
 // memory with tcgen05.st; the MMA reads A from TMEM and B from shared memory.
 //
-// What limits tcgen05 here is the issuing thread, not the tensor pipe: measured on GB300, one
-// thread issuing M=128, K=16 BF16 MMAs back to back sustains N/2 cycles per MMA (8192 FLOP/clk
-// per SM), but every instruction between two MMAs delays the next, and an mbarrier wait costs
-// ~250 cycles even when its phase has long completed.  So each tile has its own MMA-issuing warp
-// (one waits while the other issues), each stage has ONE full and ONE empty barrier (decoders and
-// the B copy arrive on the same full barrier; each MMA warp commits once to the empty barrier),
-// and the four MMAs of a stage use descriptors advanced by constants.
+// What limits tcgen05 here is the issuing thread, not the tensor pipe.  Measured on GB300: one
+// thread issuing M=128, N=144, K=16 BF16 MMAs back to back keeps the pipe full (72 cycles per
+// MMA, 8192 FLOP/clk per SM) whether A comes from TMEM or shared memory, but a barrier wait and
+// fence between groups of MMAs leave it idle for ~150 cycles each unless a second thread issues
+// meanwhile, and every instruction of the issuing thread competes for issue slots with the decoder
+// warps on its SM sub-partition (their integer/FMA work, not their TMEM stores, costs ~100 cycles
+// per 576-cycle stage).  So each tile has its own MMA-issuing warp, each stage costs that thread
+// one wait, one fence, four MMAs and ONE commit, and its loop is unrolled over the ring so slots,
+// parities and descriptor offsets are constants.
 //
 // Roles (warp w):
-//   w = 0          packed-tile producer: SUB cp.async.bulk of 2 KB per stage, 8-deep ring;
+//   w = 0          packed-tile producer: per ring slot, one cp.async.bulk of kPkg K-tiles (8 KB)
+//                  per tile;
 //   w = 1          B producer: one TMA tile (N rows × 64 BF16, 128-byte swizzle) per stage;
 //   w = 2 … 1+SUB  MMA issuers, one per tile (w = 2 also allocates TMEM);
-//   w = 2+SUB …    NG groups of 4·SUB decoder warps; group g decodes stages i ≡ g (mod NG).
+//   w = 2+SUB …    kNG groups of 4·SUB decoder warps; group g decodes stages i ≡ g (mod kNG).
 //                  Warp w covers TMEM lanes 32·(w mod 4) …, i.e. those rows of its tile.  Group 0
 //                  also runs the epilogue (tcgen05.ld → FP32 partials).
 //
+// Barriers: pk_full/pk_empty per packed slot; st_full per A stage (the decoder warps, plus the B
+// copy's expect_tx when B rides on the A stages); b_full per B stage; done[i mod BS] per stage,
+// one commit from each MMA thread, which frees both the A stage and the B stage of stage i.
 // TMEM columns: accumulators [0, SUB·N), then S stages of SUB × 32 columns of A (64 BF16 of K per
 // row).  Every mbarrier wait is bounded by a %globaltimer budget; a wait that gives up sets a bit
 // in *err, raises the CTA's abort flag, and the CTA drains what it issued (bounded), frees its
@@ -249,12 +255,12 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   uint8_t* sPk = smem + P.pk_off;
   uint64_t* pk_full = (uint64_t*)(smem + P.bar_off);
   uint64_t* pk_empty = pk_full + PK;
-  uint64_t* st_full = pk_empty + PK;
-  uint64_t* st_empty = st_full + S;
   constexpr int BS = SB > 0 ? SB : S;          // B stages (SB = 0: B rides on the A stages)
-  uint64_t* b_full = st_empty + S;
-  uint64_t* b_empty = b_full + BS;
-  uint64_t* accum = b_empty + BS;
+  static_assert(BS % S == 0, "the stage-done ring serves both rings");
+  uint64_t* st_full = pk_empty + PK;
+  uint64_t* done = st_full + S;                // done[i % BS]: the MMAs of stage i have completed
+  uint64_t* b_full = done + BS;
+  uint64_t* accum = b_full + BS;
   uint32_t* tmem_slot = (uint32_t*)(accum + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
@@ -272,13 +278,11 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       mbar_init(&pk_full[s], 1);
       mbar_init(&pk_empty[s], dec_warps * kPkg);   // the decoders of each of the slot's K-tiles
     }
-    for (int s = 0; s < S; ++s) {
+    for (int s = 0; s < S; ++s)
       mbar_init(&st_full[s], dec_warps + (SB > 0 ? 0 : 1));   // decoder warps (+ B's expect_tx if SB = 0)
-      mbar_init(&st_empty[s], sub);            // one commit per MMA-issuing thread
-    }
-    for (int s = 0; s < (SB > 0 ? SB : 0); ++s) {
-      mbar_init(&b_full[s], 1);                // the B producer's expect_tx
-      mbar_init(&b_empty[s], sub);             // one commit per MMA-issuing thread
+    for (int s = 0; s < BS; ++s) {
+      mbar_init(&done[s], sub);                // one commit per MMA-issuing thread
+      mbar_init(&b_full[s], 1);                // the B producer's expect_tx (unused if SB = 0)
     }
     mbar_init(accum, sub);
     *abort_flag = 0;
@@ -329,9 +333,8 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       for (int i = 0; i < nk; ++i) {
         const int s = i % BS;
         const uint32_t round = (uint32_t)(i / BS);
-        uint64_t* empty = (SB > 0) ? &b_empty[s] : &st_empty[s];
         uint64_t* full = (SB > 0) ? &b_full[s] : &st_full[s];
-        if (i >= BS && !mbar_wait(empty, (round - 1) & 1, err, 16, abort_flag, 128)) break;
+        if (i >= BS && !mbar_wait(&done[s], (round - 1) & 1, err, 16, abort_flag, 128)) break;
         if (*abort_flag) break;
         mbar_arrive_expect_tx(full, bytes);
         tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, full);
@@ -354,24 +357,30 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       const uint32_t d_tmem = tmem_base + (uint32_t)(t * N);
       const uint32_t a_base = tmem_base + acol + (uint32_t)(t * 32);
       const uint32_t a_step = (uint32_t)(sub * 32);             // columns per A stage
-      int s = 0, sb = 0;
-      uint32_t phase = 0;
-      for (int i = 0; i < nk; ++i) {
-        if (!mbar_wait(&st_full[s], phase, err, 2, abort_flag)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint64_t bd = bdesc0 + (uint64_t)(sb * bstep);
-        const uint32_t ad = a_base + (uint32_t)s * a_step;
-        mma_bf16_ts(d_tmem, ad, bd, idesc, i > 0 ? 1u : 0u);
-        mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
-        mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
-        mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
-        mma_commit(&st_empty[s]);
-        if (SB > 0) mma_commit(&b_empty[sb]);
-        if (++s == S) {
-          s = 0;
-          phase ^= 1u;
+      // Unrolled over one turn of the B ring (BS stages, a whole number of A-ring turns), so
+      // ring slots, parities and descriptor offsets are constants: the issuing thread shares
+      // its SM sub-partition with decoder warps, and every instruction it waits to issue
+      // delays the tensor pipe.
+      bool ok = true;
+      for (int i0 = 0; i0 < nk && ok; i0 += BS) {
+        const uint32_t ph0 = (uint32_t)(i0 / S) & 1u;
+#pragma unroll
+        for (int u = 0; u < BS; ++u) {
+          const int i = i0 + u;
+          if (i >= nk) break;
+          if (!mbar_wait(&st_full[u % S], ph0 ^ (uint32_t)((u / S) & 1), err, 2, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint64_t bd = bdesc0 + (uint64_t)(u * bstep);
+          const uint32_t ad = a_base + (uint32_t)(u % S) * a_step;
+          mma_bf16_ts(d_tmem, ad, bd, idesc, i > 0 ? 1u : 0u);
+          mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
+          mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
+          mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
+          mma_commit(&done[u]);   // frees A stage u % S and B stage u once these MMAs complete
         }
-        if (++sb == BS) sb = 0;
       }
       mma_commit(accum);   // arrives once every MMA this thread issued has completed
     }
@@ -396,7 +405,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
 #pragma unroll
         for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
       if (i >= S) {
-        got = mbar_wait(&st_empty[s], (uint32_t)(i / S - 1) & 1, err, 64, abort_flag, 64);
+        got = mbar_wait(&done[(i - S) % BS], (uint32_t)((i - S) / BS) & 1, err, 64, abort_flag, 64);
         if (!__all_sync(0xffffffffu, got)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       }
