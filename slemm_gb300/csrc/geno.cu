@@ -133,10 +133,10 @@ __global__ void pack_GT_kernel(const uint8_t* __restrict__ raw, int64_t row_byte
 
 // ---- tiled pack (no individual subset) -----------------------------------------------------------
 // One CTA turns a block of 128 SNP rows × 128 raw bytes (512 individuals) into the 8 G tiles and
-// 8 GT tiles that cover it: the raw bytes are read row-contiguously (from device memory, or from
-// the caller's host buffer over NVLink-C2C where the device can address pageable memory), the
-// codes become 2-bit counts with four bit operations per 16 calls, and both copies are written
-// tile-contiguously through shared memory.
+// 8 GT tiles that cover it: the raw bytes are read row-contiguously from device memory (the
+// caller's rows, or a staging buffer the host rows were copied into), the codes become 2-bit
+// counts with four bit operations per 16 calls, and both copies are written tile-contiguously
+// through shared memory.
 constexpr int kPackThreads = 256;
 
 // 16 PLINK codes (code e at bits 2e) → 16 counts in the same positions: count = bit0 + bit1
@@ -162,10 +162,13 @@ __device__ __forceinline__ uint32_t unshuffle2(uint32_t x)
 
 // raw row j (global SNP index) is at raw + (j − j0)·row_stride; rows j0 … j0 + rows − 1 are present.
 // blockIdx.x: SNP group (G M-tile, GT K-tiles 2·sg, 2·sg+1); blockIdx.y: 512-individual group.
+// Also adds the block's per-SNP class counts (fields 01 and 10) into c1/c2 ([m_pad] int32 each,
+// zeroed beforehand); integer sums, so the totals do not depend on the order of the blocks.
 __global__ void __launch_bounds__(kPackThreads)
 pack_tiles_kernel(const uint8_t* __restrict__ raw, int64_t row_stride, int64_t row_bytes, int64_t j0,
                   int64_t rows, int64_t m, int64_t n, int64_t Kt_G, int64_t Mt_T, int64_t Kt_T, bool aligned4,
-                  uint32_t* __restrict__ G, uint32_t* __restrict__ GT)
+                  uint32_t* __restrict__ G, uint32_t* __restrict__ GT, int32_t* __restrict__ c1,
+                  int32_t* __restrict__ c2)
 {
   __shared__ uint32_t cnt[128][33];    // [SNP row][16-individual word], natural order
   __shared__ uint32_t outT[512][9];    // [individual][GT word 0 … 7 (2 K-tiles × 4)]
@@ -190,6 +193,17 @@ pack_tiles_kernel(const uint8_t* __restrict__ raw, int64_t row_stride, int64_t r
     cnt[r][q] = counts_of_codes(w) & valid;
   }
   __syncthreads();
+  if (tid < 128 && sg * 128 + tid < m) {   // the row's 512 individuals: count-1 and count-2 fields
+    int ones = 0, twos = 0;
+#pragma unroll 8
+    for (int q = 0; q < 32; ++q) {
+      const uint32_t w = cnt[tid][q];
+      ones += __popc(w & 0x55555555u);
+      twos += __popc(w & 0xAAAAAAAAu);
+    }
+    if (ones) atomicAdd(&c1[sg * 128 + tid], ones);
+    if (twos) atomicAdd(&c2[sg * 128 + tid], twos);
+  }
   // G: tile (sg, 8·ig + t), row r = SNP, words 0 … 3 = local words 4t … 4t+3 of that row
   for (int idx = tid; idx < 8 * 128; idx += kPackThreads) {
     const int t = idx >> 7, r = idx & 127;
@@ -265,13 +279,52 @@ __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int
 }  // namespace slemm
 
 namespace slemm {
+__global__ void counts_from_classes_kernel(const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
+                                           int64_t m, int64_t* __restrict__ pc, int32_t* __restrict__ c1,
+                                           int32_t* __restrict__ c2)
+{
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  pc[j] = (int64_t)n1[j] + 2 * (int64_t)n2[j];
+  c1[j] = n1[j];
+  c2[j] = n2[j];
+}
+
 void row_counts_device(slemm_geno* g, int64_t* pc, int32_t* c1, int32_t* c2)
 {
   const int th = 256;
-  row_counts_kernel<<<(unsigned)ceil_div(g->m * 32, th), th, 0, g->stream>>>(g->G.as<uint32_t>(), g->m,
-                                                                             g->n_pad / kTileK, pc, c1, c2);
+  if (g->dcounts_valid) {   // summed by the pack kernel
+    const int32_t* n1 = g->dcounts.as<int32_t>();
+    counts_from_classes_kernel<<<(unsigned)ceil_div(g->m, th), th, 0, g->stream>>>(n1, n1 + g->m_pad, g->m, pc, c1, c2);
+  } else {
+    row_counts_kernel<<<(unsigned)ceil_div(g->m * 32, th), th, 0, g->stream>>>(g->G.as<uint32_t>(), g->m,
+                                                                               g->n_pad / kTileK, pc, c1, c2);
+  }
   LAUNCH_CHECK();
 }
+
+// Ends the upload pipeline of genotype_create on every path out: waits for the copy stream
+// before the staging buffers (declared earlier, so released later) go back to the pool.
+struct UploadPipe {
+  cudaStream_t cs = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, packed[2] = {nullptr, nullptr}, ready = nullptr;
+  void open()
+  {
+    CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      CUDA_TRY(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
+      CUDA_TRY(cudaEventCreateWithFlags(&packed[b], cudaEventDisableTiming));
+    }
+    CUDA_TRY(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  }
+  ~UploadPipe()
+  {
+    if (cs) cudaStreamSynchronize(cs);
+    for (cudaEvent_t e : {copied[0], copied[1], packed[0], packed[1], ready})
+      if (e) cudaEventDestroy(e);
+    if (cs) cudaStreamDestroy(cs);
+  }
+};
 }  // namespace slemm
 
 using namespace slemm;
@@ -342,35 +395,54 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));
       const int64_t Mt_T = g->n_pad / kTileM;
       if (!keep_idx) {
-        // tiled pack of both copies, padding included; the raw rows are read in place when the
-        // device can address pageable host memory, else through a device staging buffer
-        int pageable = 0;
-        CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, g->device));
+        // tiled pack of both copies, padding included, with the per-SNP class counts on the side
+        g->dcounts.ensure((size_t)2 * g->m_pad * sizeof(int32_t));
+        CUDA_TRY(cudaMemsetAsync(g->dcounts.p, 0, (size_t)2 * g->m_pad * sizeof(int32_t), g->stream));
+        int32_t* d_n1 = g->dcounts.as<int32_t>();
+        int32_t* d_n2 = d_n1 + g->m_pad;
         const unsigned gy = (unsigned)ceil_div(g->n_pad, 512);
-        if (pageable || rows_on_device) {
+        if (rows_on_device) {
           const bool al = ((uintptr_t)bed_rows % 4 == 0) && (row_stride % 4 == 0);
           pack_tiles_kernel<<<dim3((unsigned)(g->m_pad / 128), gy), kPackThreads, 0, g->stream>>>(
               bed_rows, row_stride, row_bytes, 0, m, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
-              g->GT.as<uint32_t>());
+              g->GT.as<uint32_t>(), d_n1, d_n2);
           LAUNCH_CHECK();
         } else {
+          // Host rows: the host link is the bound (≈210 GB/s on GB300's C2C, whether DMA or the
+          // kernel reads host memory itself, and the pack kernel's scattered 128-byte reads got
+          // only ≈155 GB/s).  So DMA chunks of 4096 rows into two staging buffers on a copy
+          // stream while the handle's stream packs the previous chunk from HBM.
           const int64_t chunk = 4096;
-          DevBuf d_raw;
-          d_raw.ensure((size_t)chunk * row_bytes);
+          DevBuf raw0(g->stream), raw1(g->stream);
+          raw0.ensure((size_t)chunk * row_bytes);
+          raw1.ensure((size_t)chunk * row_bytes);
+          uint8_t* raw[2] = {raw0.as<uint8_t>(), raw1.as<uint8_t>()};
+          UploadPipe pipe;   // destroyed before raw0/raw1: the copy stream is drained first
+          pipe.open();
+          CUDA_TRY(cudaEventRecord(pipe.ready, g->stream));   // staging allocations and count zeroing
+          CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.ready, 0));
           const bool al = (row_bytes % 4 == 0);
-          for (int64_t j0 = 0; j0 < g->m_pad; j0 += chunk) {
+          int c = 0;
+          for (int64_t j0 = 0; j0 < g->m_pad; j0 += chunk, ++c) {
+            const int b = c & 1;
             const int64_t rows = std::max<int64_t>(0, std::min(chunk, m - j0));
-            if (rows > 0)
-              CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes,
-                                         rows, cudaMemcpyDefault, g->stream));
+            if (rows > 0) {
+              if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.packed[b], 0));   // buffer b is free
+              CUDA_TRY(cudaMemcpy2DAsync(raw[b], row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
+                                         cudaMemcpyDefault, pipe.cs));
+              CUDA_TRY(cudaEventRecord(pipe.copied[b], pipe.cs));
+              CUDA_TRY(cudaStreamWaitEvent(g->stream, pipe.copied[b], 0));
+            }
             const unsigned gx = (unsigned)(std::min(chunk, g->m_pad - j0) / 128);
             pack_tiles_kernel<<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
-                d_raw.as<uint8_t>(), row_bytes, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al,
-                g->G.as<uint32_t>(), g->GT.as<uint32_t>());
+                raw[b], row_bytes, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
+                g->GT.as<uint32_t>(), d_n1, d_n2);
             LAUNCH_CHECK();
+            CUDA_TRY(cudaEventRecord(pipe.packed[b], g->stream));
           }
-          CUDA_TRY(cudaStreamSynchronize(g->stream));   // d_raw is released on return
+          CUDA_TRY(cudaStreamSynchronize(g->stream));
         }
+        g->dcounts_valid = true;
       } else {
         CUDA_TRY(cudaMemsetAsync(g->G.p, 0, bytes_G, g->stream));
         CUDA_TRY(cudaMemsetAsync(g->GT.p, 0, bytes_GT, g->stream));

@@ -23,7 +23,11 @@ struct slemm_geno {
   slemm::DevBuf ws_B, ws_D, ws_red, ws_small, ws_T, ws_in, ws_out;
   slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
   slemm::HostScal scal;           // mapped host scalars of the Lanczos steps
-  // per-SNP popcount and class counts of the packed copy (immutable): filled on first request
+  // per-SNP class counts n1, n2 in device memory ([2][m_pad] int32), summed by the pack kernel
+  // while it builds the tiles (whole-matrix packs only; `dcounts_valid` says whether they exist)
+  slemm::DevBuf dcounts;
+  bool dcounts_valid = false;
+  // per-SNP popcount and class counts of the packed copy (immutable): host copies on first request
   std::vector<int64_t> counts_pc;
   std::vector<int32_t> counts_c1, counts_c2;
   // optional per-launch timing of the packed products (CUDA events on `stream`)
@@ -45,7 +49,8 @@ struct slemm_geno {
   template <class F>
   void for_each_buf(F&& f)
   {
-    for (slemm::DevBuf* b : {&G, &GT, &gm, &w, &rr, &Q, &ws_B, &ws_D, &ws_red, &ws_small, &ws_T, &ws_in, &ws_out, &err})
+    for (slemm::DevBuf* b : {&G, &GT, &gm, &w, &rr, &Q, &ws_B, &ws_D, &ws_red, &ws_small, &ws_T, &ws_in, &ws_out, &err,
+                             &dcounts})
       f(*b);
   }
   void bind_stream()
