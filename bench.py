@@ -77,7 +77,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def window(self, t0, t1):
+        """Keeps the lines read between host times t0 and t1 (plus one sampling period)."""
+        self.lines = [x for x in self.lines if t0 <= x[0] <= t1 + 0.25]
 
     def __exit__(self, *a):
         if self.proc:
@@ -90,7 +94,7 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -114,7 +118,9 @@ class NvmlSampler:
     BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8 | 0x80, "sw_thermal_slowdown": 0x20,
             "hw_thermal_slowdown": 0x40}
 
-    def __init__(self, cuda_index=0, interval=0.01):
+    def __init__(self, cuda_index=0, interval=None):
+        if interval is None:
+            interval = float(os.environ.get("SLEMM_BENCH_NVML_MS", "10")) / 1000.0
         self.cuda_index, self.interval = cuda_index, interval
         self.samples, self.max_mhz, self.ok = [], 0.0, False
         self._stop = threading.Event()
@@ -141,6 +147,8 @@ class NvmlSampler:
 
     def __enter__(self):
         import ctypes
+        if self.interval <= 0:
+            return self
         try:
             nv = ctypes.CDLL("libnvidia-ml.so.1")
             if nv.nvmlInit_v2() != 0:
@@ -167,7 +175,7 @@ class NvmlSampler:
             if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(clk)) == 0 and \
                     self.reasons_fn(self.h, ctypes.byref(rs)) == 0:
                 p = pw.value / 1000.0 if self.nv.nvmlDeviceGetPowerUsage(self.h, ctypes.byref(pw)) == 0 else None
-                self.samples.append((float(clk.value), int(rs.value), p))
+                self.samples.append((float(clk.value), int(rs.value), p, time.perf_counter()))
             time.sleep(self.interval)
 
     def __exit__(self, *a):
@@ -175,14 +183,19 @@ class NvmlSampler:
         if self.ok:
             self.t.join(timeout=2)
 
+    def window(self, t0, t1):
+        """Keeps the samples taken between host times t0 and t1 (the timed fits): the sampler is
+        started before the warm-up so that NVML's own start-up does not fall into the timed steps."""
+        self.samples = [x for x in self.samples if t0 <= x[3] <= t1]
+
     def summary(self):
         if not self.samples:
             return None
-        reasons = sorted(k for k, b in self.BITS.items() if any(r & b for _, r, _ in self.samples))
-        pw = [p for _, _, p in self.samples if p is not None]
-        return {"sm_mhz": statistics.median(c for c, _, _ in self.samples), "sm_max_mhz": self.max_mhz,
+        reasons = sorted(k for k, b in self.BITS.items() if any(x[1] & b for x in self.samples))
+        pw = [x[2] for x in self.samples if x[2] is not None]
+        return {"sm_mhz": statistics.median(x[0] for x in self.samples), "sm_max_mhz": self.max_mhz,
                 "reasons": reasons, "samples": len(self.samples), "power_w_median": statistics.median(pw) if pw else None,
-                "source": "NVML every 10 ms during the timed fits"}
+                "source": f"NVML every {self.interval * 1e3:.0f} ms during the timed fits"}
 
 
 def make_inputs(cfg, device="cuda"):
@@ -300,6 +313,10 @@ def run_gpu(args, cfg):
     g = api.Genotypes(rows_np, n)
     stream = torch.cuda.ExternalStream(g.stream())
     g.set_precision(_lib.PREC_BF16X2)
+    # clock samplers start before the warm-up (their start-up stays out of the timed steps) and
+    # keep only the samples of the timed window
+    nvml = NvmlSampler(local).__enter__()
+    clocks = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         r = g.SLDF_REML(None, X, y, persnp, **opts)
     # ---- timed: REML + BLUP with genotypes resident ----
@@ -307,16 +324,21 @@ def run_gpu(args, cfg):
     _prof(g, 1)
     times, res = [], None
     barrier()
-    with ClockSampler(local) as clocks, NvmlSampler(local) as nvml:
-        for _ in range(args.steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            res = g.SLDF_REML(None, X, y, persnp, **opts)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
-        barrier()
+    t_timed0 = time.perf_counter()
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = g.SLDF_REML(None, X, y, persnp, **opts)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    barrier()
+    t_timed1 = time.perf_counter()
+    time.sleep(0.25)   # the nvidia-smi line of the last period
+    for smp in (nvml, clocks):
+        smp.__exit__(None, None, None)
+        smp.window(t_timed0, t_timed1)
     launches = api.launch_count() - launches0
     prof = _prof(g, 0)
     mean_step = statistics.mean(times)
@@ -406,6 +428,7 @@ def run_gpu(args, cfg):
         "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
         "lanczos_steps": {"y": res["iters"][0], "Q": res["iters"][1], "V": res["iters"][2]},
         "phases_s": res.get("phases"),
+        "step_ms": [round(t * 1e3, 3) for t in times],
         "matvec_gbs": matvec_gbs,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
