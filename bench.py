@@ -40,6 +40,9 @@ CONFIGS = {
             name="n=2000 m=10000, 1% missing, 30 Rademacher probes, DF-REML + BLUP"),
     2: dict(n=100000, m=50000, probes=64, h2=0.4, missing=0.0,
             name="n=100000 m=50000, 64 Rademacher probes in one block, DF-REML + BLUP"),
+    3: dict(n=500000, m=60000, probes=64, h2=0.3, missing=0.0, ld_rho=0.6, ld_block=50, window=50,
+            name="n=500000 m=60000, block LD (AR(1) latent rho=0.6 in 50-SNP blocks), --iter_weighting "
+                 "with 1,200 windows of 50 SNPs, 64 Rademacher probes, DF-REML + BLUP"),
 }
 
 
@@ -201,7 +204,8 @@ class NvmlSampler:
 def make_inputs(cfg, device="cuda"):
     from slemm_gb300 import synth
     rows, y = synth.simulate_bed_torch(cfg["n"], cfg["m"], seed=1, h2=cfg["h2"], missing=cfg["missing"],
-                                       device=device)
+                                       device=device, ld_rho=cfg.get("ld_rho", 0.0),
+                                       ld_block=cfg.get("ld_block", 50))
     n, m = cfg["n"], cfg["m"]
     X = np.ones((n, 1), np.float32)
     persnp = np.ones(m, np.float32)
@@ -310,6 +314,17 @@ def run_gpu(args, cfg):
         if dist is not None:
             dist.barrier()
 
+    window = cfg.get("window")
+
+    def fit(gh):
+        """One REML + BLUP through the reference-facing calls: DF-REML, or for the windowed
+        workload `--iter_weighting` (MAF from the handle, equal-weight GREML, window weights,
+        weighted GREML)."""
+        if window:
+            maf = gh.marker_qc()[0]
+            return gh.REML_iter_weighting(None, X, y, persnp, maf, lrt=True, window_size=window, **opts)
+        return gh.SLDF_REML(None, X, y, persnp, **opts)
+
     g = api.Genotypes(rows_np, n)
     stream = torch.cuda.ExternalStream(g.stream())
     g.set_precision(_lib.PREC_BF16X2)
@@ -318,7 +333,7 @@ def run_gpu(args, cfg):
     nvml = NvmlSampler(local).__enter__()
     clocks = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
-        r = g.SLDF_REML(None, X, y, persnp, **opts)
+        r = fit(g)
     # ---- timed: REML + BLUP with genotypes resident ----
     launches0 = api.launch_count()
     _prof(g, 1)
@@ -329,7 +344,7 @@ def run_gpu(args, cfg):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        res = g.SLDF_REML(None, X, y, persnp, **opts)
+        res = fit(g)
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
@@ -353,12 +368,12 @@ def run_gpu(args, cfg):
         t0 = time.perf_counter()
         with api.Genotypes(rows_np, n) as g2:
             g2.set_precision(_lib.PREC_BF16X2)
-            r2 = g2.SLDF_REML(None, X, y, persnp, **opts)
+            r2 = fit(g2)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
     e2e = (statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]) if e2e_times else None
     h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes
-    d2h = (n + m + 1 + 1) * 4
+    d2h = (n + m + 1 + 1) * 4 + (4 * m if window else 0)
     # ---- plain FP32 per-vector GPU path (the comparison the metric names), one fit ----
     fp32 = None
     if not args.skip_fp32:
@@ -366,7 +381,7 @@ def run_gpu(args, cfg):
         g.set_per_vector(True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rf = g.SLDF_REML(None, X, y, persnp, **opts)
+        rf = fit(g)
         torch.cuda.synchronize()
         fp32 = {"s": time.perf_counter() - t0, "h2": rf["h2"], "iters": list(rf["iters"])}
         g.set_per_vector(False)
@@ -386,7 +401,7 @@ def run_gpu(args, cfg):
         exe_tf = 2.0 * n * m * dom["N"] / t_launch / 1e12 if dom["tc"] else ach_tf
         gbs = bytes_alg / t_launch / 1e9
         matvec_gbs = packed / t_launch / 1e9
-        traffic = _traffic(dom)
+        traffic = _traffic(dom, n, m)
         tensor = dom["tc"] == 1
         # The packed product runs at the full 2070 MHz SM clock without power capping inside the
         # fits (clocks below), the condition of the measured burst cuBLAS figure; the sustained
@@ -423,6 +438,8 @@ def run_gpu(args, cfg):
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "h2_sim": cfg["h2"],
+                   **({"ld_rho": cfg["ld_rho"], "ld_block": cfg["ld_block"], "window_size": window}
+                      if window else {}),
                    "precision": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars",
                    "l2": "inputs larger than L2 (packed Z 1.25 GB per pass)", "parallelism": "replicas"},
         "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
@@ -466,14 +483,17 @@ def _prof(g, enable):
     return out
 
 
-def _traffic(dom):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+def _traffic(dom, n, m):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary (captured on a
+    small case and scaled to n = 100,000, m = 50,000), rescaled by the packed bytes when the
+    workload has another size (DRAM traffic grows with them: packed matrix once plus partials)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
             t = json.load(f)
         key = f"tc{dom['tc']}_N{dom['N']}_dir{dom['dir']}"
-        return t.get(key)
+        v = t.get(key)
+        return None if v is None else v * (m * ((n + 3) // 4)) / (50000 * 25000)
     except Exception:
         return None
 

@@ -114,15 +114,20 @@ def write_csv(path: str, header, columns):
 
 
 def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal: int = 1000,
-                       missing: float = 0.0, device: str = "cuda", chunk: int = 2048):
+                       missing: float = 0.0, device: str = "cuda", chunk: int = 2048,
+                       ld_rho: float = 0.0, ld_block: int = 50):
     """Device-side generator for benchmark-sized inputs (same model as the NumPy path, torch's
     RNG): returns (.bed rows as a pinned host uint8 tensor m×ceil(n/4), y float32 numpy).
+    With ``ld_rho > 0`` the genotypes of each block of ``ld_block`` SNPs come from an AR(1)
+    latent Gaussian along the SNPs, thresholded at the Binomial(2, p_j) quantiles.
     Torch is used only as a random-number and memory utility here."""
     import torch
+    if ld_rho > 0.0:   # whole LD blocks per chunk, ≈1 GB of latent values at a time
+        chunk = ld_block * max(1, min(chunk, (1 << 28) // max(n, 1)) // ld_block)
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
     nb = (n + 3) // 4
-    rows = torch.empty((m, nb), dtype=torch.uint8, pin_memory=True)
+    rows = torch.empty((m, nb), dtype=torch.uint8, pin_memory=torch.cuda.is_available())
     p = torch.rand(m, generator=gen, device=device, dtype=torch.float64) * 0.45 + 0.05
     code_of = torch.tensor([0b00, 0b10, 0b11], dtype=torch.uint8, device=device)
     causal = torch.randperm(m, generator=gen, device=device)[: min(n_causal, m)]
@@ -134,9 +139,21 @@ def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal:
     for j0 in range(0, m, chunk):
         j1 = min(m, j0 + chunk)
         pj = p[j0:j1, None]
-        u1 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
-        u2 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
-        cnt = (u1 < pj).to(torch.uint8) + (u2 < pj).to(torch.uint8)       # Binomial(2, p)
+        if ld_rho > 0.0:
+            z = torch.empty((j1 - j0, n), device=device, dtype=torch.float32)
+            sd = (1.0 - ld_rho * ld_rho) ** 0.5
+            for r in range(j1 - j0):
+                e = torch.randn(n, generator=gen, device=device, dtype=torch.float32)
+                z[r] = e if (j0 + r) % ld_block == 0 else ld_rho * z[r - 1] + sd * e
+            u = torch.special.ndtr(z)
+            q0 = ((1.0 - pj) ** 2).float()
+            q1 = (q0 + 2.0 * pj * (1.0 - pj)).float()
+            cnt = (u >= q0).to(torch.uint8) + (u >= q1).to(torch.uint8)
+            del z, u
+        else:
+            u1 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
+            u2 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
+            cnt = (u1 < pj).to(torch.uint8) + (u2 < pj).to(torch.uint8)       # Binomial(2, p)
         sel = (causal_sorted >= j0) & (causal_sorted < j1)
         if bool(sel.any()):
             idx = causal_sorted[sel] - j0
