@@ -78,8 +78,9 @@ int64_t slemm_gpu_launch_count(void);
  * Codes follow PLINK: 00→0, 10(het)→1, 11→2, 01(missing)→1 allele-2 copies, exactly like the
  * reference's bit decode (missing counts as one copy).  The handle keeps two packed 2-bit
  * copies (SNP-major and individual-major) in HBM.  flags: 0, or SLEMM_ROWS_DEVICE when bed_rows
- * is already in device memory (keep_idx stays a host pointer).  Host rows are read in place over
- * NVLink-C2C where the device can address pageable memory, else staged. */
+ * is already in device memory (keep_idx stays a host pointer).  Host rows (pinned or pageable)
+ * are copied in 4096-row chunks into device staging buffers while the previous chunk is packed;
+ * the call returns when both copies are built and the host rows are no longer read. */
 int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
                               int64_t row_stride, const int64_t* keep_idx, int64_t n,
                               int flags, slemm_geno** out);
