@@ -447,7 +447,9 @@ def run_gpu(args, cfg):
         "phases_s": res.get("phases"),
         "step_ms": [round(t * 1e3, 3) for t in times],
         "matvec_gbs": matvec_gbs,
-        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step_ms": [round(t * 1e3, 3) for t in e2e_times],
+                "note": "mean of the steps after the first (the first grows the device memory pool)"},
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches / max(args.steps, 1)),
         "roofline": roof,

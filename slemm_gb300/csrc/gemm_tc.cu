@@ -39,31 +39,33 @@
 
 namespace slemm {
 
-// Ring depths, a template triple <PK, S, SB>: PK packed slots of kPkg K-tiles each, S A (TMEM)
-// stages and SB B (smem) stages of one K-tile.  B has its own, deeper ring: its tiles come from
-// L2 (every row tile of a split reads the same B) with a latency of ~1500 cycles under load, so
-// they are requested SB stages ahead instead of only as far ahead as the TMEM-bound A ring
-// allows; one decoder warp of each stage waits for its B tile before arriving, so the MMA thread
-// still waits on one barrier per stage.  The K-tiles of a row tile are contiguous in HBM, so one bulk copy
-// moves a whole slot: issuing one 2 KB copy per K-tile paced the kernel at ~750 cycles per
-// K-tile (the copies, not the MMAs, were the bottleneck), four K-tiles per copy take a quarter of
-// that.  Wide blocks use <4, 3, 6> (16 K-tiles in flight); narrow ones (N ≤ 64), whose MMAs are
-// short and whose B tiles are small, use <6, 6, 0>: SB = 0 puts B on the A stages' own full
-// barrier (the B producer's expect_tx), which measured faster there than a separate B ring.
+// Ring depths, a template quadruple <PK, S, SB, KT>: PK packed slots of kPkg K-tiles each, S A
+// (TMEM) stages and SB B (smem) stages, each stage KT K-tiles of 64.  B has its own, deeper ring:
+// its tiles come from L2 (every row tile of a split reads the same B) with a latency of ~1500
+// cycles under load, so they are requested SB stages ahead instead of only as far ahead as the
+// TMEM-bound A ring allows; one decoder warp of each stage waits for its B tile before arriving,
+// so the MMA thread still waits on one barrier per stage.  The K-tiles of a row tile are
+// contiguous in HBM, so one bulk copy moves a whole slot: one 2 KB copy per K-tile paced the
+// kernel at ~750 cycles per K-tile, four K-tiles per copy take a quarter of that.  Wide blocks
+// (N > 64) use <4, 3, 6, 1>.  Narrow ones, whose MMAs are short, are paced by the issuing thread's
+// fixed cost per stage (wait, fence, commit) rather than by the tensor pipe, so their stages hold
+// two K-tiles (eight MMAs per wait and commit; the small accumulators leave TMEM room for three
+// such stages): <6, 3, 0, 2>, where SB = 0 puts B on the A stages' own full barrier (the B
+// producer's expect_tx), which measured faster for narrow blocks than a separate B ring.
 constexpr int kPkg = 4;                // K-tiles per packed slot
 constexpr int kNG = 3;                 // decoder groups (each keeps one stage in flight)
 constexpr int kMaxThreads = 64 + 2 * 32 + kNG * 2 * 128;   // SUB = 2
 constexpr uint64_t kWaitBudgetNs = 2000000000ull;   // 2 s per wait
 constexpr size_t kSmemBudget = 227 * 1024;
 
-template <int PK, int S, int SB>
+template <int PK, int S, int SB, int KT>
 struct TcPlan {
   int N, sub;
   size_t b_off, pk_off, bar_off, total;
   __host__ __device__ TcPlan(int N_, int sub_) : N(N_), sub(sub_)
   {
-    b_off = 0;                                         // BS × N·128 B (1024-aligned, N%8==0)
-    pk_off = b_off + (size_t)(SB > 0 ? SB : S) * N * 128;   // PK × sub × kPkg × 2 KB
+    b_off = 0;                                         // BS × KT × N·128 B (1024-aligned, N%8==0)
+    pk_off = b_off + (size_t)(SB > 0 ? SB : S) * KT * N * 128;   // PK × sub × kPkg × 2 KB
     bar_off = pk_off + (size_t)PK * sub * kPkg * kTileBytes;
     total = bar_off + 512 + 1024;                      // barriers/slots + 1024-B base alignment
   }
@@ -74,12 +76,12 @@ struct TcPlan {
   __host__ __device__ uint32_t acol() const { return (uint32_t)(((sub * N + 31) / 32) * 32); }
 };
 
-// Two tiles when their accumulators and S A-stages fit the 512 TMEM columns, else one.
-template <int PK, int S, int SB>
-static TcPlan<PK, S, SB> plan_tc(int N)
+// Two tiles when their accumulators and S A-stages of KT K-tiles fit the 512 TMEM columns, else one.
+template <int PK, int S, int SB, int KT>
+static TcPlan<PK, S, SB, KT> plan_tc(int N)
 {
-  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * S <= 512) return TcPlan<PK, S, SB>(N, 2);
-  return TcPlan<PK, S, SB>(N, 1);
+  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * KT * S <= 512) return TcPlan<PK, S, SB, KT>(N, 2);
+  return TcPlan<PK, S, SB, KT>(N, 1);
 }
 constexpr int kNarrowN = 64;   // N ≤ 64 uses the deep ring
 
@@ -241,7 +243,7 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32
       : "memory");
 }
 
-template <int PK, int S, int SB>
+template <int PK, int S, int SB, int KT>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
                float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
@@ -250,13 +252,14 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment of the shared-window address (SWIZZLE_128B tiles need it)
   uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  const TcPlan<PK, S, SB> P(N, sub);
+  const TcPlan<PK, S, SB, KT> P(N, sub);
   uint8_t* sB = smem + P.b_off;
   uint8_t* sPk = smem + P.pk_off;
   uint64_t* pk_full = (uint64_t*)(smem + P.bar_off);
   uint64_t* pk_empty = pk_full + PK;
   constexpr int BS = SB > 0 ? SB : S;          // B stages (SB = 0: B rides on the A stages)
   static_assert(BS % S == 0, "the stage-done ring serves both rings");
+  static_assert(kPkg % KT == 0, "a stage's K-tiles lie in one packed slot");
   uint64_t* st_full = pk_empty + PK;
   uint64_t* done = st_full + S;                // done[i % BS]: the MMAs of stage i have completed
   uint64_t* b_full = done + BS;
@@ -271,12 +274,13 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   const int split = blockIdx.y;
   const int kt0 = split * tiles_per_split;
   const int kt1 = min(K_tiles, kt0 + tiles_per_split);
-  const int nk = max(0, kt1 - kt0);
+  const int nk = max(0, kt1 - kt0);            // K-tiles of this split (a multiple of KT)
+  const int ns = nk / KT;                      // stages
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < PK; ++s) {
       mbar_init(&pk_full[s], 1);
-      mbar_init(&pk_empty[s], dec_warps * kPkg);   // the decoders of each of the slot's K-tiles
+      mbar_init(&pk_empty[s], dec_warps * (kPkg / KT));   // the decoders of each of the slot's stages
     }
     for (int s = 0; s < S; ++s)
       mbar_init(&st_full[s], dec_warps + (SB > 0 ? 0 : 1));   // decoder warps (+ B's expect_tx if SB = 0)
@@ -328,16 +332,17 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   } else if (warp == 1) {
     // ---------------- B producer (L2) ----------------
     if (lane == 0) {
-      const uint32_t bytes = (uint32_t)N * 128u;
+      const uint32_t bytes = (uint32_t)N * 128u;   // one K-tile of B
       int issued = 0;
-      for (int i = 0; i < nk; ++i) {
+      for (int i = 0; i < ns; ++i) {
         const int s = i % BS;
         const uint32_t round = (uint32_t)(i / BS);
         uint64_t* full = (SB > 0) ? &b_full[s] : &st_full[s];
         if (i >= BS && !mbar_wait(&done[s], (round - 1) & 1, err, 16, abort_flag, 128)) break;
         if (*abort_flag) break;
-        mbar_arrive_expect_tx(full, bytes);
-        tma_load_2d(sB + (size_t)s * N * 128, &tmapB, (kt0 + i) * kTileK, 0, full);
+        mbar_arrive_expect_tx(full, (uint32_t)KT * bytes);
+        for (int kk = 0; kk < KT; ++kk)
+          tma_load_2d(sB + ((size_t)s * KT + kk) * N * 128, &tmapB, (kt0 + i * KT + kk) * kTileK, 0, full);
         ++issued;
       }
       if (*abort_flag)
@@ -353,32 +358,35 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16(N);
       const uint64_t bdesc0 = sw128_desc(smem_u32(sB));
-      const uint32_t bstep = (uint32_t)(N * 128) >> 4;          // descriptor units per B stage
+      const uint32_t bstep = (uint32_t)(N * 128) >> 4;          // descriptor units per B K-tile
       const uint32_t d_tmem = tmem_base + (uint32_t)(t * N);
-      const uint32_t a_base = tmem_base + acol + (uint32_t)(t * 32);
-      const uint32_t a_step = (uint32_t)(sub * 32);             // columns per A stage
+      const uint32_t a_base = tmem_base + acol + (uint32_t)(t * 32 * KT);
+      const uint32_t a_step = (uint32_t)(sub * 32 * KT);        // columns per A stage
       // Unrolled over one turn of the B ring (BS stages, a whole number of A-ring turns), so
       // ring slots, parities and descriptor offsets are constants: the issuing thread shares
       // its SM sub-partition with decoder warps, and every instruction it waits to issue
       // delays the tensor pipe.
       bool ok = true;
-      for (int i0 = 0; i0 < nk && ok; i0 += BS) {
+      for (int i0 = 0; i0 < ns && ok; i0 += BS) {
         const uint32_t ph0 = (uint32_t)(i0 / S) & 1u;
 #pragma unroll
         for (int u = 0; u < BS; ++u) {
           const int i = i0 + u;
-          if (i >= nk) break;
+          if (i >= ns) break;
           if (!mbar_wait(&st_full[u % S], ph0 ^ (uint32_t)((u / S) & 1), err, 2, abort_flag)) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint64_t bd = bdesc0 + (uint64_t)(u * bstep);
-          const uint32_t ad = a_base + (uint32_t)(u % S) * a_step;
-          mma_bf16_ts(d_tmem, ad, bd, idesc, i > 0 ? 1u : 0u);
-          mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
-          mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
-          mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
+#pragma unroll
+          for (int kk = 0; kk < KT; ++kk) {
+            const uint64_t bd = bdesc0 + (uint64_t)((u * KT + kk) * bstep);
+            const uint32_t ad = a_base + (uint32_t)(u % S) * a_step + (uint32_t)(kk * 32);
+            mma_bf16_ts(d_tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            mma_bf16_ts(d_tmem, ad + 8, bd + 2, idesc, 1u);
+            mma_bf16_ts(d_tmem, ad + 16, bd + 4, idesc, 1u);
+            mma_bf16_ts(d_tmem, ad + 24, bd + 6, idesc, 1u);
+          }
           mma_commit(&done[u]);   // frees A stage u % S and B stage u once these MMAs complete
         }
       }
@@ -391,25 +399,37 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     const int tsub = (dw % dec_warps) >> 2;  // tile 0 … sub−1
     const int lq = warp & 3;                 // TMEM lane quarter = row quarter
     const int r = lq * 32 + lane;            // row within the tile
-    for (int i = grp; i < nk; i += kNG) {
-      const int slot = i / kPkg, sp = slot % PK, u = i % kPkg, s = i % S;
+    for (int i = grp; i < ns; i += kNG) {
+      const int q0 = i * KT;                   // first K-tile of stage i
+      const int slot = q0 / kPkg, sp = slot % PK, u0 = q0 % kPkg, s = i % S;
       bool got = mbar_wait(&pk_full[sp], (uint32_t)(slot / PK) & 1, err, 4, abort_flag, 64);
       if (!__all_sync(0xffffffffu, got)) break;   // warp-uniform exit
-      const uint4 pk = *reinterpret_cast<const uint4*>(sPk + (((size_t)sp * sub + tsub) * kPkg + u) * kTileBytes + r * 16);
+      uint4 pk[KT];
+#pragma unroll
+      for (int kk = 0; kk < KT; ++kk)
+        pk[kk] = *reinterpret_cast<const uint4*>(sPk + (((size_t)sp * sub + tsub) * kPkg + u0 + kk) * kTileBytes + r * 16);
       __syncwarp();
       if (lane == 0) mbar_arrive(&pk_empty[sp]);
-      uint32_t v[32];
-      const uint32_t words[4] = {pk.x, pk.y, pk.z, pk.w};
+      bool ok = true;
 #pragma unroll
-      for (int w = 0; w < 4; ++w)
+      for (int kk = 0; kk < KT; ++kk) {
+        uint32_t v[32];
+        const uint32_t words[4] = {pk[kk].x, pk[kk].y, pk[kk].z, pk[kk].w};
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
-      if (i >= S) {
-        got = mbar_wait(&done[(i - S) % BS], (uint32_t)((i - S) / BS) & 1, err, 64, abort_flag, 64);
-        if (!__all_sync(0xffffffffu, got)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int w = 0; w < 4; ++w)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
+        if (kk == 0 && i >= S) {   // the stage that last used this A slot has been consumed
+          got = mbar_wait(&done[(i - S) % BS], (uint32_t)((i - S) / BS) & 1, err, 64, abort_flag, 64);
+          if (!__all_sync(0xffffffffu, got)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        tmem_st32(tmem_base + ((uint32_t)(lq * 32) << 16) + acol + (uint32_t)(((s * sub + tsub) * KT + kk) * 32), v);
       }
-      tmem_st32(tmem_base + ((uint32_t)(lq * 32) << 16) + acol + (uint32_t)((s * sub + tsub) * 32), v);
+      if (!ok) break;
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       if (SB > 0 && (dw % dec_warps) == 0) {   // this stage's B tile has landed before the stage is full
@@ -473,19 +493,20 @@ static PFN_encodeTiled get_encode()
 
 int gemm_tc_rows_per_cta(int N)
 {
-  return (N <= kNarrowN ? plan_tc<6, 6, 0>(N).sub : plan_tc<4, 3, 6>(N).sub) * kTileM;
+  return (N <= kNarrowN ? plan_tc<6, 3, 0, 2>(N).sub : plan_tc<4, 3, 6, 1>(N).sub) * kTileM;
 }
 
-template <int PK, int S, int SB>
+template <int PK, int S, int SB, int KT>
 static void launch_tc(const GemmArgs& a, cudaStream_t st)
 {
-  const TcPlan<PK, S, SB> P = plan_tc<PK, S, SB>(a.N);
+  const TcPlan<PK, S, SB, KT> P = plan_tc<PK, S, SB, KT>(a.N);
   CHECK_ARG(a.M_pad % (P.sub * kTileM) == 0 && a.K_pad % 128 == 0, "unpadded operand");
   CHECK_ARG(((uintptr_t)a.A % 16) == 0 && ((uintptr_t)a.B % 16) == 0, "misaligned operand");
-  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * S <= 512, "no TMEM/shared-memory plan for this N");
+  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * S * KT <= 512, "no TMEM/shared-memory plan for this N");
   const int64_t Mc = a.M_pad / (P.sub * kTileM);
   const int K_tiles = (int)(a.K_pad / kTileK);
-  const int tps = (int)ceil_div(K_tiles, a.splits);
+  CHECK_ARG(K_tiles % KT == 0, "K tiles not a multiple of the stage");
+  const int tps = (int)(ceil_div(ceil_div(K_tiles, a.splits), KT) * KT);   // whole stages per split
 
   CUtensorMap map;
   const cuuint64_t dims[2] = {(cuuint64_t)a.K_pad, (cuuint64_t)a.N};
@@ -500,7 +521,7 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
 
   static bool configured = false;
   if (!configured) {
-    CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<PK, S, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<PK, S, SB, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kSmemBudget));
     configured = true;
   }
@@ -508,15 +529,16 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
   // resident per SM, so no allocation ever has to wait for another CTA's release.
   const size_t smem = std::max<size_t>(P.total, 120 * 1024);
   dim3 grid((unsigned)Mc, (unsigned)a.splits);
-  gemm_tc_kernel<PK, S, SB><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub, a.err);
+  gemm_tc_kernel<PK, S, SB, KT><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub,
+                                                                  a.err);
   LAUNCH_CHECK();
 }
 
 void gemm_tc(const GemmArgs& a, cudaStream_t st)
 {
   CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
-  if (a.N <= kNarrowN) launch_tc<6, 6, 0>(a, st);
-  else launch_tc<4, 3, 6>(a, st);
+  if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2>(a, st);
+  else launch_tc<4, 3, 6, 1>(a, st);
 }
 
 }  // namespace slemm
