@@ -413,6 +413,10 @@ def run_gpu(args, cfg):
             "unit": "TFLOP/s" if tensor else "GB/s",
             "frac": (ach_tf / pk["bf16"]) if tensor else gbs / pk["hbm"],
             "frac_of_sustained": ach_tf / pk["bf16_sus"] if tensor else None,
+            # the hi+lo split executes two BF16 products per algorithmic one, so the algorithmic
+            # ceiling of this kernel is half the BF16 peak (TC_peak_eff of the workload's spec)
+            "tc_peak_eff": pk["bf16"] / dom["pieces"] if tensor else None,
+            "frac_eff": ach_tf / (pk["bf16"] / dom["pieces"]) if tensor else None,
             "traffic": traffic,
             "kernel": "gemm_tc_kernel" if tensor else "gemm_simt_kernel",
             "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],

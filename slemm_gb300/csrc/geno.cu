@@ -579,9 +579,20 @@ int slemm_gpu_set_weights(slemm_geno* g, const float* gm, const float* w, const 
       hrr[i] = rr ? rr[i] : 1.0f;
       CHECK_ARG(std::isfinite(hrr[i]), "non-finite rr");
     }
+    // Z_cᵀ1 = Σ_i (x_ij − gm_j) = pc_j − n·gm_j, from the exact integer popcounts
+    std::vector<int64_t> pc(g->m);
+    {
+      const int st = slemm_gpu_genotype_counts(g, pc.data(), nullptr, nullptr, nullptr);
+      if (st != SLEMM_OK) SLEMM_THROW(st, "genotype counts failed");
+    }
+    std::vector<float> hcorr(g->m_pad, 0.f);
+    for (int64_t j = 0; j < g->m; ++j) hcorr[j] = (float)((double)pc[j] - (double)g->n * (double)gm[j]);
     g->gm.ensure(g->m_pad * sizeof(float));
     g->w.ensure(g->m_pad * sizeof(float));
     g->rr.ensure(g->n_pad * sizeof(float));
+    g->gcorr.ensure(g->m_pad * sizeof(float));
+    CUDA_TRY(cudaMemcpyAsync(g->gcorr.p, hcorr.data(), g->m_pad * sizeof(float), cudaMemcpyHostToDevice,
+                             g->stream));
     CUDA_TRY(cudaMemcpyAsync(g->gm.p, hgm.data(), g->m_pad * sizeof(float), cudaMemcpyHostToDevice,
                              g->stream));
     CUDA_TRY(cudaMemcpyAsync(g->w.p, hw.data(), g->m_pad * sizeof(float), cudaMemcpyHostToDevice,

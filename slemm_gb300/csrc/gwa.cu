@@ -213,13 +213,18 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
     ModelCopy mc(g, model);
     slemm_geno* M = &mc.h;
     {
-      std::vector<float> gmm(M->m_pad, 0.f), Qf((size_t)g->n_pad * c, 0.f);
-      for (int64_t k = 0; k < n_model; ++k) gmm[k] = mean[model[k]];
+      std::vector<float> gmm(M->m_pad, 0.f), corr(M->m_pad, 0.f), Qf((size_t)g->n_pad * c, 0.f);
+      for (int64_t k = 0; k < n_model; ++k) {
+        gmm[k] = mean[model[k]];
+        corr[k] = (float)((double)pc[model[k]] - (double)n * (double)gmm[k]);   // Z_cᵀ1 of the copy's rows
+      }
       for (int j = 0; j < c; ++j)
         for (int64_t i = 0; i < n; ++i) Qf[(size_t)j * g->n_pad + i] = (float)Qd[(size_t)j * n + i];
       M->gm.ensure(gmm.size() * sizeof(float));
       M->rr.ensure(rr.size() * sizeof(float));
       M->Q.ensure(Qf.size() * sizeof(float));
+      M->gcorr.ensure(corr.size() * sizeof(float));
+      CUDA_TRY(cudaMemcpyAsync(M->gcorr.p, corr.data(), corr.size() * sizeof(float), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(M->gm.p, gmm.data(), gmm.size() * sizeof(float), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(M->rr.p, rr.data(), rr.size() * sizeof(float), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(M->Q.p, Qf.data(), Qf.size() * sizeof(float), cudaMemcpyHostToDevice, st));

@@ -27,6 +27,10 @@ struct slemm_geno {
   // while it builds the tiles (whole-matrix packs only; `dcounts_valid` says whether they exist)
   slemm::DevBuf dcounts;
   bool dcounts_valid = false;
+  // Z_cᵀ1 per SNP, pc_j − n·gm_j (FP64, stored FP32): the exact product of the centred matrix
+  // with a constant vector, set with the weights; the operators remove each input column's mean
+  // and add it back through this term (see ops.cu)
+  slemm::DevBuf gcorr;
   // per-SNP popcount and class counts of the packed copy (immutable): host copies on first request
   std::vector<int64_t> counts_pc;
   std::vector<int32_t> counts_c1, counts_c2;
@@ -50,7 +54,7 @@ struct slemm_geno {
   void for_each_buf(F&& f)
   {
     for (slemm::DevBuf* b : {&G, &GT, &gm, &w, &rr, &Q, &ws_B, &ws_D, &ws_red, &ws_small, &ws_T, &ws_in, &ws_out, &err,
-                             &dcounts})
+                             &dcounts, &gcorr})
       f(*b);
   }
   void bind_stream()

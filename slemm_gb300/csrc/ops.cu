@@ -5,7 +5,11 @@
 //   Z_c v  = Cnt v − 1·(gmᵀv)           (direction 2, K = SNPs, M = individuals)
 // where Cnt holds the exact integer counts.  The dense side is prepared once per pass by a
 // prologue (projection, rr scaling, FP32 → BF16 pieces) that also sums exactly what the
-// tensor cores multiply, in FP64, for the correction term.  Finalize kernels reduce the split-K
+// tensor cores multiply, in FP64, for the correction term.  Direction 1 first removes each
+// column's mean μ and adds it back exactly: Z_cᵀu = Z_cᵀ(u − μ1) + μ·(pc − n·gm), with pc the
+// integer popcounts.  Without it a column with a large mean (the intercept column of a Lanczos
+// block) leaves Cntᵀu and gm·(1ᵀu) nearly equal and large, and their FP32 accumulation error
+// swamps the true difference: at n = 10⁶ the intercept's Lanczos recurrence never converged.  Finalize kernels reduce the split-K
 // partials and the BF16 pieces, apply the correction and the reference's diagonal scalings,
 // and either write the result or directly build the next pass's dense operand.
 //
@@ -231,23 +235,36 @@ __device__ __forceinline__ void zero_pad_row(void* Bv, int64_t K_pad, int row, i
 // Direction-1 operand (K = individuals): x = in[i,c]; for the first nq columns
 // x −= Σ_l Q[i,l]·QtV[l,c] (QtV from its partials); optionally x *= rr[i]; rows i ≥ n are 0.
 // red[c][blk] = Σ_i stored(x).  Blocks with c ≥ k zero BF16 padding row npieces·k + (c − k).
-template <int V>
+// MEASURE: only red[c][blk] = Σ_i x (the column sums that give the means), nothing stored.
+// Otherwise, with mparts (those sums), x − μ_c is stored, μ_c = (float)(Σ/n) as in column_mean.
+__device__ __forceinline__ float column_mean(const double* __restrict__ mparts, int nblk, int c, double inv_n)
+{
+  return (float)(sum_partials(mparts + (int64_t)c * nblk, nblk) * inv_n);
+}
+
+template <int V, bool MEASURE>
 __global__ void __launch_bounds__(kRedThreads)
 prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64_t n_pad, int k,
                       const float* __restrict__ Q, int64_t ldq, int cq, const double* __restrict__ qparts,
                       int nblkq, int nq, const float* __restrict__ rr, int npieces, void* B,
-                      double* __restrict__ red, int nblk)
+                      double* __restrict__ red, int nblk, const double* __restrict__ mparts)
 {
   __shared__ double sh[32];
   __shared__ double qt[64];
+  __shared__ float smu;
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n_pad, i0 + kRowsPerBlock);
   if (c >= k) {
-    zero_pad_row(B, n_pad, npieces * k + (c - k), i0, i1);
+    if (!MEASURE) zero_pad_row(B, n_pad, npieces * k + (c - k), i0, i1);
     return;
   }
   const bool proj = qparts != nullptr && c < nq;
   if (proj) load_qt(qparts, nblkq, cq, nq, c, qt);
+  if (!MEASURE && mparts != nullptr) {
+    if (threadIdx.x == 0) smu = column_mean(mparts, nblk, c, 1.0 / (double)n);
+    __syncthreads();
+  }
+  const float mu = (!MEASURE && mparts != nullptr) ? smu : 0.f;
   DF acc;
   const float one[V] = {};
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
@@ -268,8 +285,18 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
 #pragma unroll
         for (int u = 0; u < V; ++u) x[u] = __fmul_rn(x[u], r[u]);
       }
+      if (!MEASURE) {
+#pragma unroll
+        for (int u = 0; u < V; ++u)
+          if (i + u < n) x[u] = __fsub_rn(x[u], mu);
+      }
     }
-    store_operand<V, false>(x, npieces, B, n_pad, k, c, i, acc, one);
+    if (MEASURE) {
+#pragma unroll
+      for (int u = 0; u < V; ++u) df_add(acc, x[u]);
+    } else {
+      store_operand<V, false>(x, npieces, B, n_pad, k, c, i, acc, one);
+    }
   }
   const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
@@ -300,10 +327,12 @@ __global__ void __launch_bounds__(kRedThreads)
 finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pad, int pieces, int k,
                     int64_t m, const float* __restrict__ gm, const float* __restrict__ w,
                     const double* __restrict__ cparts, int nblkc, int mode, float* __restrict__ out,
-                    int64_t ldo, int npieces2, void* B2, double* __restrict__ red, int nblk)
+                    int64_t ldo, int npieces2, void* B2, double* __restrict__ red, int nblk,
+                    const double* __restrict__ mparts, const float* __restrict__ gcorr, int64_t n_rows)
 {
   __shared__ double sh[32];
   __shared__ float sb[2];
+  __shared__ float smu;
   const int c = blockIdx.y;
   const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
   if (c >= k) {
@@ -312,10 +341,16 @@ finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pa
   }
   float ch, cl;
   block_scalar([&] { return sum_partials(cparts + (int64_t)c * nblkc, nblkc); }, sb, ch, cl);
+  if (mparts != nullptr) {   // the mean the prologue removed, added back as μ·(pc_j − n·gm_j)
+    if (threadIdx.x == 0) smu = column_mean(mparts, nblkc, c, 1.0 / (double)n_rows);
+    __syncthreads();
+  }
+  const float mu = mparts != nullptr ? smu : 0.f;
   DF acc;
   for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
-    float val[V] = {}, g[V];
+    float val[V] = {}, g[V], e[V] = {};
     ldv<V>(gm + j, g);   // gm is zero-padded to m_pad
+    if (mparts != nullptr) ldv<V>(gcorr + j, e);
     if (j < m) {
       gather_D<V>(D, splits, N, m_pad, pieces, k, c, j, val);
       float ws[V];
@@ -323,6 +358,7 @@ finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pa
 #pragma unroll
       for (int u = 0; u < V; ++u) {
         float v = __fmaf_rn(-g[u], cl, __fmaf_rn(-g[u], ch, val[u]));
+        if (mparts != nullptr) v = __fmaf_rn(mu, e[u], v);
         if (w) v = __fmul_rn(v, ws[u]);
         val[u] = v;
       }
@@ -508,11 +544,12 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   // partials: colsum [k][nblk_n] | tsum [k][nblk_m] | QᵀV [c·nq][nblk_q] | QᵀT [c·nq][nblk_q]
   const int cq = g->c;
   CHECK_ARG(cq <= 64, "more than 64 covariates");
-  const size_t nred = (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q;
+  const size_t nred = 2 * (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q;
   double* r_col = (double*)g->ws_red.ensure(nred * sizeof(double));
   double* r_t = r_col + (size_t)k * nblk_n;
   double* r_qv = r_t + (size_t)k * nblk_m;
   double* r_qt = r_qv + (size_t)std::max(cq, 1) * k * nblk_q;
+  double* r_mu = r_qt + (size_t)std::max(cq, 1) * k * nblk_q;   // column sums for the means [k][nblk_n]
   int* err = g->err.as<int>();
 
   // H0 operators: the first nq columns are projected (H0_quadform_mv), the rest are not (H0_ldet_mv)
@@ -525,14 +562,26 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     if (proj) proj_partials(g, in, ld_in, nq, r_qv, nblk_q);
     dim3 grid(nblk_n, k + pad1);
     const float* rr = h0 ? g->rr.as<float>() : nullptr;
-    if (vin)
-      prologue_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad,
-                                                             cq, proj ? r_qv : nullptr, nblk_q, nq, rr, np1, B1,
-                                                             r_col, nblk_n);
-    else
-      prologue_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, g->Q.as<float>(), g->n_pad,
-                                                             cq, proj ? r_qv : nullptr, nblk_q, nq, rr, np1, B1,
-                                                             r_col, nblk_n);
+    const float* Qp = g->Q.as<float>();
+    const double* qp = proj ? r_qv : nullptr;
+    double* const mu = g->gcorr.p ? r_mu : nullptr;   // mean removal needs Z_cᵀ1 (set with the weights)
+    if (vin) {
+      if (mu) {
+        prologue_indiv_kernel<4, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_mu, nblk_n, nullptr);
+        LAUNCH_CHECK();
+      }
+      prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp,
+                                                                    nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu);
+    } else {
+      if (mu) {
+        prologue_indiv_kernel<1, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_mu, nblk_n, nullptr);
+        LAUNCH_CHECK();
+      }
+      prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp,
+                                                                    nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu);
+    }
     LAUNCH_CHECK();
     // ---- pass 1: Cntᵀ over individuals ----
     run_gemm(g, p1, g->G.as<uint8_t>(), g->m_pad, g->n_pad, B1, D, err, k, 1);
@@ -541,17 +590,17 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     if (h0) {
       finalize_snp_kernel<4><<<dim3(nblk_m, k + pad2), kRedThreads, 0, st>>>(
           D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 1, nullptr, 0,
-          np2, B2, r_t, nblk_m);
+          np2, B2, r_t, nblk_m, mu, g->gcorr.as<float>(), g->n);
       LAUNCH_CHECK();
     } else {
       if (vec4_ok(g->m, ld_out, out))
         finalize_snp_kernel<4><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
             D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
-            0, nullptr, nullptr, 0);
+            0, nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n);
       else
         finalize_snp_kernel<1><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
             D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
-            0, nullptr, nullptr, 0);
+            0, nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n);
       LAUNCH_CHECK();
       return;
     }
@@ -619,25 +668,38 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     const int pad = p.N - pieces * kc;
     void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
     float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.N * rows * sizeof(float));
-    double* r_col = (double*)g->ws_red.ensure((size_t)kc * nblk_n * sizeof(double));
+    double* r_col = (double*)g->ws_red.ensure(2 * (size_t)kc * nblk_n * sizeof(double));
+    double* r_mu = r_col + (size_t)kc * nblk_n;
+    double* const mu = g->gcorr.p ? r_mu : nullptr;
     const float* in = U + (int64_t)c0 * ldu;
-    if (vec4_ok(g->n, ldu, in))
-      prologue_indiv_kernel<4><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n);
-    else
-      prologue_indiv_kernel<1><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n);
+    if (vec4_ok(g->n, ldu, in)) {
+      if (mu) {
+        prologue_indiv_kernel<4, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n, nullptr);
+        LAUNCH_CHECK();
+      }
+      prologue_indiv_kernel<4, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
+          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu);
+    } else {
+      if (mu) {
+        prologue_indiv_kernel<1, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n, nullptr);
+        LAUNCH_CHECK();
+      }
+      prologue_indiv_kernel<1, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
+          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu);
+    }
     LAUNCH_CHECK();
     run_gemm(g, p, A, rows, K_pad, B1, D, g->err.as<int>(), kc, 1);
     float* o = out + (int64_t)c0 * ldo;
     if (vec4_ok(m_valid, ldo, o))
       finalize_snp_kernel<4><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
           D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
-          nullptr, nullptr, 0);
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n);
     else
       finalize_snp_kernel<1><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
           D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
-          nullptr, nullptr, 0);
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n);
     LAUNCH_CHECK();
   }
 }

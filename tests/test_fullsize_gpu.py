@@ -6,6 +6,8 @@ out of reach:
   :10-22, run chunk by chunk on the CPU);
 * the adjoint identity ⟨Z_cᵀu, v⟩ = ⟨u, Z_c v⟩ and linearity of the packed products, both
   precisions;
+* a constant column: Z_cᵀ1 = pc − n·gm exactly (the intercept column of the REML blocks, whose
+  centring cancels almost completely);
 * the metric's own criterion: the mixed-precision batched DF-REML agrees with the plain FP32
   per-vector GPU path to |Δh²| ≤ 1e-4.
 """
@@ -89,3 +91,23 @@ def test_mixed_precision_reml_matches_fp32_per_vector_full_size(full):
     assert abs(mixed["h2"] - plain["h2"]) <= 1e-4, (mixed["h2"], plain["h2"])
     assert abs(mixed["vg"] - plain["vg"]) <= 1e-3 * abs(plain["vg"])
     assert 0.3 < mixed["h2"] < 0.5     # simulated h² = 0.4
+
+
+@pytest.mark.parametrize("prec", [_lib.PREC_BF16X2, _lib.PREC_FP32])
+def test_constant_column_full_size(full, prec):
+    """Z_cᵀ(c·1) = c·(pc − n·gm): the product's centring must not leave the FP32 accumulation
+    error of Cntᵀ1 (≈ 0.55·n per SNP) in a result that is only the rounding of gm."""
+    _, _, g = full
+    gm, w = _weights(g)
+    g.set_weights(gm, w)
+    g.set_precision(prec)
+    pc = g.counts()[0]
+    want = 0.37 * (pc.astype(np.float64) - N * gm.astype(np.float64))
+    got = g.rmatvec(np.full((N, 1), 0.37, np.float32))[:, 0]
+    assert np.max(np.abs(got - want)) <= 1e-5 * 0.37 * N ** 0.5 + 1e-6 * np.max(np.abs(want))
+    # and mixed with a zero-mean part: linear in the constant
+    u = np.random.default_rng(3).standard_normal((N, 1)).astype(np.float32)
+    a = g.rmatvec(u)[:, 0]
+    b = g.rmatvec(u + 0.37)[:, 0]
+    assert np.linalg.norm(b - a - got) <= 4e-5 * np.linalg.norm(a)
+    g.set_precision(_lib.PREC_BF16X2)
