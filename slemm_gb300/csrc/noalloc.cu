@@ -51,17 +51,26 @@ static void* scratch_on_current_device()
   return s_scratch[dev];
 }
 
-// B[c][i] = v[i,c] for i < n, 0 for n ≤ i < n_pad; red[c][blk] = Σ_i B[c][i] (FP64).
+// The column mean the operand has removed: μ_c = (float)(Σ_i v[i,c] / n).
+__device__ __forceinline__ float na_mean(const double* __restrict__ mu_sum, int c, int64_t n)
+{
+  return (float)(mu_sum[c] * (1.0 / (double)n));
+}
+
+// B[c][i] = v[i,c] − μ_c for i < n, 0 for n ≤ i < n_pad; red[c][blk] = Σ_i B[c][i] (FP64).
+// With B == nullptr only the sums of v are taken (μ_c's pass); mu_sum == nullptr: μ_c = 0.
 __global__ void na_prologue_kernel(const float* __restrict__ v, int64_t ldv, int64_t n, int64_t n_pad,
-                                   float* __restrict__ B, double* __restrict__ red, int nblk)
+                                   float* __restrict__ B, double* __restrict__ red, int nblk,
+                                   const double* __restrict__ mu_sum)
 {
   __shared__ double sh[32];
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kNaRows, i1 = min64(n_pad, i0 + kNaRows);
+  const float mu = mu_sum ? na_mean(mu_sum, c, n) : 0.f;
   double acc = 0.0;
   for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const float x = (i < n) ? v[(int64_t)c * ldv + i] : 0.f;
-    B[(int64_t)c * n_pad + i] = x;
+    const float x = (i < n) ? __fsub_rn(v[(int64_t)c * ldv + i], mu) : 0.f;
+    if (B) B[(int64_t)c * n_pad + i] = x;
     acc += (double)x;
   }
   for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -86,9 +95,11 @@ __global__ void na_colsum_kernel(const double* __restrict__ red, int nblk, int k
   if (lane == 0) colsum[c] = s;
 }
 
-// out[j,c] = Σ_s D[s][c][j] − gm_j·colsum_c   (j < m)
+// out[j,c] = Σ_s D[s][c][j] − gm_j·colsum_c + μ_c·(pc_j − n·gm_j)   (j < m): the mean the
+// operand removed comes back exactly through Z_cᵀ1 = pc − n·gm (see ops.cu).
 __global__ void na_finalize_kernel(const float* __restrict__ D, int splits, int k, int64_t m_pad, int64_t m,
                                    const float* __restrict__ gm, const double* __restrict__ colsum,
+                                   const double* __restrict__ mu_sum, const float* __restrict__ gcorr, int64_t n,
                                    float* __restrict__ out, int64_t ldo)
 {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,11 +107,13 @@ __global__ void na_finalize_kernel(const float* __restrict__ D, int splits, int 
   if (j >= m) return;
   float raw = 0.f;
   for (int s = 0; s < splits; ++s) raw += D[((int64_t)s * k + c) * m_pad + j];
-  out[(int64_t)c * ldo + j] = (float)((double)raw - (double)gm[j] * colsum[c]);
+  double val = (double)raw - (double)gm[j] * colsum[c];
+  if (mu_sum) val += (double)na_mean(mu_sum, c, n) * (double)gcorr[j];
+  out[(int64_t)c * ldo + j] = (float)val;
 }
 
 struct NaLayout {
-  size_t b_off, d_off, red_off, cs_off, total;
+  size_t b_off, d_off, red_off, cs_off, mu_off, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -112,7 +125,8 @@ static NaLayout na_layout(int64_t n_pad, int64_t m_pad, int k, int splits, int n
   L.d_off = align256(L.b_off + (size_t)k * n_pad * sizeof(float));
   L.red_off = align256(L.d_off + (size_t)splits * k * m_pad * sizeof(float));
   L.cs_off = align256(L.red_off + (size_t)nblk * k * sizeof(double));
-  L.total = L.cs_off + (size_t)k * sizeof(double);
+  L.mu_off = align256(L.cs_off + (size_t)k * sizeof(double));
+  L.total = L.mu_off + (size_t)k * sizeof(double);
   return L;
 }
 
@@ -143,15 +157,23 @@ extern "C" int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t 
     float* D = reinterpret_cast<float*>(base + L.d_off);
     double* red = reinterpret_cast<double*>(base + L.red_off);
     double* colsum = reinterpret_cast<double*>(base + L.cs_off);
+    const float* gcorr = g->gcorr.as<float>();
+    double* mu_sum = gcorr ? reinterpret_cast<double*>(base + L.mu_off) : nullptr;
     cudaStream_t st = g->stream;
-    na_prologue_kernel<<<dim3(nblk, k), 256, 0, st>>>(v, ldv, g->n, g->n_pad, B, red, nblk);
+    if (mu_sum) {   // column means first: they are removed from the operand and added back exactly
+      na_prologue_kernel<<<dim3(nblk, k), 256, 0, st>>>(v, ldv, g->n, g->n_pad, nullptr, red, nblk, nullptr);
+      LAUNCH_CHECK();
+      na_colsum_kernel<<<(unsigned)ceil_div(k, 8), 256, 0, st>>>(red, nblk, k, mu_sum);
+      LAUNCH_CHECK();
+    }
+    na_prologue_kernel<<<dim3(nblk, k), 256, 0, st>>>(v, ldv, g->n, g->n_pad, B, red, nblk, mu_sum);
     LAUNCH_CHECK();
     na_colsum_kernel<<<(unsigned)ceil_div(k, 8), 256, 0, st>>>(red, nblk, k, colsum);
     LAUNCH_CHECK();
     GemmArgs a{g->G.as<uint8_t>(), g->m_pad, g->n_pad, B, k, D, splits, nullptr};
     gemm_simt(a, st);
     na_finalize_kernel<<<dim3((unsigned)ceil_div(g->m, 256), k), 256, 0, st>>>(
-        D, splits, k, g->m_pad, g->m, g->gm.as<float>(), colsum, out, ldo);
+        D, splits, k, g->m_pad, g->m, g->gm.as<float>(), colsum, mu_sum, gcorr, g->n, out, ldo);
     LAUNCH_CHECK();
   });
 }

@@ -54,6 +54,30 @@ def test_noalloc_matches_allocating_entry_point_twice(gpu):
             assert err <= TOL, (call, err)
 
 
+def test_noalloc_constant_column_is_exact(gpu):
+    """A constant column gives c·(pc − n·gm) (Z_cᵀ1 from the integer popcounts): the mean is
+    removed from the operand and added back exactly, as on the allocating path."""
+    import torch
+    from oracle import slemm_np as orc
+    n, m = 20000, 700
+    counts, _ = synth.simulate_counts(n, m, seed=65)
+    rows = synth.encode_bed(counts, missing=0.01, seed=66)
+    dec = orc.bed_decode(rows, n)
+    pc = orc.popcounts(dec)
+    gm = orc.genotype_mean(pc, n)
+    noalloc = _bind(gpu)
+    with api.Genotypes(rows, n) as g:
+        g.set_weights(gm, np.ones(m, np.float32))
+        stream = torch.cuda.ExternalStream(g.stream())
+        v = torch.full((1, n), 0.37, device="cuda", dtype=torch.float32)
+        out = torch.zeros(1, m, device="cuda", dtype=torch.float32)
+        _lib.check(noalloc(g.h, ctypes.c_void_p(v.data_ptr()), n, 1, ctypes.c_void_p(out.data_ptr()), m))
+        stream.synchronize()
+    want = np.float32(0.37) * (pc.astype(np.float64) - n * gm.astype(np.float64))
+    got = out.cpu().numpy()[0].astype(np.float64)
+    assert np.max(np.abs(got - want)) <= 1e-6 * max(1.0, np.max(np.abs(want)))
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
     import torch
     n, m = 4096, 512
