@@ -141,6 +141,35 @@ __global__ void score_finish_kernel(const double* __restrict__ part, int splits,
   xx[j] = (float)v;
 }
 
+// The same xy, xx from the tensor-core product when every rr is 1 (slemm_gamma's is_one_rr
+// case): out[l·m + j] = Z_hᵀv_l for the columns v = [y | Q_0 … Q_{c−1}] with Z_h centred by the
+// handle's gm_h; Σx·y and Σx·Q_l follow as out + gm_h·Σv, and Σx², the only rr-weighted sums, are
+// the integer counts pc + 2·n2.  Centred by the true mean gm = pc/n in FP64, as the FP64 kernel.
+__global__ void score_finish_tc_kernel(const float* __restrict__ out, int64_t m, int64_t n, int c,
+                                       const float* __restrict__ gmh, const int64_t* __restrict__ pc,
+                                       const int32_t* __restrict__ n2, double sum_y,
+                                       const double* __restrict__ sum_q, int mac, float* __restrict__ xy,
+                                       float* __restrict__ xx)
+{
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const double s_a1 = 2.0 * (double)n - (double)pc[j];
+  if (s_a1 <= mac || 2.0 * (double)n - s_a1 <= mac) {
+    xy[j] = __int_as_float(0x7fc00000);
+    xx[j] = __int_as_float(0x7fc00000);
+    return;
+  }
+  const double gm = (double)pc[j] / (double)n;
+  const double dg = (double)gmh[j] - gm;   // Σx·v − gm·Σv = out + (gm_h − gm)·Σv
+  xy[j] = (float)(-((double)out[j] + dg * sum_y));
+  double v = ((double)pc[j] + 2.0 * (double)n2[j]) - 2.0 * gm * (double)pc[j] + gm * gm * (double)n;
+  for (int l = 0; l < c; ++l) {
+    const double ql = (double)out[(int64_t)(1 + l) * m + j] + dg * sum_q[l];
+    v -= ql * ql;
+  }
+  xx[j] = (float)v;
+}
+
 }  // namespace slemm
 
 using namespace slemm;
@@ -206,6 +235,61 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
     CUDA_TRY(cudaMemcpyAsync(rr.data(), g->rr.p, n_pad * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (c) CUDA_TRY(cudaMemcpyAsync(Q.data(), g->Q.p, (size_t)n_pad * c * sizeof(float), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    bool one_rr = true;
+    for (int64_t i = 0; i < n && one_rr; ++i) one_rr = rr[i] == 1.0f;
+    if (one_rr) {
+      // the packed tensor-core product of [y | Q] (hi+mid+lo BF16 pieces, FP32 accumulation);
+      // the FP64 per-genotype kernel below serves general rr
+      const int k = 1 + c;
+      std::vector<float> V((size_t)k * n);
+      double sum_y = 0.0;
+      std::vector<double> sum_q(std::max(c, 1), 0.0);
+      for (int64_t i = 0; i < n; ++i) {
+        V[i] = y[i];
+        sum_y += (double)y[i];
+      }
+      for (int l = 0; l < c; ++l)
+        for (int64_t i = 0; i < n; ++i) {
+          const float q = Q[(size_t)l * n_pad + i];
+          V[(size_t)(1 + l) * n + i] = q;
+          sum_q[l] += (double)q;
+        }
+      std::vector<int64_t> pc(g->m);
+      std::vector<int32_t> n2(g->m);
+      {
+        const int s2 = slemm_gpu_genotype_counts(g, pc.data(), nullptr, nullptr, n2.data());
+        if (s2 != SLEMM_OK) SLEMM_THROW(s2, "genotype counts failed");
+      }
+      DevBuf dV(st), dO(st), dpc(st), dn2(st), dsq(st), dxy(st), dxx(st);
+      dV.ensure(V.size() * sizeof(float));
+      dO.ensure((size_t)k * g->m * sizeof(float));
+      dpc.ensure(g->m * sizeof(int64_t));
+      dn2.ensure(g->m * sizeof(int32_t));
+      dsq.ensure(sum_q.size() * sizeof(double));
+      dxy.ensure(g->m * sizeof(float));
+      dxx.ensure(g->m * sizeof(float));
+      CUDA_TRY(cudaMemcpyAsync(dV.p, V.data(), V.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(dpc.p, pc.data(), g->m * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(dn2.p, n2.data(), g->m * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(dsq.p, sum_q.data(), sum_q.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+      const int prec = g->prec;
+      g->prec = SLEMM_PREC_BF16X3;
+      try {
+        op_device(g, SLEMM_OP_RMATVEC, 0.f, dV.as<float>(), n, k, dO.as<float>(), g->m);
+      } catch (...) {
+        g->prec = prec;
+        throw;
+      }
+      g->prec = prec;
+      score_finish_tc_kernel<<<(unsigned)ceil_div(g->m, 256), 256, 0, st>>>(
+          dO.as<float>(), g->m, n, c, g->gm.as<float>(), dpc.as<int64_t>(), dn2.as<int32_t>(), sum_y,
+          dsq.as<double>(), mac, dxy.as<float>(), dxx.as<float>());
+      LAUNCH_CHECK();
+      CUDA_TRY(cudaMemcpyAsync(xy, dxy.p, g->m * sizeof(float), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(xx, dxx.p, g->m * sizeof(float), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      return;
+    }
     const int C = 2 + c;
     std::vector<float> B((size_t)C * n_pad, 0.f);
     double sum_y = 0.0, sum_r2 = 0.0;

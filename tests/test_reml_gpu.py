@@ -145,6 +145,26 @@ def test_score_terms_vs_reference_script(gpu):
     assert np.max(np.abs(np.log10(p[ok]) - np.log10(rp[ok]))) <= 1e-3
 
 
+@pytest.mark.parametrize("unit_rr", [True, False])
+def test_score_terms_both_paths_vs_oracle(gpu, unit_rr):
+    """slemm_gamma's per-variant xy, xx (bin/slemm_gamma.py:302-319) through both GPU paths: the
+    tensor-core product when every rr is 1, the FP64 per-genotype kernel otherwise."""
+    counts, rows, _, rvec, X, _ = _problem(n=3001, m=900, seed=71, c=3, rvar=not unit_rr)
+    n, m = counts.shape[1], counts.shape[0]
+    rr = np.ones(n, np.float32) if unit_rr else (1 / np.sqrt(rvec)).astype(np.float32)
+    Q, _, _ = orc.qr_colpiv(rr[:, None] * X)
+    Py = np.random.default_rng(5).standard_normal(n).astype(np.float32)
+    want_xy, want_xx = orc.gamma_terms(counts, Py, rr, Q, 20)
+    with api.Genotypes(rows, n) as g:
+        g.set_weights(np.zeros(m, np.float32), np.zeros(m, np.float32), rr)
+        g.set_projection(Q.astype(np.float32))
+        xy, xx = g.score_terms(Py, mac=20)
+    ok = np.isfinite(want_xy)
+    assert np.array_equal(ok, np.isfinite(xy)) and np.array_equal(ok, np.isfinite(xx))
+    assert np.allclose(xy[ok], want_xy[ok], rtol=1e-4, atol=1e-4 * np.max(np.abs(want_xy[ok])))
+    assert np.allclose(xx[ok], want_xx[ok], rtol=1e-5)
+
+
 @pytest.mark.parametrize("seed,n,n_V", [(0, 37, 3), (1, 1000, 5), (42, 2049, 2), (7, 100003, 1),
                                         (5, 1, 1000), (9, 200, 3000), (11, 79872, 4), (3, 100000, 64)])
 def test_gpu_probes_match_reference_draws(gpu, seed, n, n_V):
