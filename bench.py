@@ -201,6 +201,17 @@ class NvmlSampler:
                 "source": f"NVML every {self.interval * 1e3:.0f} ms during the timed fits"}
 
 
+def max_over_ranks(x, dist=None, device="cuda"):
+    """The largest of the ranks' values (every rank gets it): replicas run side by side, so a
+    step lasts as long as the slowest rank's.  x is None on no rank or on all of them."""
+    if dist is None or x is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_inputs(cfg, device="cuda"):
     from slemm_gb300 import synth
     rows, y = synth.simulate_bed_torch(cfg["n"], cfg["m"], seed=1, h2=cfg["h2"], missing=cfg["missing"],
@@ -356,11 +367,7 @@ def run_gpu(args, cfg):
         smp.window(t_timed0, t_timed1)
     launches = api.launch_count() - launches0
     prof = _prof(g, 0)
-    mean_step = statistics.mean(times)
-    if dist is not None:
-        tt = torch.tensor([mean_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        mean_step = float(tt.item())
+    mean_step = max_over_ranks(statistics.mean(times), dist)
     # ---- e2e: host buffers through the reference-facing calls ----
     e2e_times = []
     for _ in range(0 if args.skip_e2e else max(2, args.steps)):
@@ -372,6 +379,7 @@ def run_gpu(args, cfg):
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
     e2e = (statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]) if e2e_times else None
+    e2e = max_over_ranks(e2e, dist)
     h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes
     d2h = (n + m + 1 + 1) * 4 + (4 * m if window else 0)
     # ---- plain FP32 per-vector GPU path (the comparison the metric names), one fit ----
