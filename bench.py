@@ -15,6 +15,8 @@ One step = one REML + BLUP fit through the C ABI.
            the timed steps;
   cpu_baseline — the NumPy FP32 restatement of the reference operators on this host's cores,
            timed on a bounded sample and extrapolated with the fit's Lanczos step counts.
+  integer_stages — decode, popcounts and class counts: the GPU pack from rows in HBM vs the C
+           restatement on this host's cores (bounded sample, scaled).
 `--impl reference` times the reference's CPU path (the oracle port; the reference itself does
 not build here) on the same workload, on this host's cores.
 """
@@ -249,6 +251,27 @@ def cpu_operator_sample(rows_np, n, m, probes, subsets=4):
     return s_ldet, s_quad, info
 
 
+def cpu_integer_sample(rows_np, n, m, threads, rows_max=4000):
+    """The integer stages (src/input.cpp:343-386 decode, src/reml.cpp:613-621 popcounts,
+    src/input.cpp:10-22 class counts) through the oracle's C restatement, on `rows_max` SNP rows
+    split over `threads` host threads (ctypes releases the GIL), scaled to all m rows."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import slemm_np as orc
+    rows_s = np.ascontiguousarray(rows_np[:min(m, rows_max)])
+    parts = [c for c in np.array_split(np.arange(rows_s.shape[0]), threads) if c.size]
+
+    def work(ix):
+        dec = orc.bed_decode(rows_s[ix[0]:ix[-1] + 1], n)
+        orc.popcounts(dec)
+        orc.hwe_counts(dec)
+
+    with ThreadPoolExecutor(len(parts)) as ex:
+        t0 = time.perf_counter()
+        list(ex.map(work, parts))
+        dt = time.perf_counter() - t0
+    return dt * m / rows_s.shape[0], f"{rows_s.shape[0]} SNP rows × {n} individuals on {len(parts)} threads, scaled ×{m / rows_s.shape[0]:.1f}"
+
+
 def cpu_threads():
     try:
         from threadpoolctl import threadpool_info
@@ -444,6 +467,25 @@ def run_gpu(args, cfg):
         cpu = {"value": est, "unit": "s", "cores": cpu_threads(), "kind": "port",
                "sample": f"{info}; REML time = {max(it_q, it_v)}·t(ldet, {1 + probes} cols) + "
                          f"{it_y}·t(quadform, 1 col) with this fit's Lanczos step counts"}
+    # ---- integer stages (decode, popcounts, class counts): GPU pack from HBM vs the C oracle ----
+    integer = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        rows_dev = torch.from_numpy(rows_np).to("cuda")
+        tg = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with api.Genotypes(rows_dev, n) as g3:
+                g3.counts()
+            torch.cuda.synchronize()
+            tg.append(time.perf_counter() - t0)
+        del rows_dev
+        thr = os.cpu_count() or 1
+        s_int, info_int = cpu_integer_sample(rows_np, n, m, thr)
+        integer = {"gpu_s": min(tg), "cpu_s": s_int, "cores": thr, "kind": "port",
+                   "gpu": "genotype_create from .bed rows already in HBM (both tiled copies and the "
+                          "per-SNP class counts) + counts to the host",
+                   "cpu_sample": info_int}
     line = {
         "metric": METRIC, "value": mean_step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
@@ -466,6 +508,7 @@ def run_gpu(args, cfg):
         "gpu_launches_per_step": int(launches / max(args.steps, 1)),
         "roofline": roof,
         "cpu_baseline": cpu,
+        "integer_stages": integer,
         "clocks": nvml.summary() or clocks.summary(),
         "clocks_nvidia_smi": clocks.summary(),
     }
