@@ -166,6 +166,10 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
     for (int64_t k = 0; k < n_model; ++k)
       CHECK_ARG(model_idx[k] >= 0 && model_idx[k] < m && (k == 0 || model_idx[k] > model_idx[k - 1]),
                 "model SNP indices must be increasing handle indices");
+    // as in the script, the model SNPs and the tested variants are those of one chromosome, so
+    // every block's share of the tested range (below) is a non-empty or empty interval
+    CHECK_ARG(model_idx[0] >= test_begin && model_idx[n_model - 1] <= test_end,
+              "model SNPs must lie inside the tested range (one chromosome)");
     CHECK_ARG(tau > 0.f && std::isfinite(tau), "tau must be positive");
     cudaStream_t st = g->stream;
     // blocks and the tested range each serves (bin/slemm_gwa.py:319-344)
@@ -185,6 +189,8 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
       hi[i] = model_idx[start[i] + bs - ext];
     }
     hi[nb - 1] = test_end + 1;
+    for (int i = 0; i < nb; ++i)
+      CHECK_ARG(test_begin <= lo[i] && lo[i] <= hi[i] && hi[i] <= test_end + 1, "inconsistent block ranges");
     // rr, Q of the covariates (scipy's economic QR in the script; any orthonormal basis gives the
     // same projection)
     std::vector<float> rr(g->n_pad, 0.f);

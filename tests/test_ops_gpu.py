@@ -160,6 +160,21 @@ def test_errors_are_status_codes(gpu):
         assert e.value.code == -1
 
 
+def test_gwa_windows_rejects_model_snps_outside_the_tested_range(gpu):
+    """slemm_gwa's blocks take their share of the tested range from the model SNPs' positions, so
+    model SNPs outside [test_begin, test_end] are an argument error (nothing is launched)."""
+    rows, _, dec = make_case(600, 400, seed=67)
+    y = np.random.default_rng(1).standard_normal(600).astype(np.float32)
+    model = np.arange(0, 400, 4, dtype=np.int64)   # up to SNP 396
+    with api.Genotypes(rows, 600) as g:
+        with pytest.raises(_lib.SlemmError) as e:
+            g.gwa_windows(y, None, np.ones((600, 1), np.float32), model, 0, 199, 40, 1.5, model.size, 1.0, 0.5)
+        assert e.value.code == -1
+        beta, _, _, _ = g.gwa_windows(y, None, np.ones((600, 1), np.float32), model, 0, 399, 40, 1.5, model.size,
+                                      1.0, 0.5)
+        assert beta.shape == (400,)
+
+
 def test_create_from_device_rows(gpu):
     """SLEMM_ROWS_DEVICE: .bed rows already in HBM build the same tiles as host rows."""
     import torch
