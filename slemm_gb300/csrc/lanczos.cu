@@ -571,6 +571,8 @@ int slemm_gpu_lanczos_seed(slemm_geno* g, int op_kind, float tau0, const float* 
     CHECK_ARG(g && B && out, "null argument");
     *out = nullptr;
     CHECK_ARG(ldb >= g->n, "ldb < n");
+    CHECK_ARG(t >= 1 && t <= 4096, "t out of [1, 4096]");
+    CHECK_ARG(mem == SLEMM_MEM_HOST || mem == SLEMM_MEM_DEVICE, "mem must be SLEMM_MEM_HOST or SLEMM_MEM_DEVICE");
     DevBuf dB;
     const float* src = B;
     if (mem == SLEMM_MEM_HOST || ldb != g->n) {
@@ -613,6 +615,7 @@ int slemm_gpu_lanczos_solve(slemm_lseed* s, float sigma, float tol, float* X, in
   return guarded([&] {
     CHECK_ARG(s && X, "null argument");
     CHECK_ARG(ldx >= s->n, "ldx < n");
+    CHECK_ARG(mem == SLEMM_MEM_HOST || mem == SLEMM_MEM_DEVICE, "mem must be SLEMM_MEM_HOST or SLEMM_MEM_DEVICE");
     if (mem == SLEMM_MEM_DEVICE) {
       lanczos_solve_device(s, sigma, tol, X, ldx, 0);
       return;
