@@ -191,6 +191,19 @@ int slemm_gpu_reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t
                        const float* y, const float* persnp, const slemm_reml_opts* opts,
                        float* Py, float* snp_blup, float* blue, slemm_reml_result* res);
 
+/* Gradient of the REML log-likelihood of the DF-REML model at (sigma_g2, sigma_e2) with respect to
+ * the variance components and to per-window SNP weights: Var(y) = sigma_g2·Z_c W Z_cᵀ + sigma_e2·R,
+ * W_j = gw_j·wwin[window[j]] with gw the reference's per-SNP weights (src/reml.cpp:613-622 from
+ * persnp) and window[j] in [-1, n_win) (-1: weight 1, no window).  Traces by Hutchinson with the
+ * reference's n_V normalised Rademacher probes of `seed` (src/reml.cpp:597-605); P·[y | probes]
+ * by one projected Lanczos seed and solve (tolerance tol).  grad[0] = ∂ℓ/∂sigma_g2,
+ * grad[1] = ∂ℓ/∂sigma_e2, grad[2 + k] = ∂ℓ/∂wwin[k].  Host pointers; leaves the handle's weights
+ * set to W. */
+int slemm_gpu_reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c,
+                        const float* y, const float* persnp, const int32_t* window, int n_win,
+                        const float* wwin, double sigma_g2, double sigma_e2, int n_V, int seed,
+                        float tol, double* grad);
+
 /* Iterative window weighting (`--iter_weighting`, src/option.cpp:437-530): equal-weight GREML
  * (DF-REML when lrt and n < 5000, else MC-REML with n_MC samples), per-SNP variance
  * 2·maf(1−maf)·b² normalised to mean 1, fixed-effect SNPs by clumping (largest variance above

@@ -933,3 +933,73 @@ def dense_reml_criterion(counts, gm, gw, rr, Q, y_proj, h2):
     sol = np.linalg.lstsq(Pt + Q @ Q.T, yp, rcond=None)[0]
     return float(yp @ sol), float(np.linalg.slogdet(H)[1]), float(
         np.linalg.slogdet(Q.T @ np.linalg.solve(H, Q))[1])
+
+
+# ------------------------------------------------------------------------------------------
+# REML log-likelihood and its gradient (variance components, per-window SNP weights), FP64
+# ------------------------------------------------------------------------------------------
+def _grad_model(counts, rvec, X, y, persnp, window, wwin):
+    """Dense pieces of Ṽ = σ_g²·Z̃WZ̃ᵀ + σ_e²·I in the rr-transformed space (rr = R^-½ in FP32
+    as the reference, Z̃ = rr∘(Z − gm)), W_j = gw_j·w_{window_j} with gw from
+    src/reml.cpp:613-622 (FP32) and weight 1 outside every window."""
+    m, n = counts.shape
+    pc = popcounts(counts)
+    gm = genotype_mean(pc, n)
+    gw = snp_weights(gm, np.asarray(persnp, np.float32)).astype(np.float64)
+    ww = np.ones(m)
+    if window is not None:
+        window = np.asarray(window)
+        sel = window >= 0
+        ww[sel] = np.asarray(wwin, np.float64)[window[sel]]
+    rr = np.ones(n) if rvec is None else (np.float32(1) / np.sqrt(np.asarray(rvec, np.float32))).astype(np.float64)
+    Zt = rr[:, None] * (counts.T.astype(np.float64) - gm.astype(np.float64)[None, :])
+    Xt = rr[:, None] * np.asarray(X, np.float64)
+    yt = rr * np.asarray(y, np.float64)
+    return Zt, Xt, yt, gw, ww
+
+
+def _reml_P(Zt, Xt, W, sg2, se2):
+    n = Zt.shape[0]
+    V = sg2 * (Zt * W[None, :]) @ Zt.T + se2 * np.eye(n)
+    Vi = np.linalg.inv(V)
+    ViX = Vi @ Xt
+    XVX = Xt.T @ ViX
+    P = Vi - ViX @ np.linalg.solve(XVX, ViX.T)
+    return V, XVX, P
+
+
+def reml_loglik_dense(counts, rvec, X, y, persnp, window, wwin, sg2, se2):
+    """ℓ = −½[log|Ṽ| + log|X̃ᵀṼ⁻¹X̃| + ỹᵀP̃ỹ] (the constant dropped), exact FP64 for small n."""
+    Zt, Xt, yt, gw, ww = _grad_model(counts, rvec, X, y, persnp, window, wwin)
+    V, XVX, P = _reml_P(Zt, Xt, gw * ww, sg2, se2)
+    return -0.5 * (np.linalg.slogdet(V)[1] + np.linalg.slogdet(XVX)[1] + yt @ P @ yt)
+
+
+def reml_grad_dense(counts, rvec, X, y, persnp, window, wwin, sg2, se2, probes=None):
+    """∂ℓ/∂θ = −½[tr(P̃·∂Ṽ/∂θ) − ỹᵀP̃(∂Ṽ/∂θ)P̃ỹ] for θ = σ_g², σ_e², w_1 … w_K.  Traces exact, or by
+    Hutchinson with the given normalised probes (n×n_V): tr(A) ≈ (n/n_V)·Σ_v vᵀAv.  Returns
+    (d_sigma_g2, d_sigma_e2, d_w)."""
+    Zt, Xt, yt, gw, ww = _grad_model(counts, rvec, X, y, persnp, window, wwin)
+    n, m = Zt.shape
+    W = gw * ww
+    _, _, P = _reml_P(Zt, Xt, W, sg2, se2)
+    py = P @ yt
+    a = (Zt.T @ py) ** 2                               # (z̃_jᵀP̃ỹ)²
+    if probes is None:
+        b = np.einsum("ij,ij->j", Zt, P @ Zt)          # z̃_jᵀP̃z̃_j
+        trP = np.trace(P)
+    else:
+        Vp = np.asarray(probes, np.float64)
+        s = n / Vp.shape[1]
+        b = s * np.einsum("jv,jv->j", Zt.T @ (P @ Vp), Zt.T @ Vp)
+        trP = s * np.einsum("iv,iv->", Vp, P @ Vp)
+    d_sg = -0.5 * (W @ b - W @ a)
+    d_se = -0.5 * (trP - py @ py)
+    K = 0 if wwin is None else len(wwin)
+    d_w = np.zeros(K)
+    if K:
+        window = np.asarray(window)
+        for k in range(K):
+            sel = window == k
+            d_w[k] = -0.5 * sg2 * (gw[sel] @ (b[sel] - a[sel]))
+    return d_sg, d_se, d_w

@@ -70,6 +70,8 @@ _SIGS = {
                                   ctypes.POINTER(RemlResult)]),
     "slemm_gpu_reml_lmc": (I32, [P, P, P, I64, I32, P, P, ctypes.POINTER(RemlOpts), P, P, P,
                                  ctypes.POINTER(RemlResult)]),
+    "slemm_gpu_reml_grad": (I32, [P, P, P, I64, I32, P, P, P, I32, P, ctypes.c_double, ctypes.c_double, I32, I32,
+                                  ctypes.c_float, P]),
     "slemm_gpu_reml_iter_weighting": (I32, [P, P, P, I64, I32, P, P, P, ctypes.POINTER(RemlOpts),
                                             ctypes.POINTER(WindowOpts), P, P, P, P, P, P,
                                             ctypes.POINTER(I32), ctypes.POINTER(RemlResult)]),

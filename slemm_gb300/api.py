@@ -224,6 +224,18 @@ class Genotypes:
                     n_criterion=r.n_criterion, seconds=r.seconds,
                     phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
+    def REML_grad(self, rvec, X, y, persnp, window, wwin, sigma_g2, sigma_e2, n_V=30, seed=0, tol=1e-6):
+        """Gradient of the REML log-likelihood with respect to (σ_g², σ_e², per-window SNP
+        weights): dict with d_sigma_g2, d_sigma_e2 and d_w (one per window)."""
+        rv, Xf, c, yv, ps = self._reml_args(rvec, X, y, persnp)
+        win = None if window is None else np.ascontiguousarray(window, np.int32)
+        ww = np.ascontiguousarray(np.zeros(0) if wwin is None else wwin, np.float32)
+        grad = np.zeros(2 + ww.size, np.float64)
+        check(self._lib.slemm_gpu_reml_grad(self.h, _ptr(rv), _ptr(Xf), self.n, c, _ptr(yv), _ptr(ps), _ptr(win),
+                                            int(ww.size), _ptr(ww), float(sigma_g2), float(sigma_e2), int(n_V),
+                                            int(seed), float(tol), _ptr(grad)))
+        return dict(d_sigma_g2=grad[0], d_sigma_e2=grad[1], d_w=grad[2:])
+
     def REML_iter_weighting(self, rvec, X, y, persnp, maf, lrt=True, seed=0, n_V=30, n_MC=0,
                             n_MC_final=0, tol_L=5e-4, s2max=0.7, window_size=20, sig_chisq=1e6,
                             indep_r2=0.5, max_fixed=64, verbose=False):

@@ -708,6 +708,119 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
 
 using namespace slemm;
 
+// ================================================================================================
+// REML log-likelihood gradient
+// ================================================================================================
+// In the rr-transformed space (ỹ = rr∘y, X̃ = rr∘X, Z̃ = rr∘Z_c) the model of the DF-REML path is
+//   Ṽ = σ_g²·Z̃WZ̃ᵀ + σ_e²·I,   W_j = gw_j·w_{window_j},
+// gw the reference's per-SNP weights (src/reml.cpp:613-622) and w one weight per window of SNPs
+// (1 outside every window).  ℓ = −½[log|Ṽ| + log|X̃ᵀṼ⁻¹X̃| + ỹᵀP̃ỹ] has
+//   ∂ℓ/∂θ = −½[tr(P̃·∂Ṽ/∂θ) − ỹᵀP̃(∂Ṽ/∂θ)P̃ỹ].
+// With H = Z̃WZ̃ᵀ + τI (τ = σ_e²/σ_g²), P̃ = P_H/σ_g² where P_H = (I−QQᵀ)H̃⁺(I−QQᵀ) is the projected
+// solve of the DF-REML path (H0_quadform_mv at shift τ).  Traces take the reference's normalised
+// Rademacher probes v (tr(A) ≈ (n/n_V)·Σ_v vᵀAv, src/reml.cpp:597-605); per SNP
+//   a_j = (z̃_jᵀP_Hỹ)²,   b_j = (n/n_V)·Σ_v (z̃_jᵀP_Hv)(z̃_jᵀv),
+// and
+//   ∂ℓ/∂σ_g² = −½[Σ_j W_j·b_j/σ_g² − Σ_j W_j·a_j/σ_g⁴]
+//   ∂ℓ/∂σ_e² = −½[tr(P_H)/σ_g² − ‖P_Hỹ‖²/σ_g⁴],   tr(P_H) ≈ (n/n_V)·Σ_v vᵀP_Hv
+//   ∂ℓ/∂w_k  = −½·Σ_{j ∈ window k} gw_j·[b_j − a_j/σ_g²].
+// The per-SNP terms of every window come from one packed product Z̃ᵀ[P_Hỹ | P_HV | V] (hi+mid+lo
+// pieces), the transposed product the operators use, reduced per window on the host in FP64.
+void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+               const float* persnp, const int32_t* window, int n_win, const float* wwin, double sg2,
+               double se2, int n_V, int seed, float tol, double* grad)
+{
+  const int64_t n = g->n, m = g->m;
+  cudaStream_t st = g->stream;
+  const int t = 1 + n_V, k = 1 + 2 * n_V;
+  DevBuf d_B(st), d_X(st), d_U(st), d_T(st), d_s(st);
+  d_B.ensure((size_t)n * t * sizeof(float));
+  // probes straight into the block, drawn while the host set-up runs
+  rademacher_device(seed, n, n_V, d_B.as<float>() + n, n, st);
+  Setup S = reml_setup(g, rvec, X, ldx, c, persnp);
+  std::vector<float> W(m);
+  for (int64_t j = 0; j < m; ++j) W[j] = S.gw[j] * ((window && window[j] >= 0) ? wwin[window[j]] : 1.0f);
+  {
+    const int s2 = slemm_gpu_set_weights(g, S.gm.data(), W.data(), S.rr.data());
+    if (s2 != SLEMM_OK) SLEMM_THROW(s2, "set_weights failed");
+  }
+  // ỹ_proj = (I − QQᵀ)(rr∘y) on the host in FP64, as the DF-REML path
+  std::vector<float> yproj(n);
+  {
+    std::vector<double> ry(n);
+    for (int64_t i = 0; i < n; ++i) ry[i] = (double)(S.rr[i] * y[i]);
+    for (int l = 0; l < c; ++l) {
+      const double* q = S.qr.Q.data() + (size_t)l * n;
+      double sum = 0.0;
+      for (int64_t i = 0; i < n; ++i) sum += q[i] * ry[i];
+      for (int64_t i = 0; i < n; ++i) ry[i] -= sum * q[i];
+    }
+    for (int64_t i = 0; i < n; ++i) yproj[i] = (float)ry[i];
+  }
+  upload(g, d_B.as<float>(), yproj.data(), n);
+  // U's last n_V columns keep the raw probes; the block's get projected
+  d_U.ensure((size_t)n * k * sizeof(float));
+  CUDA_TRY(cudaMemcpyAsync(d_U.as<float>() + (size_t)(1 + n_V) * n, d_B.as<float>() + n, (size_t)n * n_V * sizeof(float),
+                           cudaMemcpyDeviceToDevice, st));
+  double* d_scal = (double*)d_s.ensure((size_t)64 * t * sizeof(double) + 2 * (size_t)t * sizeof(double));
+  proj_coeffs(g, d_B.as<float>() + n, n, n_V, d_scal);
+  proj_apply(g, d_B.as<float>() + n, n, n_V, d_scal);
+  // P_H[ỹ | V] by one projected Lanczos seed at shift τ, solved at σ = 0 (groups ỹ, probes)
+  const float tau = (float)(se2 / sg2);
+  slemm_lseed* sd = lanczos_seed_device(g, SLEMM_OP_QUADFORM, tau, d_B.as<float>(), t, tol, 600, false, {1, n_V}, 5, t);
+  std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold(sd, lseed_free);
+  d_X.ensure((size_t)n * t * sizeof(float));
+  lanczos_solve_device(sd, 0.0, 1e-6, d_X.as<float>(), n, 0);
+  lanczos_solve_device(sd, 0.0, 1e-6, d_X.as<float>() + n, n, 1);
+  proj_coeffs(g, d_X.as<float>(), n, t, d_scal);
+  proj_apply(g, d_X.as<float>(), n, t, d_scal);
+  // tr(P_H) ≈ (n/n_V)·Σ_v vᵀP_Hv and ‖P_Hỹ‖²
+  double* d_dots = d_scal + (size_t)64 * t;
+  col_dots(g, d_U.as<float>() + (size_t)(1 + n_V) * n, n, d_X.as<float>() + n, n, n, n_V, d_dots);
+  col_dots(g, d_X.as<float>(), n, nullptr, 0, n, 1, d_dots + n_V);
+  const std::vector<double> dots = d2h(g, d_dots, (size_t)n_V + 1);
+  double vPv = 0.0;
+  for (int v = 0; v < n_V; ++v) vPv += dots[v];
+  const double trP = vPv * (double)n / (double)n_V, pyy = dots[n_V];
+  // Z̃ᵀ[P_Hỹ | P_HV | V]: rr∘ on the rows, then the transposed packed product
+  CUDA_TRY(cudaMemcpyAsync(d_U.as<float>(), d_X.as<float>(), (size_t)n * t * sizeof(float), cudaMemcpyDeviceToDevice,
+                           st));
+  scale_rows(g, d_U.as<float>(), n, n, k, g->rr.as<float>());
+  d_T.ensure((size_t)m * k * sizeof(float));
+  const int prec = g->prec;
+  g->prec = SLEMM_PREC_BF16X3;
+  try {
+    op_device(g, SLEMM_OP_RMATVEC, 0.f, d_U.as<float>(), n, k, d_T.as<float>(), m);
+  } catch (...) {
+    g->prec = prec;
+    throw;
+  }
+  g->prec = prec;
+  std::vector<float> T((size_t)m * k);
+  CUDA_TRY(cudaMemcpyAsync(T.data(), d_T.p, T.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  check_device_error(g);
+  double sa = 0.0, sb = 0.0;
+  std::vector<double> ga(std::max(n_win, 1), 0.0), gb(std::max(n_win, 1), 0.0);
+  const double scale = (double)n / (double)n_V;
+  for (int64_t j = 0; j < m; ++j) {
+    const double ty = T[j];
+    const double a = ty * ty;
+    double b = 0.0;
+    for (int v = 0; v < n_V; ++v) b += (double)T[(size_t)(1 + v) * m + j] * (double)T[(size_t)(1 + n_V + v) * m + j];
+    b *= scale;
+    sa += (double)W[j] * a;
+    sb += (double)W[j] * b;
+    if (window && window[j] >= 0) {
+      ga[window[j]] += (double)S.gw[j] * a;
+      gb[window[j]] += (double)S.gw[j] * b;
+    }
+  }
+  grad[0] = -0.5 * (sb / sg2 - sa / (sg2 * sg2));
+  grad[1] = -0.5 * (trP / sg2 - pyy / (sg2 * sg2));
+  for (int q = 0; q < n_win; ++q) grad[2 + q] = -0.5 * (gb[q] - ga[q] / sg2);
+}
+
 extern "C" {
 
 int slemm_gpu_reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
@@ -731,6 +844,25 @@ int slemm_gpu_reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t
     CHECK_ARG(ldx >= g->n, "ldx < n");
     CHECK_ARG(opts->s2max > 0 && opts->s2max < 1, "bad h2 bound");
     reml_lmc(g, rvec, X, ldx, c, y, persnp, *opts, Py, snp_blup, blue, res);
+  });
+}
+
+int slemm_gpu_reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
+                        const float* persnp, const int32_t* window, int n_win, const float* wwin, double sigma_g2,
+                        double sigma_e2, int n_V, int seed, float tol, double* grad)
+{
+  return guarded([&] {
+    CHECK_ARG(g && X && y && persnp && grad, "null argument");
+    CHECK_ARG(ldx >= g->n && c >= 1 && c <= 64, "bad covariate matrix");
+    CHECK_ARG(n_win >= 0 && (n_win == 0 || (window && wwin)), "windows given without their weights");
+    CHECK_ARG(sigma_g2 > 0.0 && sigma_e2 > 0.0 && std::isfinite(sigma_g2) && std::isfinite(sigma_e2),
+              "variance components must be positive");
+    CHECK_ARG(n_V >= 1 && n_V <= 256, "n_V out of [1, 256]");
+    CHECK_ARG(tol > 0.f, "tol must be positive");
+    for (int q = 0; q < n_win; ++q) CHECK_ARG(wwin[q] > 0.f && std::isfinite(wwin[q]), "window weights must be > 0");
+    if (window)
+      for (int64_t j = 0; j < g->m; ++j) CHECK_ARG(window[j] >= -1 && window[j] < n_win, "window index out of range");
+    reml_grad(g, rvec, X, ldx, c, y, persnp, window, n_win, wwin, sigma_g2, sigma_e2, n_V, seed, tol, grad);
   });
 }
 

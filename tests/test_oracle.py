@@ -255,3 +255,47 @@ def test_window_weights_sliding_rule():
             seg = sv[i - ws // 2: i - ws // 2 + ws + 1]
         x = seg.mean()
         assert math.isclose(w[i], 0.001 / (0.001 + 0.999 * math.exp(-0.5 * x)), rel_tol=1e-5)
+
+
+def _grad_problem(n=300, m=240, seed=9):
+    counts, _ = synth.simulate_counts(n, m, seed=seed)
+    y, _, _ = synth.simulate_phenotype(counts, 0.5, n_causal=50, seed=seed)
+    rng = np.random.default_rng(seed)
+    X = np.column_stack([np.ones(n), rng.standard_normal(n)])
+    rvec = rng.uniform(0.8, 1.3, n)
+    persnp = rng.uniform(0.5, 1.5, m)
+    window = np.repeat(np.arange(6), m // 6)
+    window[:10] = -1
+    wwin = rng.uniform(0.5, 2.0, 6)
+    return counts, rvec, X, y, persnp, window, wwin
+
+
+def test_reml_gradient_matches_central_finite_differences():
+    """The FP64 gradient formulas (variance components and per-window weights) against central
+    differences of the exact REML log-likelihood, step 1e-4."""
+    counts, rvec, X, y, persnp, window, wwin = _grad_problem()
+    sg2, se2, h = 0.6, 0.9, 1e-4
+    d_sg, d_se, d_w = orc.reml_grad_dense(counts, rvec, X, y, persnp, window, wwin, sg2, se2)
+
+    def f(sg=sg2, se=se2, w=wwin):
+        return orc.reml_loglik_dense(counts, rvec, X, y, persnp, window, w, sg, se)
+
+    assert abs(d_sg - (f(sg=sg2 + h) - f(sg=sg2 - h)) / (2 * h)) <= 1e-6 * abs(d_sg)
+    assert abs(d_se - (f(se=se2 + h) - f(se=se2 - h)) / (2 * h)) <= 1e-6 * abs(d_se)
+    for k in range(len(wwin)):
+        wp, wm = wwin.copy(), wwin.copy()
+        wp[k] += h
+        wm[k] -= h
+        assert abs(d_w[k] - (f(w=wp) - f(w=wm)) / (2 * h)) <= 1e-6 * np.max(np.abs(d_w))
+
+
+def test_reml_gradient_hutchinson_estimate_converges():
+    """With the reference's Rademacher probes the trace estimate approaches the exact gradient
+    (4000 probes: within 3 %)."""
+    counts, rvec, X, y, persnp, window, wwin = _grad_problem()
+    exact = orc.reml_grad_dense(counts, rvec, X, y, persnp, window, wwin, 0.6, 0.9)
+    est = orc.reml_grad_dense(counts, rvec, X, y, persnp, window, wwin, 0.6, 0.9,
+                              probes=orc.rademacher(0, counts.shape[1], 4000))
+    assert abs(est[0] - exact[0]) <= 0.03 * abs(exact[0])
+    assert abs(est[1] - exact[1]) <= 0.03 * abs(exact[1])
+    assert np.max(np.abs(est[2] - exact[2])) <= 0.03 * np.max(np.abs(exact[2]))

@@ -145,6 +145,24 @@ def test_score_terms_vs_reference_script(gpu):
     assert np.max(np.abs(np.log10(p[ok]) - np.log10(rp[ok]))) <= 1e-3
 
 
+def test_reml_gradient_vs_oracle(gpu):
+    """Gradient of the REML log-likelihood (σ_g², σ_e², 8 window weights) against the FP64 oracle
+    with the same 30 Rademacher probes: the Hutchinson estimate is deterministic given them."""
+    counts, rows, y, rvec, X, persnp = _problem(n=1500, m=1200, seed=73)
+    n, m = counts.shape[1], counts.shape[0]
+    window = np.repeat(np.arange(8), m // 8).astype(np.int32)
+    window[:30] = -1
+    wwin = np.random.default_rng(4).uniform(0.5, 2.0, 8).astype(np.float32)
+    sg2, se2, n_V, seed = 0.55, 0.8, 30, 3
+    ref = orc.reml_grad_dense(counts, rvec, X, y, persnp, window, wwin, sg2, se2,
+                              probes=orc.rademacher(seed, n, n_V))
+    with api.Genotypes(rows, n) as g:
+        r = g.REML_grad(rvec, X, y, persnp, window, wwin, sg2, se2, n_V=n_V, seed=seed, tol=1e-6)
+    assert abs(r["d_sigma_g2"] - ref[0]) <= 2e-3 * abs(ref[0])
+    assert abs(r["d_sigma_e2"] - ref[1]) <= 2e-3 * abs(ref[1])
+    assert np.max(np.abs(r["d_w"] - ref[2])) <= 2e-3 * np.max(np.abs(ref[2]))
+
+
 @pytest.mark.parametrize("unit_rr", [True, False])
 def test_score_terms_both_paths_vs_oracle(gpu, unit_rr):
     """slemm_gamma's per-variant xy, xx (bin/slemm_gamma.py:302-319) through both GPU paths: the
