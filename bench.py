@@ -45,6 +45,9 @@ CONFIGS = {
     3: dict(n=500000, m=60000, probes=64, h2=0.3, missing=0.0, ld_rho=0.6, ld_block=50, window=50,
             name="n=500000 m=60000, block LD (AR(1) latent rho=0.6 in 50-SNP blocks), --iter_weighting "
                  "with 1,200 windows of 50 SNPs, 64 Rademacher probes, DF-REML + BLUP"),
+    4: dict(n=200000, m=100000, probes=64, h2=0.4, missing=0.0, grad_windows=2000, sigma_g2=0.4, sigma_e2=0.6,
+            name="n=200000 m=100000, REML log-likelihood gradient for (sigma_g2, sigma_e2) and 2,000 per-window "
+                 "SNP weights in (0, 2] (windows of 50 SNPs), 64 Rademacher probes"),
 }
 
 
@@ -418,46 +421,7 @@ def run_gpu(args, cfg):
         g.set_per_vector(False)
         g.set_precision(_lib.PREC_BF16X2)
     # ---- roofline of the dominant packed-product launch shape ----
-    pk = peaks()
-    dom = max(prof, key=lambda r: r["ms"]) if prof else None
-    roof = None
-    matvec_gbs = None
-    if dom:
-        k = dom["k"]
-        t_launch = dom["ms"] / dom["launches"] / 1e3
-        packed = m * ((n + 3) // 4)
-        bytes_alg = packed + 4 * n * k + 4 * m * k
-        flops_alg = 2.0 * n * m * k
-        ach_tf = flops_alg / t_launch / 1e12
-        exe_tf = 2.0 * n * m * dom["N"] / t_launch / 1e12 if dom["tc"] else ach_tf
-        gbs = bytes_alg / t_launch / 1e9
-        matvec_gbs = packed / t_launch / 1e9
-        traffic = _traffic(dom, n, m)
-        tensor = dom["tc"] == 1
-        # The packed product runs at the full 2070 MHz SM clock without power capping inside the
-        # fits (clocks below), the condition of the measured burst cuBLAS figure; the sustained
-        # figure was taken at ~1450 MHz under the power cap and is reported beside it.
-        roof = {
-            "bound": "tensor" if tensor else "hbm",
-            "achieved": ach_tf if tensor else gbs,
-            "peak": pk["bf16"] if tensor else pk["hbm"],
-            "unit": "TFLOP/s" if tensor else "GB/s",
-            "frac": (ach_tf / pk["bf16"]) if tensor else gbs / pk["hbm"],
-            "frac_of_sustained": ach_tf / pk["bf16_sus"] if tensor else None,
-            # the hi+lo split executes two BF16 products per algorithmic one, so the algorithmic
-            # ceiling of this kernel is half the BF16 peak (TC_peak_eff of the workload's spec)
-            "tc_peak_eff": pk["bf16"] / dom["pieces"] if tensor else None,
-            "frac_eff": ach_tf / (pk["bf16"] / dom["pieces"]) if tensor else None,
-            "traffic": traffic,
-            "kernel": "gemm_tc_kernel" if tensor else "gemm_simt_kernel",
-            "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],
-                       "direction": "Z^T U (M=SNPs)" if dom["dir"] == 1 else "Z V (M=individuals)",
-                       "avg_ms": t_launch * 1e3, "launches": dom["launches"]},
-            "executed_tflops": exe_tf, "frac_executed": exe_tf / pk["bf16"],
-            "algorithmic_gbs": gbs, "frac_hbm": gbs / pk["hbm"],
-            "peak_source": "measured burst cuBLAS BF16 (MEASURED_PEAKS.json)" if pk["src"] == "measured" else "fallback",
-            "shapes": prof,
-        }
+    roof, matvec_gbs = roofline(prof, n, m)
     # ---- CPU baseline (oracle port), rank 0, N = 1 only ----
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
@@ -516,6 +480,192 @@ def run_gpu(args, cfg):
         line["fp32_per_vector"] = fp32
         line["speedup_vs_fp32_per_vector"] = fp32["s"] / mean_step
         line["dh2_vs_fp32"] = abs(fp32["h2"] - res["h2"])
+    g.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def roofline(prof, n, m):
+    """Roofline object of the dominant packed-product launch shape (most device time in the
+    timed region) and the packed bytes per second it streamed."""
+    pk = peaks()
+    dom = max(prof, key=lambda r: r["ms"]) if prof else None
+    if not dom:
+        return None, None
+    k = dom["k"]
+    t_launch = dom["ms"] / dom["launches"] / 1e3
+    packed = m * ((n + 3) // 4)
+    bytes_alg = packed + 4 * n * k + 4 * m * k
+    flops_alg = 2.0 * n * m * k
+    ach_tf = flops_alg / t_launch / 1e12
+    exe_tf = 2.0 * n * m * dom["N"] / t_launch / 1e12 if dom["tc"] else ach_tf
+    gbs = bytes_alg / t_launch / 1e9
+    tensor = dom["tc"] == 1
+    # The packed product runs at the full 2070 MHz SM clock without power capping inside the
+    # fits, the condition of the measured burst cuBLAS figure; the sustained figure was taken at
+    # ~1450 MHz under the power cap and is reported beside it.
+    roof = {
+        "bound": "tensor" if tensor else "hbm",
+        "achieved": ach_tf if tensor else gbs,
+        "peak": pk["bf16"] if tensor else pk["hbm"],
+        "unit": "TFLOP/s" if tensor else "GB/s",
+        "frac": (ach_tf / pk["bf16"]) if tensor else gbs / pk["hbm"],
+        "frac_of_sustained": ach_tf / pk["bf16_sus"] if tensor else None,
+        # a split into P BF16 pieces executes P products per algorithmic one, so the algorithmic
+        # ceiling of this kernel is the BF16 peak over P (TC_peak_eff of the workload's spec)
+        "tc_peak_eff": pk["bf16"] / dom["pieces"] if tensor else None,
+        "frac_eff": ach_tf / (pk["bf16"] / dom["pieces"]) if tensor else None,
+        "traffic": _traffic(dom, n, m),
+        "kernel": "gemm_tc_kernel" if tensor else "gemm_simt_kernel",
+        "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],
+                   "direction": "Z^T U (M=SNPs)" if dom["dir"] == 1 else "Z V (M=individuals)",
+                   "avg_ms": t_launch * 1e3, "launches": dom["launches"]},
+        "executed_tflops": exe_tf, "frac_executed": exe_tf / pk["bf16"],
+        "algorithmic_gbs": gbs, "frac_hbm": gbs / pk["hbm"],
+        "peak_source": "measured burst cuBLAS BF16 (MEASURED_PEAKS.json)" if pk["src"] == "measured" else "fallback",
+        "shapes": prof,
+    }
+    return roof, packed / t_launch / 1e9
+
+
+def grad_inputs(cfg):
+    """Window index per SNP (consecutive windows of m / K SNPs) and K weights in (0, 2]."""
+    m, K = cfg["m"], cfg["grad_windows"]
+    window = np.minimum(np.arange(m) // (m // K), K - 1).astype(np.int32)
+    wwin = (2.0 - np.random.default_rng(7).uniform(0.0, 2.0, K)).astype(np.float32)
+    return window, wwin
+
+
+def run_grad(args, cfg):
+    """Gradient workload: one step = ∂ℓ/∂(σ_g², σ_e², w_1..w_K) of the REML log-likelihood through
+    the reference-facing call (projected Lanczos seed/solve of [ỹ | probes], one packed product
+    Z̃ᵀ[P_Hỹ | P_HV | V], per-window reductions)."""
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from slemm_gb300 import api, _lib
+    api.init(local)
+    n, m, probes = cfg["n"], cfg["m"], cfg["probes"]
+    rows, y, X, persnp = make_inputs(cfg)
+    rows_np = rows.numpy()
+    window, wwin = grad_inputs(cfg)
+    sg2, se2 = cfg["sigma_g2"], cfg["sigma_e2"]
+
+    def step(gh):
+        return gh.REML_grad(None, X, y, persnp, window, wwin, sg2, se2, n_V=probes, seed=0, tol=1e-6)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    g = api.Genotypes(rows_np, n)
+    stream = torch.cuda.ExternalStream(g.stream())
+    g.set_precision(_lib.PREC_BF16X2)
+    nvml = NvmlSampler(local).__enter__()
+    clocks = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        r = step(g)
+    launches0 = api.launch_count()
+    _prof(g, 1)
+    times = []
+    barrier()
+    t_timed0 = time.perf_counter()
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = step(g)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    barrier()
+    t_timed1 = time.perf_counter()
+    time.sleep(0.25)
+    for smp in (nvml, clocks):
+        smp.__exit__(None, None, None)
+        smp.window(t_timed0, t_timed1)
+    launches = api.launch_count() - launches0
+    prof = _prof(g, 0)
+    mean_step = max_over_ranks(statistics.mean(times), dist)
+    e2e_times = []
+    for _ in range(0 if args.skip_e2e else max(5, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with api.Genotypes(rows_np, n) as g2:
+            g2.set_precision(_lib.PREC_BF16X2)
+            step(g2)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = (statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]) if e2e_times else None
+    e2e = max_over_ranks(e2e, dist)
+    h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes + window.nbytes + wwin.nbytes
+    d2h = 8 * (2 + wwin.size)
+    # the same gradient with FP32 products throughout the Lanczos solves
+    fp32 = None
+    if not args.skip_fp32:
+        g.set_precision(_lib.PREC_FP32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rf = step(g)
+        torch.cuda.synchronize()
+        dw = np.max(np.abs(rf["d_w"] - r["d_w"])) / np.max(np.abs(rf["d_w"]))
+        fp32 = {"s": time.perf_counter() - t0,
+                "rel_diff": {"d_sigma_g2": abs(rf["d_sigma_g2"] - r["d_sigma_g2"]) / abs(rf["d_sigma_g2"]),
+                             "d_sigma_e2": abs(rf["d_sigma_e2"] - r["d_sigma_e2"]) / abs(rf["d_sigma_e2"]),
+                             "d_w_max_over_max": float(dw)}}
+        g.set_precision(_lib.PREC_BF16X2)
+    roof, matvec_gbs = roofline(prof, n, m)
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        s_ldet, _, info = cpu_operator_sample(rows_np, n, m, probes, subsets=args.cpu_subsets)
+        t = 1 + probes
+        # Lanczos steps: Zᵀ passes of the solve block, each weighted by its width against 1 + probes;
+        # the closing Z̃ᵀ[P_Hỹ | P_HV | V] pass counts as one more block application
+        # (the closing pass is the one at hi+mid+lo)
+        zt = [s for s in prof if s["dir"] == 1 and s["pieces"] != 3]
+        eq = sum(s["launches"] * s["k"] / t for s in zt) / max(args.steps, 1) + 1.0
+        cpu = {"value": eq * s_ldet, "unit": "s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"{info}; gradient time = {eq:.1f} block applications of H0_ldet_mv on "
+                         f"{t} columns (this run's Lanczos steps + the closing Z^T pass)"}
+    h = {"d_sigma_g2": r["d_sigma_g2"], "d_sigma_e2": r["d_sigma_e2"],
+         "d_w_head": [float(v) for v in r["d_w"][:4]],
+         "homogeneity_residual": abs(sg2 * r["d_sigma_g2"] - float(np.dot(wwin.astype(np.float64), r["d_w"])))
+                                 / abs(sg2 * r["d_sigma_g2"])}
+    line = {
+        "metric": "REML log-likelihood gradient wall time", "value": mean_step, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "windows": int(wwin.size),
+                   "sigma_g2": sg2, "sigma_e2": se2,
+                   "precision": "BF16 hi+lo products in the Lanczos solves, hi+mid+lo in the closing "
+                                "Z^T pass, FP32 accumulation, FP64 scalars and reductions",
+                   "l2": "inputs larger than L2 (packed Z 5.0 GB per pass)", "parallelism": "replicas"},
+        "gradient": h,
+        "step_ms": [round(t * 1e3, 3) for t in times],
+        "matvec_gbs": matvec_gbs,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step_ms": [round(t * 1e3, 3) for t in e2e_times],
+                "median_s": statistics.median(e2e_times[1:]) if len(e2e_times) > 1 else None,
+                "note": "mean of the steps after the first (the first grows the device memory pool)"},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": int(launches / max(args.steps, 1)),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": nvml.summary() or clocks.summary(),
+        "clocks_nvidia_smi": clocks.summary(),
+    }
+    if fp32:
+        line["fp32"] = fp32
     g.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -610,11 +760,17 @@ def main():
         run_kernel_case(args)
         return
     if args.impl == "reference":
+        if cfg.get("grad_windows"):
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference computes no REML gradient; "
+                                  "the gb300 line's cpu_baseline times the same operator work on the host"}),
+                      flush=True)
+            return
         run_reference(args, cfg)
     else:
         from slemm_gb300 import build
         build.build()
-        run_gpu(args, cfg)
+        (run_grad if cfg.get("grad_windows") else run_gpu)(args, cfg)
 
 
 if __name__ == "__main__":

@@ -186,19 +186,33 @@ __global__ void lz_final_kernel(const double* __restrict__ dot, const double* __
   if (c == 0) out[3 * t] = (double)*err;
 }
 
-// X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]   (FP64 accumulation)
-// (columns c0 … c0+tc−1 of the block; coef is steps × tc, X has tc columns)
+// X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]
+// (columns c0 … c0+tc−1 of the block; coef is steps × tc FP64 values held as hi+lo FP32 pairs,
+// coef2[2q] + coef2[2q+1]).  The sum is carried as a double-float pair — each product by
+// TwoProd, the low coefficient word by one more FMA — so X is the FP64 combination rounded once,
+// at FP32 rates (a per-element FP64 FMA chain would bound this kernel by GB300's FP64 pipe, not
+// by the stored basis it streams).
 __global__ void lz_combine_kernel(float* __restrict__ X, int64_t ldx, const float* __restrict__ B,
                                   const float* const* __restrict__ blocks, int J,
-                                  const double* __restrict__ coef, int64_t n, int c0, int tc)
+                                  const float* __restrict__ coef2, int64_t n, int c0, int tc)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (i >= n) return;
   const int64_t o = (int64_t)(c0 + c) * n + i;
-  double acc = coef[c] * (double)B[o];
-  for (int j = 1; j <= J; ++j) acc += coef[(int64_t)j * tc + c] * (double)blocks[j][o];
-  X[(int64_t)c * ldx + i] = (float)acc;
+  DF acc;
+  {
+    const float b = B[o];
+    df_fma(acc, coef2[2 * c], b);
+    acc.lo = __fmaf_rn(coef2[2 * c + 1], b, acc.lo);
+  }
+  for (int j = 1; j <= J; ++j) {
+    const float u = blocks[j][o];
+    const int64_t q = (int64_t)j * tc + c;
+    df_fma(acc, coef2[2 * q], u);
+    acc.lo = __fmaf_rn(coef2[2 * q + 1], u, acc.lo);
+  }
+  X[(int64_t)c * ldx + i] = __fadd_rn(acc.hi, acc.lo);
 }
 
 }  // namespace slemm
@@ -472,13 +486,18 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
   for (int i = 0; i < steps; ++i) hblocks[i] = (i == 0) ? nullptr : S->block(i);
   DevBuf& dcoef = S->solve_coef;
   DevBuf& dblk = S->solve_blk;
-  dcoef.ensure(coef.size() * sizeof(double));
+  std::vector<float> coef2(2 * coef.size());
+  for (size_t q = 0; q < coef.size(); ++q) {
+    coef2[2 * q] = (float)coef[q];
+    coef2[2 * q + 1] = (float)(coef[q] - (double)coef2[2 * q]);
+  }
+  dcoef.ensure(coef2.size() * sizeof(float));
   dblk.ensure(hblocks.size() * sizeof(float*));
-  CUDA_TRY(cudaMemcpyAsync(dcoef.p, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(dcoef.p, coef2.data(), coef2.size() * sizeof(float), cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(dblk.p, hblocks.data(), hblocks.size() * sizeof(float*), cudaMemcpyHostToDevice, st));
   dim3 gr((unsigned)ceil_div(S->n, 256), tc);
   lz_combine_kernel<<<gr, 256, 0, st>>>(dX, ldx, S->B.as<float>(), dblk.as<const float*>(), steps - 1,
-                                        dcoef.as<double>(), S->n, c0, tc);
+                                        dcoef.as<float>(), S->n, c0, tc);
   LAUNCH_CHECK();
   CUDA_TRY(cudaStreamSynchronize(st));   // the host coefficient vectors go out of scope on return
   return steps;

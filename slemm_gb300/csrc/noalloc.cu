@@ -21,6 +21,7 @@
 //   * v and out are device pointers; the work is queued on the handle's stream and the call
 //     returns without synchronising.
 #include "internal.h"
+#include "reduce.cuh"
 
 #include <mutex>
 
@@ -57,7 +58,7 @@ __device__ __forceinline__ float na_mean(const double* __restrict__ mu_sum, int 
   return (float)(mu_sum[c] * (1.0 / (double)n));
 }
 
-// B[c][i] = v[i,c] − μ_c for i < n, 0 for n ≤ i < n_pad; red[c][blk] = Σ_i B[c][i] (FP64).
+// B[c][i] = v[i,c] − μ_c for i < n, 0 for n ≤ i < n_pad; red[c][blk] = Σ_i B[c][i] (double-float per thread, FP64 per block).
 // With B == nullptr only the sums of v are taken (μ_c's pass); mu_sum == nullptr: μ_c = 0.
 __global__ void na_prologue_kernel(const float* __restrict__ v, int64_t ldv, int64_t n, int64_t n_pad,
                                    float* __restrict__ B, double* __restrict__ red, int nblk,
@@ -67,12 +68,13 @@ __global__ void na_prologue_kernel(const float* __restrict__ v, int64_t ldv, int
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kNaRows, i1 = min64(n_pad, i0 + kNaRows);
   const float mu = mu_sum ? na_mean(mu_sum, c, n) : 0.f;
-  double acc = 0.0;
+  DF sum;   // double-float: FP32 operations per element, FP64 once per thread
   for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const float x = (i < n) ? __fsub_rn(v[(int64_t)c * ldv + i], mu) : 0.f;
     if (B) B[(int64_t)c * n_pad + i] = x;
-    acc += (double)x;
+    df_add(sum, x);
   }
+  double acc = df_value(sum);
   for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
   __syncthreads();
@@ -102,14 +104,21 @@ __global__ void na_finalize_kernel(const float* __restrict__ D, int splits, int 
                                    const double* __restrict__ mu_sum, const float* __restrict__ gcorr, int64_t n,
                                    float* __restrict__ out, int64_t ldo)
 {
+  __shared__ float sc[3];   // colsum_c as a hi+lo FP32 pair, μ_c
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
+  if (threadIdx.x == 0) {
+    split_double(colsum[c], sc[0], sc[1]);
+    sc[2] = mu_sum ? na_mean(mu_sum, c, n) : 0.f;
+  }
+  __syncthreads();
   if (j >= m) return;
   float raw = 0.f;
   for (int s = 0; s < splits; ++s) raw += D[((int64_t)s * k + c) * m_pad + j];
-  double val = (double)raw - (double)gm[j] * colsum[c];
-  if (mu_sum) val += (double)na_mean(mu_sum, c, n) * (double)gcorr[j];
-  out[(int64_t)c * ldo + j] = (float)val;
+  const float g = gm[j];
+  float val = __fmaf_rn(-g, sc[1], __fmaf_rn(-g, sc[0], raw));
+  if (mu_sum) val = __fmaf_rn(sc[2], gcorr[j], val);
+  out[(int64_t)c * ldo + j] = val;
 }
 
 struct NaLayout {

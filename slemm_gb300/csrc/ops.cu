@@ -68,11 +68,31 @@ proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __res
   if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.x] = s;
 }
 
-// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ 64
-__device__ __forceinline__ void load_qt(const double* __restrict__ parts, int nblk, int cq, int k, int c, double* qt)
+// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ 64, as hi+lo FP32 pairs
+__device__ __forceinline__ void load_qt(const double* __restrict__ parts, int nblk, int cq, int k, int c, float2* qt)
 {
-  if ((int)threadIdx.x < cq) qt[threadIdx.x] = sum_partials(parts + (int64_t)(threadIdx.x * k + c) * nblk, nblk);
+  if ((int)threadIdx.x < cq) {
+    float h, l;
+    split_double(sum_partials(parts + (int64_t)(threadIdx.x * k + c) * nblk, nblk), h, l);
+    qt[threadIdx.x] = make_float2(h, l);
+  }
   __syncthreads();
+}
+
+// Σ_l Q[i,l]·qt_l rounded once to FP32.  The products (TwoProd by FMA, plus the low coefficient
+// word) and their sum are carried as a double-float pair, so the value is the FP64 one to about
+// 2⁻⁴⁴ before the final rounding, at FP32 rates: GB300's FP64 pipe would otherwise bound the
+// row-wise kernels that project every element.
+__device__ __forceinline__ float proj_dot(const float* __restrict__ Q, int64_t ldq, int cq, int64_t i,
+                                          const float2* qt)
+{
+  DF a;
+  for (int l = 0; l < cq; ++l) {
+    const float q = Q[(int64_t)l * ldq + i];
+    df_fma(a, q, qt[l].x);
+    a.lo = __fmaf_rn(q, qt[l].y, a.lo);
+  }
+  return __fadd_rn(a.hi, a.lo);
 }
 
 // X[i,c] −= Σ_l Q[i,l]·QtX[l,c] (+ tau0·Vin[i,c] when Vin != nullptr)
@@ -82,7 +102,7 @@ proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq, float* __res
                   int64_t n, int k, const double* __restrict__ qparts, int nblkq,
                   const float* __restrict__ Vin, int64_t ld_v, float tau0)
 {
-  __shared__ double qt[64];
+  __shared__ float2 qt[64];
   const int c = blockIdx.y;
   load_qt(qparts, nblkq, cq, k, c, qt);
   const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
@@ -91,9 +111,7 @@ proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq, float* __res
   ldv<V>(X + (int64_t)c * ldx + i, x);
 #pragma unroll
   for (int u = 0; u < V; ++u) {
-    double a = 0.0;
-    for (int l = 0; l < cq; ++l) a += (double)Q[(int64_t)l * ldq + i + u] * qt[l];
-    x[u] = x[u] - (float)a;
+    x[u] = __fsub_rn(x[u], proj_dot(Q, ldq, cq, i + u, qt));
     if (Vin) x[u] = __fmaf_rn(tau0, Vin[(int64_t)c * ld_v + i + u], x[u]);
   }
   stv<V>(X + (int64_t)c * ldx + i, x);
@@ -250,7 +268,7 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
                       double* __restrict__ red, int nblk, const double* __restrict__ mparts)
 {
   __shared__ double sh[32];
-  __shared__ double qt[64];
+  __shared__ float2 qt[64];
   __shared__ float smu;
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n_pad, i0 + kRowsPerBlock);
@@ -273,11 +291,7 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
       ldv<V>(in + (int64_t)c * ld + i, x);
       if (proj) {
 #pragma unroll
-        for (int u = 0; u < V; ++u) {
-          double p = 0.0;
-          for (int l = 0; l < cq; ++l) p += (double)Q[(int64_t)l * ldq + i + u] * qt[l];
-          x[u] = x[u] - (float)p;
-        }
+        for (int u = 0; u < V; ++u) x[u] = __fsub_rn(x[u], proj_dot(Q, ldq, cq, i + u, qt));
       }
       if (rr) {
         float r[V];

@@ -726,6 +726,20 @@ using namespace slemm;
 //   ∂ℓ/∂w_k  = −½·Σ_{j ∈ window k} gw_j·[b_j − a_j/σ_g²].
 // The per-SNP terms of every window come from one packed product Z̃ᵀ[P_Hỹ | P_HV | V] (hi+mid+lo
 // pieces), the transposed product the operators use, reduced per window on the host in FP64.
+// Per-SNP terms of the gradient from T = Z̃ᵀ[P_Hỹ | P_HV | V] (column-major, m rows):
+// a_j = t_{0,j}², b_j = scale·Σ_v t_{1+v,j}·t_{1+n_V+v,j}, accumulated in FP64 (n_V FMAs per SNP).
+__global__ void grad_terms_kernel(const float* __restrict__ T, int64_t m, int n_V, double scale,
+                                  double* __restrict__ ab)
+{
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const double t0 = T[j];
+    double b = 0.0;
+    for (int v = 0; v < n_V; ++v) b = fma((double)T[(int64_t)(1 + v) * m + j], (double)T[(int64_t)(1 + n_V + v) * m + j], b);
+    ab[j] = t0 * t0;
+    ab[m + j] = b * scale;
+  }
+}
+
 void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int c, const float* y,
                const float* persnp, const int32_t* window, int n_win, const float* wwin, double sg2,
                double se2, int n_V, int seed, float tol, double* grad)
@@ -796,19 +810,20 @@ void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     throw;
   }
   g->prec = prec;
-  std::vector<float> T((size_t)m * k);
-  CUDA_TRY(cudaMemcpyAsync(T.data(), d_T.p, T.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaStreamSynchronize(st));
+  // per-SNP a_j, b_j on the device; only these 2m doubles come back
+  double* d_ab = (double*)d_U.p;   // U is free again (n·k floats ≥ 2m doubles is checked below)
+  DevBuf d_abuf(st);
+  if ((size_t)n * k * sizeof(float) < 2 * (size_t)m * sizeof(double))
+    d_ab = (double*)d_abuf.ensure(2 * (size_t)m * sizeof(double));
+  grad_terms_kernel<<<(unsigned)std::min<int64_t>(ceil_div(m, 256), 152 * 8), 256, 0, st>>>(
+      d_T.as<float>(), m, n_V, (double)n / (double)n_V, d_ab);
+  LAUNCH_CHECK();
+  const std::vector<double> ab = d2h(g, d_ab, 2 * (size_t)m);
   check_device_error(g);
   double sa = 0.0, sb = 0.0;
   std::vector<double> ga(std::max(n_win, 1), 0.0), gb(std::max(n_win, 1), 0.0);
-  const double scale = (double)n / (double)n_V;
   for (int64_t j = 0; j < m; ++j) {
-    const double ty = T[j];
-    const double a = ty * ty;
-    double b = 0.0;
-    for (int v = 0; v < n_V; ++v) b += (double)T[(size_t)(1 + v) * m + j] * (double)T[(size_t)(1 + n_V + v) * m + j];
-    b *= scale;
+    const double a = ab[j], b = ab[m + j];
     sa += (double)W[j] * a;
     sb += (double)W[j] * b;
     if (window && window[j] >= 0) {
