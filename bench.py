@@ -48,6 +48,11 @@ CONFIGS = {
     4: dict(n=200000, m=100000, probes=64, h2=0.4, missing=0.0, grad_windows=2000, sigma_g2=0.4, sigma_e2=0.6,
             name="n=200000 m=100000, REML log-likelihood gradient for (sigma_g2, sigma_e2) and 2,000 per-window "
                  "SNP weights in (0, 2] (windows of 50 SNPs), 64 Rademacher probes"),
+    5: dict(n=1000000, m=50000, probes=64, h2=0.4, missing=0.0, traits=16, miss_lo=0.05, miss_hi=0.40,
+            gwas_m=200000,
+            name="n=1000000 m=50000, 16 traits with 5-40% of individuals missing per trait (one handle per trait "
+                 "packed from the .bed rows held in HBM), DF-REML + BLUP with 64 probes each; GWAS score terms "
+                 "over a 1000000 x 200000 .bed for the first trait's individuals"),
 }
 
 
@@ -309,6 +314,8 @@ def run_reference(args, cfg):
         s_ldet *= m / min(m, 4000)
         s_quad *= m / min(m, 4000)
         est = max(it_q, it_v) * s_ldet + it_y * s_quad
+        if cfg.get("traits"):   # one fit per trait on its own individuals
+            est *= sum(k.size for k in trait_keeps(cfg)[0]) / n
         if s >= args.warmup:
             vals.append(est)
     value = statistics.mean(vals)
@@ -320,7 +327,9 @@ def run_reference(args, cfg):
         "cpu_baseline": {"value": value, "unit": "s", "cores": cpu_threads(), "kind": "port",
                          "sample": f"{info}; Lanczos steps (y {it_y}, Q {it_q}, V {it_v}) from the "
                                    f"reference algorithm run in full on an n={small_n}, m={small_m} "
-                                   f"problem with the same n/m ratio"},
+                                   f"problem with the same n/m ratio"
+                                   + (f"; summed over {cfg['traits']} traits in proportion to their individuals "
+                                      f"(GWAS score terms not included)" if cfg.get("traits") else "")},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -673,6 +682,232 @@ def run_grad(args, cfg):
         dist.destroy_process_group()
 
 
+def trait_keeps(cfg):
+    """Per trait the kept individuals (sorted .fam indices): trait t misses a fraction of the
+    individuals that runs evenly from miss_lo to miss_hi over the traits, drawn at random."""
+    n, T = cfg["n"], cfg["traits"]
+    rng = np.random.default_rng(11)
+    frac = np.linspace(cfg["miss_lo"], cfg["miss_hi"], T)
+    return [np.sort(rng.choice(n, size=n - int(round(f * n)), replace=False)).astype(np.int64) for f in frac], frac
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    return int(ln.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+def run_multi(args, cfg):
+    """Multi-trait workload: one step = DF-REML + BLUP for every trait on its own individuals —
+    each trait's handle packed (both tiled copies, per-SNP counts of its individuals) from the
+    .bed rows held in HBM, as the reference analyses each trait on its own individual set — then
+    the GWAS score terms of the first trait over a 10⁶-row, 2·10⁵-SNP .bed (resident handle of
+    that trait's individuals)."""
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from slemm_gb300 import api, _lib, synth
+    api.init(local)
+    n, m, probes, T, m2 = cfg["n"], cfg["m"], cfg["probes"], cfg["traits"], cfg["gwas_m"]
+    rows_dev, Y = synth.simulate_bed_torch(n, m, seed=1, h2=cfg["h2"], n_traits=T, rows_device=True)
+    Y = Y.astype(np.float32)
+    keeps, frac = trait_keeps(cfg)
+    persnp = np.ones(m, np.float32)
+    Xs = [np.ones((k.size, 1), np.float32) for k in keeps]
+    ys = [np.ascontiguousarray(Y[k, t]) for t, k in enumerate(keeps)]
+    # GWAS .bed: rows generated in HBM, packed for trait 0's individuals, rows then released
+    grows, _ = synth.simulate_bed_torch(n, m2, seed=7, h2=cfg["h2"], rows_device=True)
+    torch.cuda.empty_cache()   # the generator's temporaries
+    gw = api.Genotypes(grows, n, keep_idx=keeps[0])
+    keep_gw_host = None
+    if not args.skip_e2e and _mem_available_gb() > 2.0 * (grows.numel() + rows_dev.numel()) / 1e9:
+        keep_gw_host = grows.cpu().pin_memory().numpy()   # pinned host copy for the end-to-end leg
+    del grows
+    torch.cuda.empty_cache()
+    n0 = keeps[0].size
+    Q0 = np.full((n0, 1), 1.0 / np.sqrt(n0), np.float32)
+    ones0 = np.ones(n0, np.float32)
+    zeros2 = np.zeros(m2, np.float32)
+
+    def gwas(gh, Py):
+        gh.set_weights(zeros2, zeros2, ones0)
+        gh.set_projection(Q0)
+        return gh.score_terms(Py, mac=20)
+
+    def step(rows, gwas_handle=None, gwas_rows=None):
+        res = []
+        for t in range(T):
+            with api.Genotypes(rows, n, keep_idx=keeps[t]) as gt:
+                gt.set_precision(_lib.PREC_BF16X2)
+                res.append(gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes))
+        if gwas_handle is not None:
+            sc = gwas(gwas_handle, res[0]["Py"])
+        else:
+            with api.Genotypes(gwas_rows, n, keep_idx=keeps[0]) as g2:
+                sc = gwas(g2, res[0]["Py"])
+        return res, sc
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    nvml = NvmlSampler(local).__enter__()
+    clocks = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        step(rows_dev, gw)
+    launches0 = api.launch_count()
+    times = []
+    barrier()
+    t_timed0 = time.perf_counter()
+    for _ in range(args.steps):
+        # the per-trait handles run on their own streams: time on the host around a device sync
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, sc = step(rows_dev, gw)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    barrier()
+    t_timed1 = time.perf_counter()
+    time.sleep(0.25)
+    for smp in (nvml, clocks):
+        smp.__exit__(None, None, None)
+        smp.window(t_timed0, t_timed1)
+    launches = api.launch_count() - launches0
+    mean_step = max_over_ranks(statistics.mean(times), dist)
+    # per-phase split of one step: trait handles (pack), fits, GWAS score pass
+    # (the first trait's fit also gives the packed-product launch shapes for the roofline)
+    ph = {"pack_s": 0.0, "fit_s": 0.0}
+    prof = None
+    for t in range(T):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gt = api.Genotypes(rows_dev, n, keep_idx=keeps[t])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        gt.set_precision(_lib.PREC_BF16X2)
+        if t == 0:
+            _prof(gt, 1)
+        gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes)
+        torch.cuda.synchronize()
+        if t == 0:
+            prof = _prof(gt, 0)
+        ph["pack_s"] += t1 - t0
+        ph["fit_s"] += time.perf_counter() - t1
+        gt.close()
+    roof, matvec_gbs = roofline(prof, int(keeps[0].size), m)
+    t0 = time.perf_counter()
+    gwas(gw, res[0]["Py"])
+    torch.cuda.synchronize()
+    ph["gwas_score_s"] = time.perf_counter() - t0
+    # ---- e2e: .bed rows from host memory through the reference-facing calls ----
+    e2e, e2e_times, h2d, e2e_note = None, [], 0, None
+    if not args.skip_e2e:
+        rows_host = rows_dev.cpu().pin_memory()
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rows_up = rows_host.to("cuda", non_blocking=True)   # the .bed rows cross the link once
+            if keep_gw_host is not None:
+                step(rows_up, gwas_rows=keep_gw_host)
+            else:
+                step(rows_up, gw)
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+            del rows_up
+        e2e = max_over_ranks(statistics.mean(e2e_times), dist)
+        h2d = rows_host.numel() + sum(y.nbytes + x.nbytes for y, x in zip(ys, Xs)) + T * persnp.nbytes
+        if keep_gw_host is not None:
+            h2d += keep_gw_host.nbytes
+            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, every trait's handle "
+                        "packed from them in HBM; the GWAS .bed uploaded from host memory through genotype_create")
+        else:
+            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, every trait's handle "
+                        "packed from them in HBM; the GWAS handle stays resident (too little free host memory "
+                        "for a host copy of its 50 GB of rows)")
+        del rows_host
+    d2h = sum((k.size + m + 1 + 1) * 4 for k in keeps) + 2 * 4 * m2
+    # plain FP32 per-vector fit of the first trait (the comparison the metric names)
+    fp32 = None
+    if not args.skip_fp32:
+        with api.Genotypes(rows_dev, n, keep_idx=keeps[0]) as gt:
+            gt.set_precision(_lib.PREC_FP32)
+            gt.set_per_vector(True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rf = gt.SLDF_REML(None, Xs[0], ys[0], persnp, seed=0, n_V=probes)
+            torch.cuda.synchronize()
+            fp32 = {"trait": 0, "s": time.perf_counter() - t0, "h2": rf["h2"], "dh2": abs(rf["h2"] - res[0]["h2"])}
+    # CPU baseline: the oracle's operators on a bounded SNP sample at full n, scaled per trait
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        rows_s = rows_dev[:4000].cpu().numpy()
+        s_ldet, s_quad, info = cpu_operator_sample(rows_s, n, 4000, probes, subsets=max(1, args.cpu_subsets - 1))
+        s_ldet *= m / 4000
+        s_quad *= m / 4000
+        est = 0.0
+        for r, k in zip(res, keeps):
+            it_y, it_q, it_v = r["iters"]
+            est += (max(it_q, it_v) * s_ldet + it_y * s_quad) * k.size / n
+        from oracle import slemm_np as orc
+        sel = np.arange(0, m2, m2 // 64)[:64]
+        mask = np.zeros(n, np.uint8)
+        mask[keeps[0]] = 1
+        t0 = time.perf_counter()
+        grows_s = keep_gw_host[sel] if keep_gw_host is not None else None
+        if grows_s is not None:
+            dec = orc.bed_decode(grows_s, n, mask)
+            orc.gamma_terms(dec, res[0]["Py"], ones0, Q0.astype(np.float64), 20)
+            s_gw = (time.perf_counter() - t0) * m2 / sel.size
+            est += s_gw
+            info += f"; GWAS score terms: {sel.size} SNPs decoded and scored by the oracle, scaled ×{m2 / sel.size:.0f}"
+        cpu = {"value": est, "unit": "s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"{info} (4000 SNP rows of the REML .bed); per trait Lanczos steps × t(ldet, 65 cols) "
+                         f"+ steps × t(quadform), scaled by the trait's share of individuals"}
+    line = {
+        "metric": METRIC, "value": mean_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "traits": T,
+                   "missing_fraction": [round(float(f), 4) for f in frac], "gwas_m": m2,
+                   "precision": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars; GWAS hi+mid+lo",
+                   "l2": "inputs larger than L2 (packed Z ≥ 7.5 GB per pass)", "parallelism": "replicas",
+                   "timing": "host clock around a device synchronisation (each trait handle has its own stream)"},
+        "per_trait": [{"n": int(k.size), "h2": r["h2"], "iters": list(r["iters"])} for r, k in zip(res, keeps)],
+        "phases_s": ph,
+        "gwas": {"tested": int(np.isfinite(sc[0]).sum())},
+        "step_ms": [round(t * 1e3, 3) for t in times],
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step_ms": [round(t * 1e3, 3) for t in e2e_times], "note": e2e_note},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": int(launches / max(args.steps, 1)),
+        "roofline": roof,
+        "matvec_gbs_trait0": matvec_gbs,
+        "cpu_baseline": cpu,
+        "clocks": nvml.summary() or clocks.summary(),
+        "clocks_nvidia_smi": clocks.summary(),
+    }
+    if fp32:
+        line["fp32_per_vector_trait0"] = fp32
+    gw.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def _prof(g, enable):
     import ctypes
     from slemm_gb300 import _lib
@@ -770,7 +1005,7 @@ def main():
     else:
         from slemm_gb300 import build
         build.build()
-        (run_grad if cfg.get("grad_windows") else run_gpu)(args, cfg)
+        (run_grad if cfg.get("grad_windows") else run_multi if cfg.get("traits") else run_gpu)(args, cfg)
 
 
 if __name__ == "__main__":

@@ -174,7 +174,7 @@ struct GemmArgs {
 void gemm_simt(const GemmArgs& a, cudaStream_t st);
 // Tensor-core path (tcgen05); N must be a multiple of 16 in [16, 256].
 void gemm_tc(const GemmArgs& a, cudaStream_t st);
-int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int num_sms);
+int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int num_sms, int min_splits = 1);
 // Rows one tensor-core CTA covers for this N (128 or 256).
 int gemm_tc_rows_per_cta(int N);
 int num_sms();

@@ -50,14 +50,15 @@ int num_sms()
 }
 
 // Picks the split-K factor so that M_tiles·splits CTAs fill whole waves, keeping at least
-// 16 K-tiles per split.
-int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int sms)
+// 16 K-tiles per split and at least min_splits splits.
+int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int sms, int min_splits)
 {
   const int64_t slots = (int64_t)ctas_per_sm * sms;
   int best = 1;
   double best_eff = -1.0;
-  for (int s = 1; s <= 16; ++s) {
+  for (int s = 1; s <= std::max(16, min_splits); ++s) {
     if (s > 1 && K_tiles / s < 16) break;
+    if (s < min_splits) continue;
     const int64_t ctas = M_tiles * s;
     const double waves = (double)ctas / slots;
     const double eff = waves / std::ceil(waves) - 0.015 * (s - 1);   // partials cost per split
@@ -69,74 +70,15 @@ int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int sms)
   return best;
 }
 
-// ---- pack kernels ------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned count_of(const uint8_t* __restrict__ row, int64_t f)
-{
-  const unsigned code = (row[f >> 2] >> (2 * (f & 3))) & 3u;
-  return (code & 1u) + (code >> 1);   // missing (01) → 1, exactly as the reference's b[k]+b[k+1]
-}
-
-__device__ __forceinline__ unsigned plane_bits(unsigned x, int e)
-{
-  // element e (0..15) of a word; x = count as a 2-bit field
-  const int q = e >> 1;
-  return (e & 1) ? (x << (16 + 2 * q)) : (x << (2 * q));
-}
-
-// G words: thread → (SNP row j, word wi along individuals).
-__global__ void pack_G_kernel(const uint8_t* __restrict__ raw, int64_t row_bytes, int64_t j0,
-                              int64_t rows_in_chunk, const int64_t* __restrict__ keep, int64_t n,
-                              int64_t K_tiles, uint32_t* __restrict__ G)
-{
-  const int64_t words_per_row = K_tiles * 4;   // 64 elements per tile row = 4 words
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t jl = gid / words_per_row;
-  const int64_t wi = gid % words_per_row;
-  if (jl >= rows_in_chunk) return;
-  const int64_t j = j0 + jl;
-  const uint8_t* row = raw + jl * row_bytes;
-  unsigned word = 0;
-#pragma unroll 4
-  for (int e = 0; e < 16; ++e) {
-    const int64_t i = wi * 16 + e;
-    if (i < n) word |= plane_bits(count_of(row, keep ? keep[i] : i), e);
-  }
-  const int64_t mt = j / 128, r = j % 128, kt = wi / 4, wr = wi % 4;
-  G[((mt * K_tiles + kt) * 128 + r) * 4 + wr] = word;
-}
-
-// GT words: thread → (individual row i, word wj along SNPs of this chunk).
-__global__ void pack_GT_kernel(const uint8_t* __restrict__ raw, int64_t row_bytes, int64_t j0,
-                               int64_t rows_in_chunk, int64_t m, const int64_t* __restrict__ keep,
-                               int64_t n, int64_t n_pad, int64_t K_tiles_T,
-                               uint32_t* __restrict__ GT)
-{
-  // chunk covers SNPs j0 .. j0+rows_in_chunk (j0 multiple of 128); words of 16 SNPs
-  const int64_t words_in_chunk = ceil_div(rows_in_chunk, 16);
-  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t i = gid % n_pad;
-  const int64_t wl = gid / n_pad;
-  if (wl >= words_in_chunk) return;
-  unsigned word = 0;
-  if (i < n) {
-    const int64_t f = keep ? keep[i] : i;
-#pragma unroll 4
-    for (int e = 0; e < 16; ++e) {
-      const int64_t jl = wl * 16 + e;
-      if (jl < rows_in_chunk && j0 + jl < m) word |= plane_bits(count_of(raw + jl * row_bytes, f), e);
-    }
-  }
-  const int64_t wj = j0 / 16 + wl;   // global word index along SNPs
-  const int64_t mt = i / 128, r = i % 128, kt = wj / 4, wr = wj % 4;
-  GT[((mt * K_tiles_T + kt) * 128 + r) * 4 + wr] = word;
-}
-
-// ---- tiled pack (no individual subset) -----------------------------------------------------------
-// One CTA turns a block of 128 SNP rows × 128 raw bytes (512 individuals) into the 8 G tiles and
-// 8 GT tiles that cover it: the raw bytes are read row-contiguously from device memory (the
-// caller's rows, or a staging buffer the host rows were copied into), the codes become 2-bit
-// counts with four bit operations per 16 calls, and both copies are written tile-contiguously
-// through shared memory.
+// ---- tiled pack -------------------------------------------------------------------------------------
+// One CTA turns a block of 128 SNP rows × 512 analysed individuals into the 8 G tiles and 8 GT
+// tiles that cover it.  The raw bytes are read from device memory (the caller's rows, or a
+// staging buffer the host rows were copied into): row-contiguously (128 bytes per row) when every
+// individual is analysed; with a keep list, each thread gathers the 16 codes of one count word
+// from one .bed row through the block's 512 .fam positions (staged in shared memory), loading a
+// byte only when the position moves to the next one — sorted lists of a few percent to a few tens
+// of percent missing read each byte about once.  The codes become 2-bit counts with four bit
+// operations per 16 calls, and both copies are written tile-contiguously through shared memory.
 constexpr int kPackThreads = 256;
 
 // 16 PLINK codes (code e at bits 2e) → 16 counts in the same positions: count = bit0 + bit1
@@ -164,33 +106,67 @@ __device__ __forceinline__ uint32_t unshuffle2(uint32_t x)
 // blockIdx.x: SNP group (G M-tile, GT K-tiles 2·sg, 2·sg+1); blockIdx.y: 512-individual group.
 // Also adds the block's per-SNP class counts (fields 01 and 10) into c1/c2 ([m_pad] int32 each,
 // zeroed beforehand); integer sums, so the totals do not depend on the order of the blocks.
+// keep (KEEP only): .fam position of each of the n analysed individuals, < row_bytes·4.
+template <bool KEEP>
 __global__ void __launch_bounds__(kPackThreads)
 pack_tiles_kernel(const uint8_t* __restrict__ raw, int64_t row_stride, int64_t row_bytes, int64_t j0,
                   int64_t rows, int64_t m, int64_t n, int64_t Kt_G, int64_t Mt_T, int64_t Kt_T, bool aligned4,
-                  uint32_t* __restrict__ G, uint32_t* __restrict__ GT, int32_t* __restrict__ c1,
-                  int32_t* __restrict__ c2)
+                  const int32_t* __restrict__ keep, uint32_t* __restrict__ G, uint32_t* __restrict__ GT,
+                  int32_t* __restrict__ c1, int32_t* __restrict__ c2)
 {
   __shared__ uint32_t cnt[128][33];    // [SNP row][16-individual word], natural order
   __shared__ uint32_t outT[512][9];    // [individual][GT word 0 … 7 (2 K-tiles × 4)]
+  __shared__ int32_t sfam[KEEP ? 512 : 1];   // .fam positions of the block's individuals, −1 past n
   const int tid = threadIdx.x;
   const int64_t sg = (int64_t)blockIdx.x + j0 / 128;
   const int64_t ig = blockIdx.y;
-  for (int idx = tid; idx < 128 * 32; idx += kPackThreads) {
-    const int r = idx >> 5, q = idx & 31;
-    const int64_t j = sg * 128 + r;
-    const int64_t b0 = ig * 128 + 4 * q;
-    uint32_t w = 0;
-    if (j < m && j - j0 < rows && b0 < row_bytes) {
-      const uint8_t* p = raw + (j - j0) * row_stride + b0;
-      if (aligned4 && b0 + 4 <= row_bytes) {
-        w = *reinterpret_cast<const uint32_t*>(p);
-      } else {
-        for (int k = 0; k < 4 && b0 + k < row_bytes; ++k) w |= (uint32_t)p[k] << (8 * k);
-      }
+  if constexpr (KEEP) {
+    for (int t = tid; t < 512; t += kPackThreads) {
+      const int64_t i = ig * 512 + t;
+      sfam[t] = i < n ? keep[i] : -1;
     }
-    const int64_t i0 = 4 * b0;   // first individual of the word
-    const uint32_t valid = (i0 + 16 <= n) ? 0xFFFFFFFFu : (i0 >= n ? 0u : ((1u << (2 * (n - i0))) - 1u));
-    cnt[r][q] = counts_of_codes(w) & valid;
+    __syncthreads();
+    // a warp: one SNP row, 32 consecutive count words (512 individuals) — neighbouring bytes
+    for (int idx = tid; idx < 128 * 32; idx += kPackThreads) {
+      const int r = idx >> 5, q = idx & 31;
+      const int64_t j = sg * 128 + r;
+      uint32_t w = 0;   // codes in natural order; 00 (count 0) past n
+      if (j < m && j - j0 < rows) {
+        const uint8_t* p = raw + (j - j0) * row_stride;
+        int64_t at = -1;
+        uint32_t byte = 0;
+#pragma unroll 4
+        for (int e = 0; e < 16; ++e) {
+          const int32_t f = sfam[16 * q + e];
+          if (f < 0) break;
+          const int64_t bi = f >> 2;
+          if (bi != at) {
+            byte = p[bi];
+            at = bi;
+          }
+          w |= ((byte >> (2 * (f & 3))) & 3u) << (2 * e);
+        }
+      }
+      cnt[r][q] = counts_of_codes(w);
+    }
+  } else {
+    for (int idx = tid; idx < 128 * 32; idx += kPackThreads) {
+      const int r = idx >> 5, q = idx & 31;
+      const int64_t j = sg * 128 + r;
+      const int64_t b0 = ig * 128 + 4 * q;
+      uint32_t w = 0;
+      if (j < m && j - j0 < rows && b0 < row_bytes) {
+        const uint8_t* p = raw + (j - j0) * row_stride + b0;
+        if (aligned4 && b0 + 4 <= row_bytes) {
+          w = *reinterpret_cast<const uint32_t*>(p);
+        } else {
+          for (int k = 0; k < 4 && b0 + k < row_bytes; ++k) w |= (uint32_t)p[k] << (8 * k);
+        }
+      }
+      const int64_t i0 = 4 * b0;   // first individual of the word
+      const uint32_t valid = (i0 + 16 <= n) ? 0xFFFFFFFFu : (i0 >= n ? 0u : ((1u << (2 * (n - i0))) - 1u));
+      cnt[r][q] = counts_of_codes(w) & valid;
+    }
   }
   __syncthreads();
   if (tid < 128 && sg * 128 + tid < m) {   // the row's 512 individuals: count-1 and count-2 fields
@@ -367,7 +343,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
     CHECK_ARG(row_stride >= row_bytes, "row_stride < ceil(n_fam/4)");
     if (!keep_idx) CHECK_ARG(n == n_fam, "keep_idx is null but n != n_fam");
     CHECK_ARG(n <= n_fam, "n > n_fam");
-    CHECK_ARG(n < (int64_t)INT32_MAX && m < (int64_t)INT32_MAX, "dimension exceeds 2^31");
+    CHECK_ARG(n_fam < (int64_t)INT32_MAX && m < (int64_t)INT32_MAX, "dimension exceeds 2^31");
     if (keep_idx)
       for (int64_t i = 0; i < n; ++i)
         CHECK_ARG(keep_idx[i] >= 0 && keep_idx[i] < n_fam, "keep_idx entry out of range");
@@ -394,88 +370,69 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       g->err.ensure(sizeof(int));
       CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));
       const int64_t Mt_T = g->n_pad / kTileM;
-      if (!keep_idx) {
-        // tiled pack of both copies, padding included, with the per-SNP class counts on the side
-        g->dcounts.ensure((size_t)2 * g->m_pad * sizeof(int32_t));
-        CUDA_TRY(cudaMemsetAsync(g->dcounts.p, 0, (size_t)2 * g->m_pad * sizeof(int32_t), g->stream));
-        int32_t* d_n1 = g->dcounts.as<int32_t>();
-        int32_t* d_n2 = d_n1 + g->m_pad;
-        const unsigned gy = (unsigned)ceil_div(g->n_pad, 512);
-        if (rows_on_device) {
-          const bool al = ((uintptr_t)bed_rows % 4 == 0) && (row_stride % 4 == 0);
-          pack_tiles_kernel<<<dim3((unsigned)(g->m_pad / 128), gy), kPackThreads, 0, g->stream>>>(
-              bed_rows, row_stride, row_bytes, 0, m, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
-              g->GT.as<uint32_t>(), d_n1, d_n2);
-          LAUNCH_CHECK();
-        } else {
-          // Host rows: the host link is the bound (≈210 GB/s on GB300's C2C, whether DMA or the
-          // kernel reads host memory itself, and the pack kernel's scattered 128-byte reads got
-          // only ≈155 GB/s).  So DMA chunks of 4096 rows into two staging buffers on a copy
-          // stream while the handle's stream packs the previous chunk from HBM.
-          const int64_t chunk = 4096;
-          DevBuf raw0(g->stream), raw1(g->stream);
-          raw0.ensure((size_t)chunk * row_bytes);
-          raw1.ensure((size_t)chunk * row_bytes);
-          uint8_t* raw[2] = {raw0.as<uint8_t>(), raw1.as<uint8_t>()};
-          UploadPipe pipe;   // destroyed before raw0/raw1: the copy stream is drained first
-          pipe.open();
-          CUDA_TRY(cudaEventRecord(pipe.ready, g->stream));   // staging allocations and count zeroing
-          CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.ready, 0));
-          const bool al = (row_bytes % 4 == 0);
-          int c = 0;
-          for (int64_t j0 = 0; j0 < g->m_pad; j0 += chunk, ++c) {
-            const int b = c & 1;
-            const int64_t rows = std::max<int64_t>(0, std::min(chunk, m - j0));
-            if (rows > 0) {
-              if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.packed[b], 0));   // buffer b is free
-              CUDA_TRY(cudaMemcpy2DAsync(raw[b], row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
-                                         cudaMemcpyDefault, pipe.cs));
-              CUDA_TRY(cudaEventRecord(pipe.copied[b], pipe.cs));
-              CUDA_TRY(cudaStreamWaitEvent(g->stream, pipe.copied[b], 0));
-            }
-            const unsigned gx = (unsigned)(std::min(chunk, g->m_pad - j0) / 128);
-            pack_tiles_kernel<<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
-                raw[b], row_bytes, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al, g->G.as<uint32_t>(),
-                g->GT.as<uint32_t>(), d_n1, d_n2);
-            LAUNCH_CHECK();
-            CUDA_TRY(cudaEventRecord(pipe.packed[b], g->stream));
-          }
-          CUDA_TRY(cudaStreamSynchronize(g->stream));
-        }
-        g->dcounts_valid = true;
-      } else {
-        CUDA_TRY(cudaMemsetAsync(g->G.p, 0, bytes_G, g->stream));
-        CUDA_TRY(cudaMemsetAsync(g->GT.p, 0, bytes_GT, g->stream));
-        DevBuf d_keep;
-        d_keep.ensure(n * sizeof(int64_t));
-        CUDA_TRY(cudaMemcpyAsync(d_keep.p, keep_idx, n * sizeof(int64_t), cudaMemcpyHostToDevice, g->stream));
-        // stream SNP chunks of 4096 rows (multiple of 128) through a device staging buffer
-        const int64_t chunk = 4096;
-        DevBuf d_raw;
-        d_raw.ensure((size_t)chunk * row_bytes);
-        for (int64_t j0 = 0; j0 < m; j0 += chunk) {
-          const int64_t rows = std::min(chunk, m - j0);
-          CUDA_TRY(cudaMemcpy2DAsync(d_raw.p, row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
-                                     cudaMemcpyDefault, g->stream));
-          {
-            const int64_t total = rows * (Kt_G * 4);
-            const int th = 256;
-            pack_G_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
-                d_raw.as<uint8_t>(), row_bytes, j0, rows, d_keep.as<int64_t>(), n, Kt_G, g->G.as<uint32_t>());
-            LAUNCH_CHECK();
-          }
-          {
-            const int64_t total = ceil_div(rows, 16) * g->n_pad;
-            const int th = 256;
-            pack_GT_kernel<<<(unsigned)ceil_div(total, th), th, 0, g->stream>>>(
-                d_raw.as<uint8_t>(), row_bytes, j0, rows, m, d_keep.as<int64_t>(), n, g->n_pad, Kt_GT,
-                g->GT.as<uint32_t>());
-            LAUNCH_CHECK();
-          }
-        }
-        CUDA_TRY(cudaStreamSynchronize(g->stream));   // staging buffers are released on return
+      // kept individuals as 32-bit .fam positions (checked on the host above)
+      DevBuf d_keep(g->stream);
+      const int32_t* kp = nullptr;
+      if (keep_idx) {
+        std::vector<int32_t> k32(n);
+        for (int64_t i = 0; i < n; ++i) k32[i] = (int32_t)keep_idx[i];
+        d_keep.ensure((size_t)n * sizeof(int32_t));
+        CUDA_TRY(cudaMemcpyAsync(d_keep.p, k32.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                 g->stream));   // pageable source: copied out before the call returns
+        kp = d_keep.as<int32_t>();
       }
-      CUDA_TRY(cudaStreamSynchronize(g->stream));
+      // tiled pack of both copies, padding included, with the per-SNP class counts on the side
+      g->dcounts.ensure((size_t)2 * g->m_pad * sizeof(int32_t));
+      CUDA_TRY(cudaMemsetAsync(g->dcounts.p, 0, (size_t)2 * g->m_pad * sizeof(int32_t), g->stream));
+      int32_t* d_n1 = g->dcounts.as<int32_t>();
+      int32_t* d_n2 = d_n1 + g->m_pad;
+      const unsigned gy = (unsigned)ceil_div(g->n_pad, 512);
+      auto pack = [&](const uint8_t* raw, int64_t stride, int64_t j0, int64_t rows, unsigned gx, bool al) {
+        if (kp)
+          pack_tiles_kernel<true><<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
+              raw, stride, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al, kp, g->G.as<uint32_t>(),
+              g->GT.as<uint32_t>(), d_n1, d_n2);
+        else
+          pack_tiles_kernel<false><<<dim3(gx, gy), kPackThreads, 0, g->stream>>>(
+              raw, stride, row_bytes, j0, rows, m, n, Kt_G, Mt_T, Kt_GT, al, nullptr, g->G.as<uint32_t>(),
+              g->GT.as<uint32_t>(), d_n1, d_n2);
+        LAUNCH_CHECK();
+      };
+      if (rows_on_device) {
+        pack(bed_rows, row_stride, 0, m, (unsigned)(g->m_pad / 128),
+             ((uintptr_t)bed_rows % 4 == 0) && (row_stride % 4 == 0));
+      } else {
+        // Host rows: the host link is the bound (≈210 GB/s on GB300's C2C, whether DMA or the
+        // kernel reads host memory itself, and the pack kernel's scattered 128-byte reads got
+        // only ≈155 GB/s).  So DMA chunks of 4096 rows into two staging buffers on a copy
+        // stream while the handle's stream packs the previous chunk from HBM.
+        const int64_t chunk = 4096;
+        DevBuf raw0(g->stream), raw1(g->stream);
+        raw0.ensure((size_t)chunk * row_bytes);
+        raw1.ensure((size_t)chunk * row_bytes);
+        uint8_t* raw[2] = {raw0.as<uint8_t>(), raw1.as<uint8_t>()};
+        UploadPipe pipe;   // destroyed before raw0/raw1: the copy stream is drained first
+        pipe.open();
+        CUDA_TRY(cudaEventRecord(pipe.ready, g->stream));   // staging allocations, keep list, count zeroing
+        CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.ready, 0));
+        const bool al = (row_bytes % 4 == 0);
+        int c = 0;
+        for (int64_t j0 = 0; j0 < g->m_pad; j0 += chunk, ++c) {
+          const int b = c & 1;
+          const int64_t rows = std::max<int64_t>(0, std::min(chunk, m - j0));
+          if (rows > 0) {
+            if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.packed[b], 0));   // buffer b is free
+            CUDA_TRY(cudaMemcpy2DAsync(raw[b], row_bytes, bed_rows + j0 * row_stride, row_stride, row_bytes, rows,
+                                       cudaMemcpyDefault, pipe.cs));
+            CUDA_TRY(cudaEventRecord(pipe.copied[b], pipe.cs));
+            CUDA_TRY(cudaStreamWaitEvent(g->stream, pipe.copied[b], 0));
+          }
+          pack(raw[b], row_bytes, j0, rows, (unsigned)(std::min(chunk, g->m_pad - j0) / 128), al);
+          CUDA_TRY(cudaEventRecord(pipe.packed[b], g->stream));
+        }
+      }
+      g->dcounts_valid = true;
+      CUDA_TRY(cudaStreamSynchronize(g->stream));   // staging buffers and the keep list are released on return
     } catch (...) {
       g->for_each_buf([](DevBuf& b) { b.release(); });
       if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);

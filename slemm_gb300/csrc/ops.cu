@@ -453,6 +453,17 @@ struct PassPlan {
   int splits;
 };
 
+// Fewest splits of a tensor-core pass.  Once the dense operand (K_pad·N BF16) is larger than half
+// the L2, CTAs with long K ranges run slower per K-tile — co-running CTAs drift apart along K and
+// miss on the dense tiles they share.  Measured for Zᵀ over n = 950,000 individuals at N = 144:
+// 4,948 K-tiles per CTA 0.417 µs per K-tile, 1,485 0.356 (8.25 → 6.87 ms per launch), and 0.331
+// at n = 100,000 where the operand stays in L2.  So such passes keep ≤ 1,536 K-tiles per CTA.
+static int tc_min_splits(int64_t K_tiles, int N)
+{
+  const double dense_bytes = (double)K_tiles * kTileK * N * 2.0;
+  return dense_bytes > 64.0 * 1024 * 1024 ? (int)ceil_div(K_tiles, 1536) : 1;
+}
+
 static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_pad)
 {
   PassPlan p;
@@ -460,7 +471,8 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
   p.pieces = g->prec == SLEMM_PREC_BF16X3 ? 3 : (g->prec == SLEMM_PREC_BF16X2 ? 2 : 1);
   p.N = p.tc ? (int)round_up((int64_t)p.pieces * k, 16) : k;
   const int64_t M_tiles = M_pad / kTileM, K_tiles = K_pad / kTileK;
-  p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms())
+  p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(),
+                                  tc_min_splits(K_tiles, p.N))
                   : choose_splits(M_tiles, K_tiles, 8, num_sms());
   return p;
 }
@@ -678,7 +690,7 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     p.tc = true;
     p.pieces = pieces;
     p.N = (int)round_up((int64_t)pieces * kc, 16);
-    p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms());
+    p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(), tc_min_splits(K_tiles, p.N));
     const int pad = p.N - pieces * kc;
     void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
     float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.N * rows * sizeof(float));

@@ -115,11 +115,15 @@ def write_csv(path: str, header, columns):
 
 def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal: int = 1000,
                        missing: float = 0.0, device: str = "cuda", chunk: int = 2048,
-                       ld_rho: float = 0.0, ld_block: int = 50):
+                       ld_rho: float = 0.0, ld_block: int = 50, n_traits: int = 1,
+                       rows_device: bool = False):
     """Device-side generator for benchmark-sized inputs (same model as the NumPy path, torch's
     RNG): returns (.bed rows as a pinned host uint8 tensor m×ceil(n/4), y float32 numpy).
     With ``ld_rho > 0`` the genotypes of each block of ``ld_block`` SNPs come from an AR(1)
     latent Gaussian along the SNPs, thresholded at the Binomial(2, p_j) quantiles.
+    ``n_traits > 1`` draws that many phenotypes, each with its own causal SNPs and effects (y is
+    then n × n_traits); ``rows_device`` keeps the rows in device memory.  With the defaults the
+    random stream is that of the single-trait generator.
     Torch is used only as a random-number and memory utility here."""
     import torch
     if ld_rho > 0.0:   # whole LD blocks per chunk, ≈1 GB of latent values at a time
@@ -127,14 +131,21 @@ def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal:
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
     nb = (n + 3) // 4
-    rows = torch.empty((m, nb), dtype=torch.uint8, pin_memory=torch.cuda.is_available())
+    if rows_device:
+        rows = torch.empty((m, nb), dtype=torch.uint8, device=device)
+    else:
+        rows = torch.empty((m, nb), dtype=torch.uint8, pin_memory=torch.cuda.is_available())
     p = torch.rand(m, generator=gen, device=device, dtype=torch.float64) * 0.45 + 0.05
     code_of = torch.tensor([0b00, 0b10, 0b11], dtype=torch.uint8, device=device)
-    causal = torch.randperm(m, generator=gen, device=device)[: min(n_causal, m)]
-    causal_sorted, _ = torch.sort(causal)
-    beta = torch.randn(causal_sorted.numel(), generator=gen, device=device, dtype=torch.float64) * \
-        (h2 / max(causal_sorted.numel(), 1)) ** 0.5
-    g = torch.zeros(n, dtype=torch.float64, device=device)
+    causal_t, beta_t = [], []
+    for _ in range(max(1, n_traits)):
+        causal = torch.randperm(m, generator=gen, device=device)[: min(n_causal, m)]
+        causal_sorted, _ = torch.sort(causal)
+        beta = torch.randn(causal_sorted.numel(), generator=gen, device=device, dtype=torch.float64) * \
+            (h2 / max(causal_sorted.numel(), 1)) ** 0.5
+        causal_t.append(causal_sorted)
+        beta_t.append(beta)
+    gt = torch.zeros((len(causal_t), n), dtype=torch.float64, device=device)
     shifts = torch.tensor([0, 2, 4, 6], dtype=torch.uint8, device=device)
     for j0 in range(0, m, chunk):
         j1 = min(m, j0 + chunk)
@@ -154,12 +165,13 @@ def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal:
             u1 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
             u2 = torch.rand((j1 - j0, n), generator=gen, device=device, dtype=torch.float32)
             cnt = (u1 < pj).to(torch.uint8) + (u2 < pj).to(torch.uint8)       # Binomial(2, p)
-        sel = (causal_sorted >= j0) & (causal_sorted < j1)
-        if bool(sel.any()):
-            idx = causal_sorted[sel] - j0
-            x = cnt[idx].to(torch.float64)
-            sd = x.std(dim=1, unbiased=False).clamp_min(1e-12)
-            g += (beta[sel, None] * (x - x.mean(dim=1, keepdim=True)) / sd[:, None]).sum(0)
+        for t, (causal_sorted, beta) in enumerate(zip(causal_t, beta_t)):
+            sel = (causal_sorted >= j0) & (causal_sorted < j1)
+            if bool(sel.any()):
+                idx = causal_sorted[sel] - j0
+                x = cnt[idx].to(torch.float64)
+                sd = x.std(dim=1, unbiased=False).clamp_min(1e-12)
+                gt[t] += (beta[sel, None] * (x - x.mean(dim=1, keepdim=True)) / sd[:, None]).sum(0)
         codes = code_of[cnt.long()]
         if missing > 0:
             miss = torch.rand((j1 - j0, n), generator=gen, device=device) < missing
@@ -168,6 +180,8 @@ def simulate_bed_torch(n: int, m: int, seed: int = 1, h2: float = 0.4, n_causal:
         pad[:, :n] = codes
         packed = (pad.view(j1 - j0, nb, 4) << shifts).sum(dim=2, dtype=torch.uint8)
         rows[j0:j1].copy_(packed, non_blocking=False)
-    e = torch.randn(n, generator=gen, device=device, dtype=torch.float64) * (1.0 - h2) ** 0.5
-    y = (g + e).float().cpu().numpy()
-    return rows, y
+    ys = []
+    for t in range(gt.shape[0]):
+        e = torch.randn(n, generator=gen, device=device, dtype=torch.float64) * (1.0 - h2) ** 0.5
+        ys.append((gt[t] + e).float().cpu().numpy())
+    return rows, (ys[0] if n_traits <= 1 else np.stack(ys, axis=1))

@@ -127,8 +127,9 @@ def test_operator_determinism(gpu):
 
 @pytest.mark.parametrize("n_fam,m", [(1001, 257), (130, 5), (4099, 300), (2048, 384)])
 def test_tiled_pack_matches_subset_pack(gpu, n_fam, m):
-    """The tiled whole-matrix pack (no individual subset) and the subset pack with the identity
-    subset build the same tiles: operator outputs agree bit for bit in both directions."""
+    """The tiled pack's row-contiguous reads (no individual subset) and its keep-list gather with
+    the identity subset build the same tiles: counts and operator outputs agree bit for bit in
+    both directions."""
     rows, _, dec = make_case(n_fam, m, seed=23, missing=0.02)
     n = dec.shape[1]
     pc = orc.popcounts(dec)

@@ -92,6 +92,31 @@ def test_sldf_reml_vs_oracle(gpu, prec):
     assert abs(r["lrt"] - r64["lrt"]) <= 1e-2 * max(1.0, abs(r64["lrt"]))
 
 
+def test_per_trait_individual_sets_vs_oracle(gpu):
+    """Several traits with their own missing individuals (5 %, 20 %, 40 %) from one set of .bed
+    rows held in device memory: each trait's handle is packed for its individuals (the reference
+    analyses each trait on its own individual set, src/input.cpp:287, src/option.cpp:320), so
+    its counts, means and fit equal the oracle's on that subset."""
+    import torch
+    n_fam, m = 1600, 1500
+    counts, _ = synth.simulate_counts(n_fam, m, seed=43)
+    rows_dev = torch.from_numpy(synth.encode_bed(counts)).cuda()
+    rng = np.random.default_rng(43)
+    persnp = np.ones(m, np.float32)
+    for t, frac in enumerate((0.05, 0.2, 0.4)):
+        keep = np.sort(rng.choice(n_fam, size=n_fam - int(frac * n_fam), replace=False)).astype(np.int64)
+        ct = np.ascontiguousarray(counts[:, keep])
+        y, _, _ = synth.simulate_phenotype(ct, 0.5, n_causal=150, seed=100 + t)
+        y = y.astype(np.float32)
+        X = np.column_stack([np.ones(keep.size), rng.standard_normal(keep.size)]).astype(np.float32)
+        r64 = orc.SLDF_REML(ct, None, X, y, persnp, seed=3, n_V=12, dtype=np.float64)
+        with api.Genotypes(rows_dev, n_fam, keep_idx=keep) as g:
+            assert np.array_equal(g.counts()[0], orc.popcounts(ct))
+            r = g.SLDF_REML(None, X, y, persnp, seed=3, n_V=12)
+        assert abs(r["h2"] - r64["h2"]) <= 2e-4
+        assert np.corrcoef(r["snp_blup"], r64["snp_blup"])[0, 1] >= 0.99999
+
+
 def test_lmc_reml_vs_oracle(gpu):
     counts, rows, y, rvec, X, persnp = _problem(seed=37, h2=0.4)
     n = counts.shape[1]
