@@ -1,0 +1,66 @@
+"""Host-side inputs of the benchmark workloads, checked on CPU: the per-trait individual sets of
+the multi-trait workload, the windows of the gradient workload and the synthetic generator's
+multi-trait option (whose single-trait random stream must stay that of the other workloads)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+from slemm_gb300 import synth  # noqa: E402
+
+
+def test_trait_individual_sets():
+    cfg = dict(bench.CONFIGS[5], n=20000)
+    keeps, frac = bench.trait_keeps(cfg)
+    assert len(keeps) == cfg["traits"] == len(frac)
+    assert frac[0] == pytest.approx(cfg["miss_lo"]) and frac[-1] == pytest.approx(cfg["miss_hi"])
+    for k, f in zip(keeps, frac):
+        assert k.dtype == np.int64
+        assert k.size == cfg["n"] - int(round(f * cfg["n"]))
+        assert np.all(np.diff(k) > 0)                 # sorted, no repeats
+        assert k[0] >= 0 and k[-1] < cfg["n"]
+    again, _ = bench.trait_keeps(cfg)                 # seeded: every run analyses the same sets
+    assert all(np.array_equal(a, b) for a, b in zip(keeps, again))
+
+
+def test_gradient_windows():
+    cfg = bench.CONFIGS[4]
+    window, wwin = bench.grad_inputs(cfg)
+    assert window.shape == (cfg["m"],) and window.dtype == np.int32
+    assert window.min() == 0 and window.max() == cfg["grad_windows"] - 1
+    assert np.all(np.diff(window) >= 0)
+    assert np.all(np.bincount(window) == cfg["m"] // cfg["grad_windows"])   # 50 SNPs each
+    assert wwin.shape == (cfg["grad_windows"],)
+    assert np.all(wwin > 0) and np.all(wwin <= 2)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(missing=0.02), dict(ld_rho=0.6, ld_block=25)])
+def test_generator_traits_option(kw):
+    torch = pytest.importorskip("torch")
+    rows1, y1 = synth.simulate_bed_torch(600, 140, seed=5, device="cpu", chunk=64, **kw)
+    rowsT, yT = synth.simulate_bed_torch(600, 140, seed=5, device="cpu", chunk=64, n_traits=3,
+                                         rows_device=True, **kw)
+    assert y1.shape == (600,) and yT.shape == (600, 3)
+    assert isinstance(rowsT, torch.Tensor) and rowsT.shape == rows1.shape
+    # each trait has its own causal SNPs: the phenotypes are far from collinear
+    c = np.corrcoef(yT.T)
+    assert np.all(np.abs(c[np.triu_indices(3, 1)]) < 0.5)
+    # the .bed rows decode to valid codes only (no 01 unless missing calls were asked for)
+    codes = np.unpackbits(rowsT.numpy()[:, :, None], axis=2, bitorder="little").reshape(140, -1, 2)
+    codes = codes[:, :600]
+    if not kw.get("missing"):
+        assert not np.any((codes[..., 0] == 1) & (codes[..., 1] == 0))
+
+
+def test_generator_single_trait_stream_is_stable():
+    """n_traits = 1 is the default call: the same draws in the same order, so the single-trait
+    workloads keep their genotypes and phenotypes."""
+    pytest.importorskip("torch")
+    rows, y = synth.simulate_bed_torch(300, 90, seed=3, device="cpu", chunk=32)
+    rows2, y2 = synth.simulate_bed_torch(300, 90, seed=3, device="cpu", chunk=32, n_traits=1)
+    assert np.array_equal(rows.numpy(), rows2.numpy()) and np.array_equal(y, y2)
