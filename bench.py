@@ -942,13 +942,14 @@ def _traffic(dom, n, m):
 
 def run_kernel_case(args):
     """Small profiling case for ncu: n = 40,000, m = 20,000 (each packed copy 200 MB, above the
-    129 MB L2), H0_ldet_mv on a 65-column block: 3 warm-up applications, then 2 timed (each is
-    one Zᵀ and one Z pass, i.e. 2 gemm_tc_kernel launches)."""
+    129 MB L2), H0_ldet_mv on a block of --kernel-k columns (65: the wide kernel at N = 144;
+    1: the narrow one at N = 16): 3 warm-up applications, then 2 timed (each is one Zᵀ and one Z
+    pass, i.e. 2 gemm_tc_kernel launches)."""
     import torch
     from slemm_gb300 import api, _lib, synth
     torch.cuda.set_device(0)
     api.init(0)
-    n, m, k = 40000, 20000, 65
+    n, m, k = 40000, 20000, args.kernel_k
     rows, _ = synth.simulate_bed_torch(n, m, seed=3)
     rows_np = rows.numpy()
     g = api.Genotypes(rows_np, n)
@@ -978,6 +979,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel-case", action="store_true", help="small operator case for ncu captures")
     ap.add_argument("--kernel-prec", type=int, default=2, choices=[2, 3])
+    ap.add_argument("--kernel-k", type=int, default=65, help="columns of the kernel case's block")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
