@@ -24,7 +24,9 @@ struct slemm_geno {
   slemm::DevBuf err;              // int error word of the kernels' bounded waits (zeroed at create)
   slemm::HostScal scal;           // mapped host scalars of the Lanczos steps
   // per-SNP class counts n1, n2 in device memory ([2][m_pad] int32), summed by the pack kernel
-  // while it builds the tiles (whole-matrix packs only; `dcounts_valid` says whether they exist)
+  // while it builds the tiles (every handle genotype_create packs; a copy derived from another
+  // handle's tiles, like slemm_gwa's model-SNP copy, has none and counts its tiles instead —
+  // `dcounts_valid` says which)
   slemm::DevBuf dcounts;
   bool dcounts_valid = false;
   // Z_cᵀ1 per SNP, pc_j − n·gm_j (FP64, stored FP32): the exact product of the centred matrix
