@@ -1,8 +1,8 @@
-"""Builds libslemm_gb300.so (and the `slemm` command-line tool) in-tree for sm_103a.
+"""Builds libslemm_gb300.so in-tree for sm_103a.
 
 Every translation unit under csrc/ is compiled by nvcc in parallel into _build/, then linked
-into lib/libslemm_gb300.so; cli/*.cpp are linked into bin/slemm against that library.
-Incremental: a unit is rebuilt only when it or a header is newer than its object.
+into lib/libslemm_gb300.so.  Incremental: a unit is rebuilt only when it or a header is newer
+than its object.
 """
 from __future__ import annotations
 
@@ -16,10 +16,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-CLI = os.path.join(HERE, "cli")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libslemm_gb300.so")
-BIN = os.path.join(HERE, "bin", "slemm")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -74,15 +72,6 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    cli_srcs = sorted(glob.glob(os.path.join(CLI, "*.cpp")))
-    if cli_srcs and _stale(BIN, cli_srcs + [LIB] + _headers()):
-        os.makedirs(os.path.dirname(BIN), exist_ok=True)
-        cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), *cli_srcs,
-               "-o", BIN, "-L" + os.path.dirname(LIB), "-lslemm_gb300",
-               "-Wl,-rpath,$ORIGIN/../lib", "-lpthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
