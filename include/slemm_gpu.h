@@ -74,7 +74,10 @@ int64_t slemm_gpu_launch_count(void);
  * bed_rows: host pointer to m SNP-major .bed rows (magic bytes already skipped), row j at
  *   bed_rows + j*row_stride, each row ceil(n_fam/4) bytes, selected SNPs in analysis order.
  * keep_idx: host pointer to n indices into [0, n_fam) of the individuals kept, in order
- *   (NULL = all n_fam individuals; then n must equal n_fam).
+ *   (NULL = all n_fam individuals; then n must equal n_fam).  The handle's counts, allele
+ *   frequencies and centring are those of the kept individuals, so several traits with their
+ *   own individual sets take one handle each, all packed from the same rows (with
+ *   SLEMM_ROWS_DEVICE, straight from device memory).  n_fam and m must be below 2^31.
  * Codes follow PLINK: 00→0, 10(het)→1, 11→2, 01(missing)→1 allele-2 copies, exactly like the
  * reference's bit decode (missing counts as one copy).  The handle keeps two packed 2-bit
  * copies (SNP-major and individual-major) in HBM.  flags: 0, or SLEMM_ROWS_DEVICE when bed_rows
