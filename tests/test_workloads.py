@@ -64,3 +64,29 @@ def test_generator_single_trait_stream_is_stable():
     rows, y = synth.simulate_bed_torch(300, 90, seed=3, device="cpu", chunk=32)
     rows2, y2 = synth.simulate_bed_torch(300, 90, seed=3, device="cpu", chunk=32, n_traits=1)
     assert np.array_equal(rows.numpy(), rows2.numpy()) and np.array_equal(y, y2)
+
+
+def test_roofline_object_arithmetic():
+    """The bench's roofline object for one packed-product launch shape: algorithmic FLOPs per
+    launch over the measured launch time, against the measured BF16 peak (and the hi+lo ceiling,
+    half of it), and the per-launch DRAM traffic scaled from the committed ncu summary."""
+    n, m = 100000, 50000
+    prof = [{"tc": 1, "N": 144, "k": 66, "pieces": 2, "dir": 2, "launches": 10, "ms": 7.2},
+            {"tc": 1, "N": 16, "k": 1, "pieces": 2, "dir": 1, "launches": 1, "ms": 0.58}]
+    roof, gbs = bench.roofline(prof, n, m)
+    pk = bench.peaks()
+    t = 7.2e-3 / 10
+    flops = 2.0 * n * m * 66
+    assert roof["bound"] == "tensor" and roof["unit"] == "TFLOP/s"
+    assert roof["achieved"] == pytest.approx(flops / t / 1e12)
+    assert roof["peak"] == pytest.approx(pk["bf16"])
+    assert roof["frac"] == pytest.approx(roof["achieved"] / pk["bf16"])
+    assert roof["frac_eff"] == pytest.approx(2 * roof["frac"])
+    assert roof["executed_tflops"] == pytest.approx(2.0 * n * m * 144 / t / 1e12)
+    assert gbs == pytest.approx(m * ((n + 3) // 4) / t / 1e9)
+    # traffic: the committed per-launch figure of this shape at this size
+    import json
+    with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+        tr = json.load(f)
+    assert roof["traffic"] == pytest.approx(tr["tc1_N144_dir2"])
+    assert bench.roofline([], n, m) == (None, None)
