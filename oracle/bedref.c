@@ -30,6 +30,30 @@ void oracle_bed_decode(const uint8_t* rows, int64_t m, int64_t n_fam, int64_t ro
   }
 }
 
+/* src/reml.cpp:28-35 (and 136-142, 174-181, 212-219) — one SNP subset of the reference's
+ * operator loop: kmat bits of SNPs j … j+m−1 (all individuals) decoded to the FP32 column
+ * count − gm (b[k] + b[k+1] − gm, the missing code counting 1), written row-major as m rows of n
+ * floats (the subset matrix the reference's SGEMMs read).  Used by the timed CPU baseline. */
+void oracle_decode_centred_f32(const uint8_t* rows, int64_t m, int64_t n, int64_t row_bytes,
+                               const float* gm, float* out)
+{
+  for (int64_t j = 0; j < m; ++j) {
+    const uint8_t* r = rows + j * row_bytes;
+    float* o = out + j * n;
+    const float g = gm[j];
+    const float v[4] = {0.0f - g, 1.0f - g, 1.0f - g, 2.0f - g};   /* by 2-bit code */
+    const int64_t full = n >> 2;
+    for (int64_t b = 0; b < full; ++b) {
+      const unsigned byte = r[b];
+      o[4 * b + 0] = v[byte & 3u];
+      o[4 * b + 1] = v[(byte >> 2) & 3u];
+      o[4 * b + 2] = v[(byte >> 4) & 3u];
+      o[4 * b + 3] = v[(byte >> 6) & 3u];
+    }
+    for (int64_t i = full * 4; i < n; ++i) o[i] = v[(r[i >> 2] >> (2 * (i & 3))) & 3u];
+  }
+}
+
 /* src/reml.cpp:613-621 (and weight.cpp:7-12) — number of set kmat bits per SNP row. */
 void oracle_popcounts(const uint8_t* counts, int64_t m, int64_t n, int64_t* pc)
 {

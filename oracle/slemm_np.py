@@ -39,6 +39,7 @@ def _lib():
             I64 = ctypes.c_int64
             lib.oracle_bed_decode.argtypes = [P, I64, I64, I64, P, P, I64]
             lib.oracle_popcounts.argtypes = [P, I64, I64, P]
+            lib.oracle_decode_centred_f32.argtypes = [P, I64, I64, I64, P, P]
             lib.oracle_hwe_counts.argtypes = [P, I64, I64, P, P, P]
             lib.oracle_lmm_variants.argtypes = [P, I64, I64, ctypes.c_int, P]
             lib.oracle_lmm_variants.restype = ctypes.c_int
@@ -283,41 +284,70 @@ class Operators:
 class PackedOperators(Operators):
     """Same operators, decoding each `subset_size` block straight from the packed .bed rows of
     the kept individuals (all individuals here), as the reference decodes kmat bits per subset
-    (src/reml.cpp:29-35) — used for the timed CPU baseline at full sizes."""
+    (src/reml.cpp:29-35) — used for the timed CPU baseline at full sizes.  The decode runs in the
+    oracle's C restatement over `threads` host threads (ctypes releases the GIL) into one reused
+    FP32 subset buffer, and the two products per subset are OpenBLAS SGEMMs, the structure of the
+    reference's OpenMP decode + MKL SGEMM loop."""
 
-    def __init__(self, bed_rows, n, gm, w, rr=None, Q=None, subset_size=1000, dtype=np.float32):
-        self.rows = bed_rows
-        self.m, self.n = bed_rows.shape[0], n
+    def __init__(self, bed_rows, n, gm, w, rr=None, Q=None, subset_size=1000, dtype=np.float32, threads=None):
+        self.rows = np.ascontiguousarray(bed_rows, dtype=np.uint8)
+        self.m, self.n = self.rows.shape[0], n
         self.dt = dtype
         self.gm = np.asarray(gm, dtype=dtype)
         self.w = np.asarray(w, dtype=dtype)
         self.rr = np.ones(n, dtype) if rr is None else np.asarray(rr, dtype=dtype)
         self.Q = np.zeros((n, 0), dtype) if Q is None else np.asarray(Q, dtype=dtype)
         self.s = int(subset_size)
-        # byte → 4 counts LUT (missing code 01 → 1, like b[k]+b[k+1])
-        codes = (np.arange(256)[:, None] >> np.array([0, 2, 4, 6])) & 3
-        self._lut4 = ((codes & 1) + (codes >> 1)).astype(dtype)
+        self.threads = max(1, int(threads or os.cpu_count() or 1))
         self.subset_limit = None
+        self._buf = None
+
+    def _decode(self, i0, i1):
+        """(i1 − i0) × n FP32 rows count − gm of SNPs i0 … i1−1."""
+        if self.dt != np.float32:
+            raise TypeError("the packed C decode writes FP32")
+        need = (i1 - i0) * self.n
+        if self._buf is None or self._buf.size < need:
+            self._buf = np.empty(need, np.float32)
+        out = self._buf[:need].reshape(i1 - i0, self.n)
+        gm = np.ascontiguousarray(self.gm[i0:i1], np.float32)
+        rb = self.rows.shape[1]
+        lib = _lib()
+        chunks = [c for c in np.array_split(np.arange(i0, i1), self.threads) if c.size]
+
+        def work(c):
+            a, b = int(c[0]), int(c[-1]) + 1
+            lib.oracle_decode_centred_f32(_p(self.rows[a:b]), b - a, self.n, rb, _p(gm[a - i0:b - i0]),
+                                          _p(out[a - i0:b - i0]))
+
+        if len(chunks) == 1:
+            work(chunks[0])
+        else:
+            from concurrent.futures import ThreadPoolExecutor
+            with ThreadPoolExecutor(len(chunks)) as ex:
+                list(ex.map(work, chunks))
+        return out
 
     def _subsets(self):
-        nb = (self.n + 3) // 4
         count = 0
         for i0 in range(0, self.m, self.s):
             if self.subset_limit is not None and count >= self.subset_limit:
                 return
             i1 = min(self.m, i0 + self.s)
-            blk = np.asarray(self.rows[i0:i1, :nb])
-            Zc = self._lut4[blk].reshape(i1 - i0, nb * 4)[:, : self.n].T - self.gm[i0:i1]
             count += 1
-            yield i0, i1, Zc
+            yield i0, i1, self._decode(i0, i1).T   # n × s view, (count − gm)
 
 
 # ------------------------------------------------------------------------------------------
 # Lanczos seed / solve / SLQ (src/reml.cpp:240-451)
 # ------------------------------------------------------------------------------------------
-def L_Seed(ops: Operators, lnr, tau0, B, tol=5e-4, maxit=600):
+def L_Seed(ops: Operators, lnr, tau0, B, tol=5e-4, maxit=600, reorth=False):
     """src/reml.cpp:246-339 — per-column Lanczos with CG coefficients; returns the basis U
-    (list of n×t), beta (t×(j+1)), delta (t×j) and the step count j."""
+    (list of n×t), beta (t×(j+1)), delta (t×j) and the step count j.
+
+    reorth=True restates the engine's opt-in mode (not in the reference): after the three-term
+    update each new vector loses its components along every stored vector of its column
+    (one classical Gram–Schmidt pass, coefficients U_iᵀw from the vector before the pass)."""
     dt = ops.dt
     B = np.asarray(B, dt).reshape(ops.n, -1)
     n, t = B.shape
@@ -337,6 +367,10 @@ def L_Seed(ops: Operators, lnr, tau0, B, tol=5e-4, maxit=600):
             tmp = tmp - U[j - 1] * beta[:, j]
         delta[:, j] = (U[j] * tmp).sum(axis=0, dtype=dt)
         tmp = tmp - U[j] * delta[:, j]
+        if reorth:
+            Ub = np.stack(U)                                   # (j+1)×n×t
+            d = np.einsum("inc,nc->ic", Ub, tmp)               # U_i[:,c]ᵀ w[:,c]
+            tmp = tmp - np.einsum("ic,inc->nc", d, Ub)
         beta[:, j + 1] = np.sqrt((tmp * tmp).sum(axis=0, dtype=dt))
         U.append(tmp / beta[:, j + 1])
         if j == 0:
@@ -437,14 +471,33 @@ def REML_criterion(ss, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, ySy):
     tau = (1 - ss) / ss
     sigma = tau - tau0
     yPy = float(y_proj @ L_Solve(seed_y, y_proj, sigma)[:, 0])
+    M = Q.T @ L_Solve(seed_Q, Q, sigma)
+    logdet = float(np.linalg.slogdet(np.asarray(M, np.float64))[1])
+    if y_proj.dtype == np.float32:
+        # The reference's criterion keeps yPy, v_g, v_e, ldet_H, lrt and slogLL in float
+        # variables; its `log` of a float quotient is the C library's double log
+        # (src/reml.cpp:470-488), each expression rounded once on assignment.
+        f32 = np.float32
+        ySy32, yPy32 = f32(ySy), f32(yPy)
+        v_g = float(f32(yPy32 / f32(n - c)))
+        v_e = float(f32(f32(v_g) * f32(tau)))
+        ldet_H = float(f32(SLQ_LDet(D_V, W_V, n, D_V.shape[0], sigma)))
+        lq = math.log(float(ySy32 / yPy32))
+        lrt = float(f32(n * lq - ldet_H))
+        slogLL = float(f32((n - c) * lq - float(f32(logdet)) - ldet_H))
+        return slogLL, v_g, v_e, lrt
     v_g = yPy / (n - c)
     v_e = v_g * tau
     ldet_H = SLQ_LDet(D_V, W_V, n, D_V.shape[0], sigma)
     lrt = n * math.log(ySy / yPy) - ldet_H
-    M = Q.T @ L_Solve(seed_Q, Q, sigma)
-    logdet = float(np.linalg.slogdet(np.asarray(M, np.float64))[1])
     slogLL = (n - c) * math.log(ySy / yPy) - logdet - ldet_H
     return slogLL, v_g, v_e, lrt
+
+
+def gss_point(a, k, h):
+    """float(a + k·h) with a, h float32 and k a double constant: the double sum rounded once to
+    float32, as the reference's `c = a + invphi2 * h;` does (src/reml.cpp:520-521)."""
+    return np.float32(float(a) + k * float(h))
 
 
 def REML_GSS(a, b, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, tol, log=None):
@@ -456,9 +509,13 @@ def REML_GSS(a, b, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, tol, log=None):
     ySy = float(np.dot(y_proj, y_proj))
     a, b = f32(a), f32(b)
     h = f32(b - a)
-    nitr = 1 if h < tol else int(math.ceil(math.log(f32(tol) / h) / math.log(invphi)))
-    c = f32(a + invphi2 * h)
-    d = f32(a + invphi * h)
+    # The reference's points and steps mix float operands with double constants
+    # (`c = a + invphi2 * h;`, `h *= invphi;`, src/reml.cpp:520-540): C++ promotes to double,
+    # evaluates there and rounds once on assignment to float.  NumPy 2 keeps a float32 times a
+    # Python float in float32, so each operand is taken to a Python float (double) first.
+    nitr = 1 if h < tol else int(math.ceil(math.log(float(f32(tol) / h)) / math.log(invphi)))
+    c = gss_point(a, invphi2, h)
+    d = gss_point(a, invphi, h)
     evals = []
     fc, vg, ve, lrt = REML_criterion(c, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, ySy)
     fd, vg, ve, lrt = REML_criterion(d, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, ySy)
@@ -466,14 +523,14 @@ def REML_GSS(a, b, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, tol, log=None):
     for _ in range(nitr):
         if fc > fd:
             b, d, fd = d, c, fc
-            h = f32(h * invphi)
-            c = f32(a + invphi2 * h)
+            h = f32(float(h) * invphi)
+            c = gss_point(a, invphi2, h)
             fc, vg, ve, lrt = REML_criterion(c, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, ySy)
             evals.append((c, fc))
         else:
             a, c, fc = c, d, fd
-            h = f32(h * invphi)
-            d = f32(a + invphi * h)
+            h = f32(float(h) * invphi)
+            d = gss_point(a, invphi, h)
             fd, vg, ve, lrt = REML_criterion(d, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, ySy)
             evals.append((d, fd))
     if log is not None:
@@ -482,9 +539,9 @@ def REML_GSS(a, b, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, tol, log=None):
 
 
 def SLDF_REML(counts, rvec, X, y, persnp, seed=0, n_V=30, tol_L=5e-4, s2max=0.7, s2min=1e-4,
-              tol_VC=1e-4, subset_size=1000, dtype=np.float32, maxit=600):
+              tol_VC=1e-4, subset_size=1000, dtype=np.float32, maxit=600, reorth=False):
     """src/reml.cpp:549-690 — DF-REML; returns a dict with vg, ve, h2, lrt, Py, snp_blup, blue,
-    var_blue and the Lanczos step counts."""
+    var_blue and the Lanczos step counts.  reorth: the engine's opt-in reorthogonalised seeds."""
     dt = dtype
     n = y.size
     rvec = np.ones(n) if rvec is None else rvec
@@ -501,9 +558,9 @@ def SLDF_REML(counts, rvec, X, y, persnp, seed=0, n_V=30, tol_L=5e-4, s2max=0.7,
     gw = snp_weights(gm, persnp, dt)
     ops = Operators(counts, gm, gw, rr, Q, subset_size, dt)
     tau0 = (1 - np.float32(s2max)) / np.float32(s2max)
-    seed_y = L_Seed(ops, "quadform", tau0, y_proj, tol_L, maxit)
-    seed_Q = L_Seed(ops, "ldet", tau0, Q, tol_L, maxit)
-    seed_V = L_Seed(ops, "ldet", tau0, V, tol_L, maxit)
+    seed_y = L_Seed(ops, "quadform", tau0, y_proj, tol_L, maxit, reorth)
+    seed_Q = L_Seed(ops, "ldet", tau0, Q, tol_L, maxit, reorth)
+    seed_V = L_Seed(ops, "ldet", tau0, V, tol_L, maxit, reorth)
     D_V, W_V = jacobi_eig(seed_V)
     log = []
     vg, ve, lrt = REML_GSS(s2min, s2max, tau0, y_proj, seed_y, Q, seed_Q, D_V, W_V, tol_VC, log)
@@ -544,7 +601,7 @@ def REML_first_order(ops: Operators, ss, tau0, V, seed_V, gw):
 
 
 def LMC_REML(counts, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, s2min=1e-4,
-             subset_size=1000, dtype=np.float32, maxit=600):
+             subset_size=1000, dtype=np.float32, maxit=600, reorth=False):
     """src/reml.cpp:730-883 — MC-REML with secant iterations on log((1−h²)/h²)."""
     dt = dtype
     n = y.size
@@ -568,7 +625,7 @@ def LMC_REML(counts, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, 
     V[:, :1 + n_MC] *= rr[:, None]
     V = ops._proj(V)
     tau0 = (1 - np.float32(s2max)) / np.float32(s2max)
-    seed_V = L_Seed(ops, "quadform", tau0, V, 10 * np.float32(tol_L), maxit)
+    seed_V = L_Seed(ops, "quadform", tau0, V, 10 * np.float32(tol_L), maxit, reorth)
     s2 = np.float32(s2max) / 2
     log_tau1 = np.float32(math.log((1 - s2) / s2))
     f1, PyMC = REML_first_order(ops, s2, tau0, V, seed_V, gw)
@@ -829,7 +886,7 @@ def clump_fixed_snps(counts, snpvar, sig_chisq, indep_r2):
 
 def REML_iter_weighting(counts, rvec, X, y, persnp, maf_vals, lrt=True, seed=0, n_V=30, n_MC=None,
                         n_MC_final=None, tol_L=5e-4, s2max=0.7, window_size=20, sig_chisq=1e6,
-                        indep_r2=0.5, dtype=np.float32):
+                        indep_r2=0.5, dtype=np.float32, reorth=False):
     """src/option.cpp:437-530 — equal-weight GREML (DF-REML when --lrt and n < 5000, else MC-REML),
     per-SNP variance 2·maf(1−maf)·b² normalised to mean 1, fixed-effect SNPs by clumping, window
     weights, then the window-weighted GREML with those SNPs as covariates; their SNP-BLUP entries
@@ -841,9 +898,11 @@ def REML_iter_weighting(counts, rvec, X, y, persnp, maf_vals, lrt=True, seed=0, 
     n_MC_final = n_MC if n_MC_final is None else n_MC_final
     ones = np.ones(m, f32)
     if lrt and n < 5000:
-        r1 = SLDF_REML(counts, rvec, X, y, ones, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype)
+        r1 = SLDF_REML(counts, rvec, X, y, ones, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype,
+                       reorth=reorth)
     else:
-        r1 = LMC_REML(counts, rvec, X, y, ones, seed=seed, n_MC=n_MC, tol_L=tol_L, s2max=s2max, dtype=dtype)
+        r1 = LMC_REML(counts, rvec, X, y, ones, seed=seed, n_MC=n_MC, tol_L=tol_L, s2max=s2max, dtype=dtype,
+                      reorth=reorth)
     snpvar, _ = window_weights(maf_vals, r1["snp_blup"], window_size)
     sig, Xs = clump_fixed_snps(counts, snpvar, sig_chisq, indep_r2)
     _, w = window_weights(maf_vals, r1["snp_blup"], window_size, sig)
@@ -851,10 +910,11 @@ def REML_iter_weighting(counts, rvec, X, y, persnp, maf_vals, lrt=True, seed=0, 
     p2 = (p2 / f32(p2.astype(np.float64).mean())).astype(f32)
     X2 = np.column_stack([np.asarray(X, f32).reshape(n, -1), Xs])
     if lrt:
-        r2 = SLDF_REML(counts, rvec, X2, y, p2, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype)
+        r2 = SLDF_REML(counts, rvec, X2, y, p2, seed=seed, n_V=n_V, tol_L=tol_L, s2max=s2max, dtype=dtype,
+                       reorth=reorth)
     else:
         r2 = LMC_REML(counts, rvec, X2, y, p2, seed=seed, n_MC=n_MC_final, tol_L=tol_L, s2max=s2max,
-                      dtype=dtype)
+                      dtype=dtype, reorth=reorth)
     c = np.asarray(X).reshape(n, -1).shape[1]
     blup = np.asarray(r2["snp_blup"], f32).copy()
     for i, j in enumerate(sig):
