@@ -50,6 +50,8 @@ extern "C" {
 #define SLEMM_PREC_FP32    0  /* CUDA-core FP32 FMA on exact integer counts                      */
 #define SLEMM_PREC_BF16X2  1  /* tcgen05 BF16 MMA, dense side split hi+lo, FP32 accumulation     */
 #define SLEMM_PREC_BF16X3  2  /* tcgen05 BF16 MMA, dense side split hi+mid+lo (≈FP32 mantissa)   */
+#define SLEMM_PREC_FP16X2  3  /* tcgen05 FP16 MMA, dense side scaled by a power of two per column
+                                 and split hi+lo (22 mantissa bits) at the cost of hi+lo BF16     */
 
 /* ---- memory location flags ---------------------------------------------------------------- */
 #define SLEMM_MEM_HOST     0
@@ -131,6 +133,18 @@ int slemm_gpu_op(slemm_geno* g, int op_kind, float tau0, const float* in, int64_
                  float* out, int64_t ld_out, int mem);
 
 /* ---- Lanczos seed / shifted solves (src/reml.cpp:246-431) ------------------------------- */
+/* Lanczos mode of a handle (bits; 0, the default, is the reference's recurrence):
+ * SLEMM_LANCZOS_REORTH  each new basis vector is made orthogonal to every stored vector of its
+ *                       column (classical Gram-Schmidt with FP64-accurate coefficients over the FP32
+ *                       basis in HBM; two passes over the stored basis per step).  The reference
+ *                       runs the plain three-term recurrence (src/reml.cpp:293-322), which on
+ *                       ill-conditioned systems (window-weighted GREML) needs more steps and stops
+ *                       at a step that depends on rounding.
+ * The mode applies to every seed run on the handle afterwards (L_Seed, the REML drivers, the
+ * gradient, --lmm, --iter_weighting). */
+#define SLEMM_LANCZOS_REORTH 1
+int slemm_gpu_set_lanczos(slemm_geno* g, int mode);
+
 /* Runs the per-column Lanczos/CG recurrence on B (n×t) with operator op_kind (QUADFORM or LDET)
  * at shift tau0 until max_col |ρ|·‖u‖/‖b‖ ≤ tol or maxit, storing the basis in HBM.  The
  * recurrence scalars are accumulated in FP64.  *iters receives the number of steps j. */
@@ -170,6 +184,7 @@ typedef struct {
   int   verbose;    /* print the reference's progress lines to stdout                      */
 } slemm_reml_opts;
 
+#define SLEMM_TRACE_MAX 64
 typedef struct {
   float vg, ve, h2, lrt;  /* variance components, h2 = vg/(vg+ve), LRT (SLDF only, else 0) */
   int   iters_y, iters_Q, iters_V;   /* Lanczos steps per seed system                     */
@@ -179,6 +194,13 @@ typedef struct {
   double t_seed;          /* Lanczos recurrence (operator applications)                    */
   double t_search;        /* golden-section or secant search on h2                         */
   double t_final;         /* BLUP, BLUE and copies back                                    */
+  /* The search's evaluations in order (the first SLEMM_TRACE_MAX): h2 of each point and its
+   * criterion — 2logLL of the golden-section search (src/reml.cpp:512-541) or the first-order
+   * function of the secant iterations (src/reml.cpp:821-851).  Two runs took the same branches
+   * exactly when their h2_points agree. */
+  int    n_points;
+  float  h2_points[SLEMM_TRACE_MAX];
+  double f_points[SLEMM_TRACE_MAX];
 } slemm_reml_result;
 
 /* DF-REML with Rademacher probes + golden-section search (src/reml.cpp:549-690).
@@ -284,8 +306,11 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
  * nothing and returns without synchronising (work queued on the handle's stream).  Its scratch is
  * one static device array of SLEMM_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library;
  * calls needing more (about 4·k·(n + m) bytes plus split-K partials) fail with
- * SLEMM_ERR_UNSUPPORTED.  The first call on a device looks up the array's address — make it
- * before any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * SLEMM_ERR_UNSUPPORTED.  The call runs with the handle's device current (the caller's current
+ * device is restored on return), so the array and the launches are always those of the handle's
+ * GPU.  The first call on a device looks up the array's address — make it before any stream
+ * capture; the address is kept for the life of the process (do not use the call after a
+ * cudaDeviceReset).  Calls share the array: calls that overlap on the GPU race. */
 #define SLEMM_NOALLOC_SCRATCH_BYTES (32u << 20)
 int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t ldv, int k, float* out,
                               int64_t ldo);

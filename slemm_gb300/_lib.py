@@ -15,8 +15,9 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "slemm_gpu.h")
 
 OP_QUADFORM, OP_LDET, OP_MATVEC, OP_RMATVEC, OP_WRMATVEC = range(5)
 ROWS_DEVICE = 1
-PREC_FP32, PREC_BF16X2, PREC_BF16X3 = range(3)
+PREC_FP32, PREC_BF16X2, PREC_BF16X3, PREC_FP16X2 = range(4)
 MEM_HOST, MEM_DEVICE = 0, 1
+LANCZOS_REORTH = 1
 
 P = ctypes.c_void_p
 I64 = ctypes.c_int64
@@ -29,11 +30,19 @@ class RemlOpts(ctypes.Structure):
                 ("tol_VC", F32), ("maxit", I32), ("verbose", I32)]
 
 
+TRACE_MAX = 64
+
+
 class RemlResult(ctypes.Structure):
     _fields_ = [("vg", F32), ("ve", F32), ("h2", F32), ("lrt", F32), ("iters_y", I32),
                 ("iters_Q", I32), ("iters_V", I32), ("n_criterion", I32), ("seconds", ctypes.c_double),
                 ("t_setup", ctypes.c_double), ("t_seed", ctypes.c_double), ("t_search", ctypes.c_double),
-                ("t_final", ctypes.c_double)]
+                ("t_final", ctypes.c_double), ("n_points", I32), ("h2_points", F32 * TRACE_MAX),
+                ("f_points", ctypes.c_double * TRACE_MAX)]
+
+    def trace(self):
+        """[(h², criterion)] of the search's evaluations, in order."""
+        return [(float(self.h2_points[q]), float(self.f_points[q])) for q in range(self.n_points)]
 
 
 class WindowOpts(ctypes.Structure):
@@ -59,6 +68,7 @@ _SIGS = {
     "slemm_gpu_set_projection": (I32, [P, P, I64, I32]),
     "slemm_gpu_set_precision": (I32, [P, I32]),
     "slemm_gpu_set_per_vector": (I32, [P, I32]),
+    "slemm_gpu_set_lanczos": (I32, [P, I32]),
     "slemm_gpu_op": (I32, [P, I32, F32, P, I64, I32, P, I64, I32]),
     "slemm_gpu_lanczos_seed": (I32, [P, I32, F32, P, I64, I32, F32, I32, I32, ctypes.POINTER(P),
                                      ctypes.POINTER(I32)]),

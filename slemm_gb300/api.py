@@ -126,6 +126,10 @@ class Genotypes:
     def set_per_vector(self, flag: bool):
         check(self._lib.slemm_gpu_set_per_vector(self.h, 1 if flag else 0))
 
+    def set_lanczos(self, reorth: bool = False):
+        """Lanczos mode of the seeds run on this handle (default: the reference's recurrence)."""
+        check(self._lib.slemm_gpu_set_lanczos(self.h, _lib.LANCZOS_REORTH if reorth else 0))
+
     def set_stream(self, stream_ptr: int | None):
         check(self._lib.slemm_gpu_set_stream(self.h, stream_ptr))
 
@@ -206,7 +210,7 @@ class Genotypes:
                                             _ptr(blue), _ptr(vb), ctypes.byref(r)))
         return dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue,
                     var_blue=vb, iters=(r.iters_y, r.iters_Q, r.iters_V),
-                    n_criterion=r.n_criterion, seconds=r.seconds,
+                    n_criterion=r.n_criterion, seconds=r.seconds, trace=r.trace(),
                     phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
     def LMC_REML(self, rvec, X, y, persnp, seed=0, n_MC=3, tol_L=5e-4, s2max=0.7, s2min=1e-4,
@@ -221,7 +225,7 @@ class Genotypes:
                                            _ptr(ps), ctypes.byref(o), _ptr(Py), _ptr(b),
                                            _ptr(blue), ctypes.byref(r)))
         return dict(vg=r.vg, ve=r.ve, h2=r.h2, Py=Py, snp_blup=b, blue=blue, iters=r.iters_V,
-                    n_criterion=r.n_criterion, seconds=r.seconds,
+                    n_criterion=r.n_criterion, seconds=r.seconds, trace=r.trace(),
                     phases=dict(setup=r.t_setup, seed=r.t_seed, search=r.t_search, final=r.t_final))
 
     def REML_grad(self, rvec, X, y, persnp, window, wwin, sigma_g2, sigma_e2, n_V=30, seed=0, tol=1e-6):
@@ -261,7 +265,8 @@ class Genotypes:
         k = nf.value
         cc = c + k
         out = dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue[:cc],
-                   fixed=list(fixed[:k]), persnp=p2, iters=(r.iters_y, r.iters_Q, r.iters_V))
+                   fixed=list(fixed[:k]), persnp=p2, iters=(r.iters_y, r.iters_Q, r.iters_V),
+                   trace=r.trace(), seconds=r.seconds)
         if lrt:
             out["var_blue"] = vb[:cc * cc].reshape(cc, cc, order="F")
         return out

@@ -158,17 +158,22 @@ void configure_pool(int device);
 // ---- packed product plan ------------------------------------------------------------------------
 // D[M_pad × N] = Cnt[M_pad × K_pad] · B where the count matrix is a tiled 2-bit packed array
 // (tiles of kTileM rows × kTileK K-elements, 2048 contiguous bytes each, see geno.cu) and B is
-// either FP32 [k][K_pad] (SIMT) or BF16 [N][K_pad] (tensor cores).  The raw product goes to
-// partials [splits][N][M_pad] (FP32), reduced by the finalize kernels of ops.cu.
+// either FP32 [k][K_pad] (SIMT) or 16-bit pieces [N][K_pad] (tensor cores: piece p of column c
+// in row p·kp + c, kp = k rounded up to 8, BF16 or FP16).  The raw product goes to partials
+// [splits][kp][M_pad] (FP32; the tensor-core epilogue adds a column's pieces before the store),
+// reduced by the finalize kernels of ops.cu.
 struct GemmArgs {
   const uint8_t* A;     // tiled packed counts
   int64_t M_pad;        // rows (multiple of 128)
   int64_t K_pad;        // K elements (multiple of 128)
   const void* B;        // dense side
-  int N;                // columns of D (k for SIMT, padded pieces*k for TC)
+  int N;                // columns of the product (k for SIMT, padded pieces·kp for TC)
   float* D;             // partials
   int splits;           // split-K factor
   int* err;             // device error word (bounded waits that gave up set bits here)
+  int kp = 0;           // columns of D per split (TC: k rounded up to 8; SIMT: N)
+  int pieces = 1;       // pieces per column (TC)
+  bool f16 = false;     // TC operand type: FP16 (true) or BF16
 };
 
 void gemm_simt(const GemmArgs& a, cudaStream_t st);

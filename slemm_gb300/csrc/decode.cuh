@@ -1,4 +1,4 @@
-// decode.cuh — 2-bit packed counts → BF16 / FP32 (device helpers shared by the kernels).
+// decode.cuh — 2-bit packed counts → BF16 / FP16 / FP32 (device helpers shared by the kernels).
 //
 // A 32-bit word holds 16 counts x ∈ {0,1,2} as 2-bit binary fields (layout in geno.cu): the even
 // elements 2q in bits 2q..2q+1 of the low half-word, the odd elements 2q+1 in bits 16+2q.. of the
@@ -12,6 +12,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace slemm {
 
@@ -24,6 +25,27 @@ __device__ __forceinline__ uint32_t bf16pair_of(uint32_t word, int q)
   const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&bits);
   const __nv_bfloat162 r = __hfma2(v, __float2bfloat162_rn(sc), __float2bfloat162_rn(-128.0f * sc));
   return *reinterpret_cast<const uint32_t*>(&r);
+}
+
+// The same pair as FP16: (src & (0x00030003 ≪ k)) | 0x64006400 is an FP16 pair whose halves are
+// 1024 + x·2^k (0x6400 is 1024, whose mantissa step is 1; x·2^k ≤ 128 stays inside the 10-bit
+// mantissa), and one HFMA2, v·2^−k − 1024·2^−k, gives x exactly.
+__device__ __forceinline__ uint32_t f16pair_of(uint32_t word, int q)
+{
+  const uint32_t src = (q < 4) ? word : (word >> 8);
+  const int k = 2 * (q & 3);
+  const uint32_t bits = (src & (0x00030003u << k)) | 0x64006400u;
+  const float sc = 1.0f / (float)(1 << k);
+  const __half2 v = *reinterpret_cast<const __half2*>(&bits);
+  const __half2 r = __hfma2(v, __float2half2_rn(sc), __float2half2_rn(-1024.0f * sc));
+  return *reinterpret_cast<const uint32_t*>(&r);
+}
+
+template <bool F16>
+__device__ __forceinline__ uint32_t pair_of(uint32_t word, int q)
+{
+  if constexpr (F16) return f16pair_of(word, q);
+  else return bf16pair_of(word, q);
 }
 
 // The 4 BF16 pairs of elements 8h … 8h+7 of a word (h = 0: pairs 0-3, h = 1: pairs 4-7).

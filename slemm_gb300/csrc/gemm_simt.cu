@@ -2,11 +2,13 @@
 //
 // D[s][c][r] = Σ_{K in split s} count[r,K] · B[c][K] for a 128-row tile per CTA: thread t owns
 // row t, reads its 16 packed bytes of each tile (the CTA's 128 threads read one contiguous
-// 2048-byte tile), decodes exact integer counts to FP32 and accumulates in FP32 like the
-// reference's SGEMM (src/reml.cpp:36, 144, 182, 220).  B columns are staged in shared memory for
-// kStageTiles tiles at a time and read as broadcasts.
+// 2048-byte tile), decodes exact integer counts to FP32 and multiplies and adds in FP32 like the
+// reference's SGEMM (src/reml.cpp:36, 144, 182, 220), one K-tile at a time, folding each tile's
+// sum into a double-float accumulator.  B columns are staged in shared memory for kStageTiles
+// tiles at a time and read as broadcasts.
 #include "common.h"
 #include "decode.cuh"
+#include "reduce.cuh"
 
 namespace slemm {
 
@@ -25,9 +27,10 @@ gemm_simt_kernel(const uint4* __restrict__ A, int64_t M_pad, int64_t K_tiles,
   const int s = blockIdx.y;
   const int64_t kt0 = (int64_t)s * tiles_per_split;
   const int64_t kt1 = min64(K_tiles, kt0 + tiles_per_split);
-  float acc[KC];
-#pragma unroll
-  for (int c = 0; c < KC; ++c) acc[c] = 0.f;
+  // Each K-tile's 64 products are summed in FP32 and folded into a double-float sum per column:
+  // one FP32 chain over a whole split (10^5 elements at 500,000 individuals) loses ~1e-5 of the
+  // result to rounding, 64-element chains ~3e-7.
+  DF acc[KC];
 
   for (int64_t ks = kt0; ks < kt1; ks += kStageTiles) {
     const int ntile = (int)min64(kStageTiles, kt1 - ks);
@@ -48,6 +51,9 @@ gemm_simt_kernel(const uint4* __restrict__ A, int64_t M_pad, int64_t K_tiles,
     for (int u = 0; u < kStageTiles; ++u) {
       if (u >= ntile) break;
       const uint32_t words[4] = {pk[u].x, pk[u].y, pk[u].z, pk[u].w};
+      float part[KC];
+#pragma unroll
+      for (int c = 0; c < KC; ++c) part[c] = 0.f;
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
 #pragma unroll
@@ -56,15 +62,17 @@ gemm_simt_kernel(const uint4* __restrict__ A, int64_t M_pad, int64_t K_tiles,
           f32pair_of(words[w], q, xe, xo);
           const int kk = u * kTileK + w * 16 + 2 * q;
 #pragma unroll
-          for (int c = 0; c < KC; ++c) acc[c] = fmaf(xe, sB[kk][c], fmaf(xo, sB[kk + 1][c], acc[c]));
+          for (int c = 0; c < KC; ++c) part[c] = fmaf(xe, sB[kk][c], fmaf(xo, sB[kk + 1][c], part[c]));
         }
       }
+#pragma unroll
+      for (int c = 0; c < KC; ++c) df_add(acc[c], part[c]);
     }
   }
 #pragma unroll
   for (int c = 0; c < KC; ++c) {
     const int col = c0 + c;
-    if (col < k_total) D[((int64_t)s * N + col) * M_pad + mt * 128 + t] = acc[c];
+    if (col < k_total) D[((int64_t)s * N + col) * M_pad + mt * 128 + t] = __fadd_rn(acc[c].hi, acc[c].lo);
   }
 }
 

@@ -188,14 +188,15 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
   return d;
 }
 
-// Instruction descriptor of kind::f16: BF16 × BF16 → FP32, both K-major, M = 128.
-__host__ __device__ constexpr uint32_t idesc_bf16(int N)
+// Instruction descriptor of kind::f16: BF16 × BF16 (or FP16 × FP16) → FP32, both K-major, M = 128.
+// A and B always have the same type.
+__host__ __device__ constexpr uint32_t idesc_f16kind(int N, bool f16)
 {
-  return (1u << 4)                      // D format F32
-         | (1u << 7)                    // A format BF16
-         | (1u << 10)                   // B format BF16
-         | ((uint32_t)(N >> 3) << 17)   // N / 8
-         | ((uint32_t)(128 >> 4) << 24);  // M / 16
+  return (1u << 4)                          // D format F32
+         | ((f16 ? 0u : 1u) << 7)           // A format: 0 FP16, 1 BF16
+         | ((f16 ? 0u : 1u) << 10)          // B format: 0 FP16, 1 BF16
+         | ((uint32_t)(N >> 3) << 17)       // N / 8
+         | ((uint32_t)(128 >> 4) << 24);    // M / 16
 }
 
 // D[tmem] (+)= A[tmem] · B[smem]
@@ -215,6 +216,15 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar)
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+
+// 8 consecutive TMEM columns (from a multiple of 8) of this warp's 32 lanes; no wait.
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8])
+{
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(taddr));
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
@@ -243,11 +253,11 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32
       : "memory");
 }
 
-template <int PK, int S, int SB, int KT>
+template <int PK, int S, int SB, int KT, bool F16>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
                float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
-               int* __restrict__ err)
+               int kp, int pieces, int* __restrict__ err)
 {
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment of the shared-window address (SWIZZLE_128B tiles need it)
@@ -356,7 +366,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     // both tiles, or four column-group issuers, measured slower).
     const int t = warp - P.mma_warp0();
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(N);
+      const uint32_t idesc = idesc_f16kind(N, F16);
       const uint64_t bdesc0 = sw128_desc(smem_u32(sB));
       const uint32_t bstep = (uint32_t)(N * 128) >> 4;          // descriptor units per B K-tile
       const uint32_t d_tmem = tmem_base + (uint32_t)(t * N);
@@ -418,7 +428,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
 #pragma unroll
         for (int w = 0; w < 4; ++w)
 #pragma unroll
-          for (int q = 0; q < 8; ++q) v[w * 8 + q] = bf16pair_of(words[w], q);
+          for (int q = 0; q < 8; ++q) v[w * 8 + q] = pair_of<F16>(words[w], q);
         if (kk == 0 && i >= S) {   // the stage that last used this A slot has been consumed
           got = mbar_wait(&done[(i - S) % BS], (uint32_t)((i - S) / BS) & 1, err, 64, abort_flag, 64);
           if (!__all_sync(0xffffffffu, got)) {
@@ -445,16 +455,24 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
       const bool ok = __all_sync(0xffffffffu, got && !*abort_flag);   // tcgen05.ld is warp-wide
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (ok) {
-        float* Dbase = D + ((size_t)split * N) * M_pad + (mt0 + tsub) * 128 + r;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-          uint32_t o[16];
-          tmem_ld16(tmem_base + ((uint32_t)(lq * 32) << 16) + (uint32_t)(tsub * N + c0), o);
+        // column c of D = Σ_p accumulator column p·kp + c (the pieces of c): kp columns per split
+        float* Dbase = D + ((size_t)split * kp) * M_pad + (mt0 + tsub) * 128 + r;
+        const uint32_t tl = tmem_base + ((uint32_t)(lq * 32) << 16) + (uint32_t)(tsub * N);
+        for (int c0 = 0; c0 < kp; c0 += 8) {
+          float acc[8] = {};
+          for (int p = 0; p < pieces; ++p) {
+            uint32_t o[8];
+            tmem_ld8_nowait(tl + (uint32_t)(p * kp + c0), o);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] = __fadd_rn(acc[j], __uint_as_float(o[j]));
+          }
           if (nk == 0) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) o[j] = 0u;
+            for (int j = 0; j < 8; ++j) acc[j] = 0.f;
           }
 #pragma unroll
-          for (int j = 0; j < 16; ++j) Dbase[(size_t)(c0 + j) * M_pad] = __uint_as_float(o[j]);
+          for (int j = 0; j < 8; ++j) Dbase[(size_t)(c0 + j) * M_pad] = acc[j];
         }
       }
     }
@@ -496,7 +514,21 @@ int gemm_tc_rows_per_cta(int N)
   return (N <= kNarrowN ? plan_tc<6, 3, 0, 2>(N).sub : plan_tc<4, 3, 6, 1>(N).sub) * kTileM;
 }
 
-template <int PK, int S, int SB, int KT>
+// Sets the kernel's shared-memory limit once per device (the attribute belongs to the device's
+// context, so a process that uses several GPUs sets it on each).
+template <auto kernel>   // one flag set per kernel instantiation
+static void configure_once()
+{
+  static std::atomic<uint64_t> done{0};
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (bit && (done.load() & bit)) return;
+  CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+  done.fetch_or(bit);
+}
+
+template <int PK, int S, int SB, int KT, bool F16>
 static void launch_tc(const GemmArgs& a, cudaStream_t st)
 {
   const TcPlan<PK, S, SB, KT> P = plan_tc<PK, S, SB, KT>(a.N);
@@ -513,32 +545,34 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
   const cuuint64_t strides[1] = {(cuuint64_t)a.K_pad * 2};
   const cuuint32_t box[2] = {64, (cuuint32_t)a.N};
   const cuuint32_t estr[2] = {1, 1};
-  CUresult r = get_encode()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(a.B), dims,
+  CUresult r = get_encode()(&map, F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                            const_cast<void*>(a.B), dims,
                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) SLEMM_THROW(SLEMM_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 
-  static bool configured = false;
-  if (!configured) {
-    CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel<PK, S, SB, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kSmemBudget));
-    configured = true;
-  }
+  configure_once<gemm_tc_kernel<PK, S, SB, KT, F16>>();
+  CHECK_ARG(a.kp % 8 == 0 && a.pieces >= 1 && a.pieces * a.kp <= a.N, "bad piece layout");
   // Each CTA allocates all 512 TMEM columns: request enough shared memory that only one CTA is
   // resident per SM, so no allocation ever has to wait for another CTA's release.
   const size_t smem = std::max<size_t>(P.total, 120 * 1024);
   dim3 grid((unsigned)Mc, (unsigned)a.splits);
-  gemm_tc_kernel<PK, S, SB, KT><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N, P.sub,
-                                                                  a.err);
+  gemm_tc_kernel<PK, S, SB, KT, F16><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N,
+                                                                       P.sub, a.kp, a.pieces, a.err);
   LAUNCH_CHECK();
 }
 
 void gemm_tc(const GemmArgs& a, cudaStream_t st)
 {
   CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
-  if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2>(a, st);
-  else launch_tc<4, 3, 6, 1>(a, st);
+  if (a.f16) {
+    if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2, true>(a, st);
+    else launch_tc<4, 3, 6, 1, true>(a, st);
+  } else {
+    if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2, false>(a, st);
+    else launch_tc<4, 3, 6, 1, false>(a, st);
+  }
 }
 
 }  // namespace slemm

@@ -583,7 +583,8 @@ int slemm_gpu_set_precision(slemm_geno* g, int prec)
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
-    CHECK_ARG(prec == SLEMM_PREC_FP32 || prec == SLEMM_PREC_BF16X2 || prec == SLEMM_PREC_BF16X3,
+    CHECK_ARG(prec == SLEMM_PREC_FP32 || prec == SLEMM_PREC_BF16X2 || prec == SLEMM_PREC_BF16X3 ||
+                  prec == SLEMM_PREC_FP16X2,
               "unknown precision");
     g->prec = prec;
   });
@@ -594,6 +595,15 @@ int slemm_gpu_set_per_vector(slemm_geno* g, int per_vector)
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
     g->per_vector = per_vector ? 1 : 0;
+  });
+}
+
+int slemm_gpu_set_lanczos(slemm_geno* g, int mode)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    CHECK_ARG((mode & ~SLEMM_LANCZOS_REORTH) == 0, "unknown Lanczos mode bits");
+    g->lanczos_mode = mode;
   });
 }
 

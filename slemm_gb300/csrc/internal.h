@@ -17,6 +17,7 @@ struct slemm_geno {
   bool weights_set = false;
   int prec = SLEMM_PREC_BF16X2;
   int per_vector = 0;
+  int lanczos_mode = 0;           // SLEMM_LANCZOS_* bits of the seeds run on this handle
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // work buffers

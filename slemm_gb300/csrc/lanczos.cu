@@ -42,6 +42,11 @@ struct slemm_lseed {
   // L_Seed call); group_iters[g] is the step at which group g met the tolerance.
   std::vector<int> group_start, group_iters;
   slemm::DevBuf solve_coef, solve_blk;       // reused by every shifted solve
+  // SLEMM_LANCZOS_* bits of the handle when the seed was run (REORTH: every new vector is made
+  // orthogonal to the whole stored basis of its column).
+  int mode = 0;
+  slemm::DevBuf ro_ptr, ro_red, ro_coef;     // reorthogonalisation: block pointers, dot partials, coefficients
+  std::vector<const float*> ro_host;         // host copy of the block pointers uploaded so far
   ~slemm_lseed()
   {
     for (auto* c : chunks) delete c;
@@ -172,6 +177,117 @@ lz_scale_kernel(float* __restrict__ Unext, const float* __restrict__ src, const 
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
+// ---- reorthogonalisation (opt-in, SLEMM_LANCZOS_REORTH) ----------------------------------------
+// The reference runs the plain three-term recurrence (src/reml.cpp:293-322).  In finite precision
+// its vectors lose orthogonality once Ritz values converge, which on ill-conditioned systems
+// (window-weighted GREML) adds steps and makes the stopping step depend on rounding.  The opt-in
+// mode removes from each new vector w (column c, after the recurrence) its components along every
+// stored vector of that column by classical Gram–Schmidt with FP64-accurate coefficients:
+//   d_i = U_i[:,c]·w (double-float sums), w ← w − Σ_i d_i·U_i[:,c] (double-float sum, rounded once).
+// Two streaming passes over the stored basis per step: the dots, then the update.
+constexpr int kRoRows = 8192;     // rows of one block of the dot pass
+constexpr int kRoGroup = 8;       // stored vectors whose block sums share one barrier
+
+// red[(i·t + c)·nblk + blk] = Σ_{rows of blk} U_i[r,c]·w[r,c] for i = 0 … J
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_reorth_dot_kernel(const float* __restrict__ w, const float* const* __restrict__ blocks, int J, int t,
+                     int64_t n, double* __restrict__ red, int nblk)
+{
+  constexpr int P = kRoRows / (kLzThreads * V);
+  __shared__ double sh[kRoGroup][kLzThreads / 32];
+  const int c = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = (int64_t)blockIdx.x * kRoRows;
+  float x[P][V];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    const int64_t r = r0 + ((int64_t)p * kLzThreads + threadIdx.x) * V;
+    if (r < n) ldv<V>(w + (int64_t)c * n + r, x[p]);
+    else
+#pragma unroll
+      for (int q = 0; q < V; ++q) x[p][q] = 0.f;
+  }
+  for (int i0 = 0; i0 <= J; i0 += kRoGroup) {
+    const int ni = min(kRoGroup, J + 1 - i0);
+    for (int q = 0; q < ni; ++q) {
+      const float* U = blocks[i0 + q] + (int64_t)c * n;
+      DF acc;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const int64_t r = r0 + ((int64_t)p * kLzThreads + threadIdx.x) * V;
+        if (r < n) {
+          float u[V];
+          ldv<V>(U + r, u);
+#pragma unroll
+          for (int e = 0; e < V; ++e) df_fma(acc, u[e], x[p][e]);
+        }
+      }
+      double s = df_value(acc);
+      for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) sh[q][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < ni) {
+      double s = 0.0;
+      for (int k = 0; k < kLzThreads / 32; ++k) s += sh[threadIdx.x][k];
+      red[((int64_t)(i0 + threadIdx.x) * t + c) * nblk + blockIdx.x] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// coef2[2q], coef2[2q+1] = hi, lo of Σ_b red[q·nblk + b] for q < nq (block order)
+__global__ void lz_reorth_coef_kernel(const double* __restrict__ red, int nblk, int nq, float* __restrict__ coef2)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) split_double(sum_partials(red + (int64_t)q * nblk, nblk), coef2[2 * q], coef2[2 * q + 1]);
+}
+
+// w[r,c] ← w[r,c] − Σ_{i ≤ J} d_{i,c}·U_i[r,c] (double-float sum rounded once);
+// red_nrm[c][blk] = Σ w² of the result (partials over blocks of kLzRows rows, as lz_orth writes them)
+template <int V>
+__global__ void __launch_bounds__(kLzThreads)
+lz_reorth_update_kernel(float* __restrict__ w, const float* const* __restrict__ blocks, int J, int t,
+                        const float* __restrict__ coef2, int64_t n, double* __restrict__ red, int nblk)
+{
+  extern __shared__ float sco[];   // (J+1) hi/lo pairs of this column
+  __shared__ double sh[32];
+  const int c = blockIdx.y;
+  for (int i = threadIdx.x; i <= J; i += kLzThreads) {
+    sco[2 * i] = coef2[2 * ((int64_t)i * t + c)];
+    sco[2 * i + 1] = coef2[2 * ((int64_t)i * t + c) + 1];
+  }
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
+  DF acc;
+  for (int64_t r = i0 + threadIdx.x * V; r < i1; r += kLzThreads * V) {
+    const int64_t o = (int64_t)c * n + r;
+    DF a[V];
+#pragma unroll 4
+    for (int i = 0; i <= J; ++i) {
+      float u[V];
+      ldv<V>(blocks[i] + o, u);
+      const float ch = sco[2 * i], cl = sco[2 * i + 1];
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        df_fma(a[e], ch, u[e]);
+        a[e].lo = __fmaf_rn(cl, u[e], a[e].lo);
+      }
+    }
+    float x[V];
+    ldv<V>(w + o, x);
+#pragma unroll
+    for (int e = 0; e < V; ++e) {
+      x[e] = __fsub_rn(__fsub_rn(x[e], a[e].hi), a[e].lo);
+      df_fma(acc, x[e], x[e]);
+    }
+    stv<V>(w + o, x);
+  }
+  const double s = block_sum_d(df_value(acc), sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
 // out[c] = Σ dot, out[t+c] = Σ nrm, out[2t+c] = Σ un (the consumers' order); out[3t] = error word.
 __global__ void lz_final_kernel(const double* __restrict__ dot, const double* __restrict__ nrm,
                                 const double* __restrict__ un, int t, int nblk, const int* __restrict__ err,
@@ -291,6 +407,42 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
       }
     };
 
+    S->mode = g->lanczos_mode;
+    const bool reorth = (S->mode & SLEMM_LANCZOS_REORTH) != 0;
+    const int nblkR = (int)ceil_div(n, kRoRows);
+    if (reorth) {
+      S->ro_ptr.stream = S->ro_red.stream = S->ro_coef.stream = st;
+      S->ro_ptr.ordered = S->ro_red.ordered = S->ro_coef.ordered = true;
+      S->ro_ptr.ensure((size_t)maxit * sizeof(float*));
+      S->ro_red.ensure((size_t)maxit * t * nblkR * sizeof(double));
+      S->ro_coef.ensure((size_t)maxit * t * 2 * sizeof(float));
+      S->ro_host.reserve(maxit);   // never reallocated while an upload from it is queued
+    }
+    // w (the new vector of step J, in tmp) ← w minus its components along U_0 … U_J, and the norm
+    // partials of the result in r_nrm (what lz_scale and the step's β read).
+    auto reorthogonalise = [&](int J) {
+      const int have = (int)S->ro_host.size();
+      if (have < J + 1) {
+        for (int i = have; i <= J; ++i) S->ro_host.push_back(S->block(i));
+        CUDA_TRY(cudaMemcpyAsync(S->ro_ptr.as<const float*>() + have, S->ro_host.data() + have,
+                                 (size_t)(J + 1 - have) * sizeof(float*), cudaMemcpyHostToDevice, st));
+      }
+      const float* const* blk = S->ro_ptr.as<const float*>();
+      double* rred = S->ro_red.as<double>();
+      float* coef = S->ro_coef.as<float>();
+      const dim3 grd(nblkR, t);
+      if (v4) lz_reorth_dot_kernel<4><<<grd, kLzThreads, 0, st>>>(tmp, blk, J, t, n, rred, nblkR);
+      else lz_reorth_dot_kernel<1><<<grd, kLzThreads, 0, st>>>(tmp, blk, J, t, n, rred, nblkR);
+      LAUNCH_CHECK();
+      const int nq = (J + 1) * t;
+      lz_reorth_coef_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, st>>>(rred, nblkR, nq, coef);
+      LAUNCH_CHECK();
+      const size_t smem = (size_t)2 * (J + 1) * sizeof(float);
+      if (v4) lz_reorth_update_kernel<4><<<gr, kLzThreads, smem, st>>>(tmp, blk, J, t, coef, n, r_nrm, nblk);
+      else lz_reorth_update_kernel<1><<<gr, kLzThreads, smem, st>>>(tmp, blk, J, t, coef, n, r_nrm, nblk);
+      LAUNCH_CHECK();
+    };
+
     // B_norm, U_0 = B / β_0
     if (v4) lz_norm_kernel<4><<<gr, kLzThreads, 0, st>>>(S->B.as<float>(), n, r_nrm, nblk);
     else lz_norm_kernel<1><<<gr, kLzThreads, 0, st>>>(S->B.as<float>(), n, r_nrm, nblk);
@@ -325,6 +477,7 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
         LAUNCH_CHECK();
         lz_orth_kernel<4><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
         LAUNCH_CHECK();
+        if (reorth) reorthogonalise(j);
         lz_scale_kernel<4><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
         LAUNCH_CHECK();
       } else {
@@ -332,6 +485,7 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
         LAUNCH_CHECK();
         lz_orth_kernel<1><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
         LAUNCH_CHECK();
+        if (reorth) reorthogonalise(j);
         lz_scale_kernel<1><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
         LAUNCH_CHECK();
       }

@@ -14,7 +14,11 @@
 //   * A call whose scratch would exceed that size is rejected with SLEMM_ERR_UNSUPPORTED and a
 //     message giving the bytes it would need; nothing is launched.
 //   * The first call on each device looks up the array's device address (cudaGetSymbolAddress)
-//     with that device current; make that first call before any stream capture.
+//     with that device current; make that first call before any stream capture.  The call makes
+//     the handle's device current for its duration (the caller's current device is restored),
+//     so a caller with another device current still gets the handle's GPU and its array.  The
+//     address is cached for the life of the process: a caller that resets the device
+//     (cudaDeviceReset) must not use this entry point afterwards.
 //   * All calls on a device share the one array and each call overwrites what it uses (nothing
 //     has to be cleared between calls).  Calls whose GPU work overlaps — on different streams or
 //     different handles at the same time — race on the array; order them on one stream.
@@ -35,11 +39,25 @@ constexpr int kMaxDevices = 64;
 static void* s_scratch[kMaxDevices] = {};
 static std::mutex s_scratch_mu;
 
-// Device address of the static scratch array on the current device (looked up once per device).
-static void* scratch_on_current_device()
+// Makes `dev` the calling thread's current device for the scope and restores the caller's after.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int dev)
+  {
+    CUDA_TRY(cudaGetDevice(&prev));
+    if (prev != dev) CUDA_TRY(cudaSetDevice(dev));
+  }
+  ~DeviceScope()
+  {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Device address of the static scratch array on device `dev`, which must be current (looked up
+// once per device; the cache assumes the device's context lives as long as the process).
+static void* scratch_on_device(int dev)
 {
-  int dev = 0;
-  CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "device index beyond 64");
   std::lock_guard<std::mutex> lk(s_scratch_mu);
   if (!s_scratch[dev]) {
@@ -161,7 +179,10 @@ extern "C" int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t 
                   "rmatvec_noalloc needs " + std::to_string(L.total) + " bytes of scratch for n=" +
                       std::to_string(g->n) + ", m=" + std::to_string(g->m) + ", k=" + std::to_string(k) +
                       "; the static scratch holds " + std::to_string(kNoAllocBytes) + " bytes");
-    uint8_t* base = static_cast<uint8_t*>(scratch_on_current_device());
+    // The handle's stream belongs to the handle's device: its scratch address and every launch
+    // below are taken with that device current, whichever device the caller has current.
+    DeviceScope on_device(g->device);
+    uint8_t* base = static_cast<uint8_t*>(scratch_on_device(g->device));
     float* B = reinterpret_cast<float*>(base + L.b_off);
     float* D = reinterpret_cast<float*>(base + L.d_off);
     double* red = reinterpret_cast<double*>(base + L.red_off);

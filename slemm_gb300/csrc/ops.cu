@@ -19,6 +19,7 @@
 #include "reduce.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace slemm {
 
@@ -199,12 +200,80 @@ void col_dots(slemm_geno* g, const float* a, int64_t lda, const float* b, int64_
 }
 
 // ---- dense-operand builders ------------------------------------------------------------------------
-// Writes x[0 … V−1] (rows kidx …) into the dense operand — FP32 row c (npieces == 0) or BF16
-// pieces p·k + c — and adds exactly what the products will see to acc (weighted by wt when
-// kWeighted).
-template <int V, bool kWeighted>
-__device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, void* Bv, int64_t K_pad, int k,
-                                              int c, int64_t kidx, DF& acc, const float (&wt)[V])
+// FP16 pieces (SLEMM_PREC_FP16X2) are a fixed-point split: the operand column is scaled by a power
+// of two 2^e, chosen from a bound on |x| so that the largest value lies in [2^10, 2^11); the hi
+// piece is rint(x·2^e), an integer of at most 11 bits (exact in FP16), and the lo piece is the
+// FP16 rounding of the remainder (|lo| ≤ 1/2).  Products count·hi are integers below 2^12, so the
+// tensor cores' FP32 accumulation of the hi pieces is exact while a partial sum stays below 2^24
+// (a random-sign sum over 10^6 individuals reaches ~2^18), and the lo pieces carry 2^−11 of the
+// magnitude: the accumulation error that bounds the BF16 and CUDA-core FP32 paths at long K
+// (≈4e-6 relative over 500,000 individuals) falls away and what remains is the lo piece's
+// rounding, ≤ 2^−23 of the column's largest value.  The products are scaled back by 2^−e
+// (exact).  BF16 shares FP32's exponent range and needs no scale.
+__device__ __forceinline__ int f16_exp(double bound)
+{
+  if (!(bound > 0.0) || !isfinite(bound)) return 0;
+  int E;
+  frexp(bound, &E);                       // bound = f·2^E, f ∈ [0.5, 1)
+  return max(-120, min(120, 11 - E));     // bound·2^e ∈ [2^10, 2^11)
+}
+
+// max_b parts[c·nblk + b]
+__device__ __forceinline__ double max_partials(const double* __restrict__ parts, int nblk, int c)
+{
+  double v = 0.0;
+  for (int b = 0; b < nblk; ++b) v = fmax(v, parts[(int64_t)c * nblk + b]);
+  return v;
+}
+
+// Block maximum of one float per thread (valid in thread 0; −∞ when every thread holds −∞);
+// sh holds ≥ 32 floats.
+__device__ __forceinline__ float block_max_f(float v, float* sh)
+{
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  float r = -INFINITY;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = fmaxf(r, sh[i]);
+  return r;
+}
+
+// Scale exponent of individual-side operand column c whose stored values are x − μ: from the
+// measure pass's signed block extremes range[(c·nblk + b)·2 + {0, 1}] = {max x, max −x} over the
+// valid rows, the bound max(max x − μ, μ − min x) ≥ |x − μ|.  A column with a large mean keeps
+// the resolution of its spread.  The prologue and the finalize take the same e from this.
+__device__ __forceinline__ int f16_col_exp(const double* __restrict__ range, int nblk, int c, float mu)
+{
+  double hi = -INFINITY, nlo = -INFINITY;
+  for (int b = 0; b < nblk; ++b) {
+    hi = fmax(hi, range[((int64_t)c * nblk + b) * 2]);
+    nlo = fmax(nlo, range[((int64_t)c * nblk + b) * 2 + 1]);
+  }
+  return f16_exp(fmax(hi - (double)mu, nlo + (double)mu));
+}
+
+// Row of piece p of column c in a tensor-core operand whose pieces are kp rows apart.
+__device__ __forceinline__ int64_t piece_row(int p, int kp, int c) { return (int64_t)p * kp + c; }
+
+// Row of padding row q (q < N − pieces·k) of such an operand: first the kp − k spare rows after
+// each piece's k columns, then the rows from pieces·kp to N.
+__device__ __forceinline__ int pad_row(int q, int k, int kp, int pieces)
+{
+  const int per = kp - k;
+  if (q < pieces * per) return (q / per) * kp + k + (q % per);
+  return pieces * kp + (q - pieces * per);
+}
+
+// Writes x[0 … V−1] (rows kidx …) into the dense operand — FP32 row c (npieces == 0) or 16-bit
+// pieces in rows p·kp + c (BF16, or the FP16 fixed-point split of x·scale when F16) — and adds
+// exactly what the products will see, in the units of x, to acc (weighted by wt when kWeighted).
+template <int V, bool kWeighted, bool F16 = false>
+__device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, void* Bv, int64_t K_pad, int kp,
+                                              int c, int64_t kidx, DF& acc, const float (&wt)[V],
+                                              float scale = 1.f, float inv_scale = 1.f)
 {
   if (npieces == 0) {
     stv<V>(static_cast<float*>(Bv) + (int64_t)c * K_pad + kidx, x);
@@ -215,27 +284,35 @@ __device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, 
     }
     return;
   }
-  __nv_bfloat16* B = static_cast<__nv_bfloat16*>(Bv);
+  uint16_t* B = static_cast<uint16_t*>(Bv);
   float r[V];
 #pragma unroll
-  for (int u = 0; u < V; ++u) r[u] = x[u];
+  for (int u = 0; u < V; ++u) r[u] = F16 ? __fmul_rn(x[u], scale) : x[u];   // exact: scale is 2^e
   for (int p = 0; p < npieces; ++p) {
-    __nv_bfloat16 h[V];
+    uint16_t h[V];
 #pragma unroll
     for (int u = 0; u < V; ++u) {
-      h[u] = __float2bfloat16_rn(r[u]);
-      const float hf = __bfloat162float(h[u]);
+      float hf;
+      if constexpr (F16) {
+        // piece 0: the integer part (|r| ≤ 2^11, exact in FP16); later pieces: FP16 rounding
+        const __half hh = __float2half_rn(p == 0 ? rintf(r[u]) : r[u]);
+        hf = __half2float(hh);
+        h[u] = __half_as_ushort(hh);
+      } else {
+        const __nv_bfloat16 hb = __float2bfloat16_rn(r[u]);
+        hf = __bfloat162float(hb);
+        h[u] = __bfloat16_as_ushort(hb);
+      }
       r[u] = __fsub_rn(r[u], hf);   // exact in FP32
-      if (kWeighted) df_fma(acc, wt[u], hf);
-      else df_add(acc, hf);
+      const float hv = F16 ? __fmul_rn(hf, inv_scale) : hf;
+      if (kWeighted) df_fma(acc, wt[u], hv);
+      else df_add(acc, hv);
     }
-    __nv_bfloat16* dst = B + (int64_t)(p * k + c) * K_pad + kidx;
+    uint16_t* dst = B + piece_row(p, kp, c) * K_pad + kidx;
     if constexpr (V == 4) {
-      __nv_bfloat162 lo2, hi2;
-      lo2.x = h[0], lo2.y = h[1], hi2.x = h[2], hi2.y = h[3];
       uint2 pk;
-      pk.x = *reinterpret_cast<uint32_t*>(&lo2);
-      pk.y = *reinterpret_cast<uint32_t*>(&hi2);
+      pk.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+      pk.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
       *reinterpret_cast<uint2*>(dst) = pk;
     } else {
       dst[0] = h[0];
@@ -243,16 +320,16 @@ __device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, 
   }
 }
 
-// Zeroes BF16 padding row `row` (rows pieces·k … N−1 of the operand) over K-range [k0, k1).
+// Zeroes 16-bit padding row `row` of the operand over K-range [k0, k1).
 __device__ __forceinline__ void zero_pad_row(void* Bv, int64_t K_pad, int row, int64_t k0, int64_t k1)
 {
-  uint2* dst = reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(Bv) + (int64_t)row * K_pad);
+  uint2* dst = reinterpret_cast<uint2*>(static_cast<uint16_t*>(Bv) + (int64_t)row * K_pad);
   for (int64_t q = k0 / 4 + threadIdx.x; q < k1 / 4; q += blockDim.x) dst[q] = make_uint2(0u, 0u);
 }
 
 // Direction-1 operand (K = individuals): x = in[i,c]; for the first nq columns
 // x −= Σ_l Q[i,l]·QtV[l,c] (QtV from its partials); optionally x *= rr[i]; rows i ≥ n are 0.
-// red[c][blk] = Σ_i stored(x).  Blocks with c ≥ k zero BF16 padding row npieces·k + (c − k).
+// red[c][blk] = Σ_i stored(x).  Blocks with c ≥ k zero the operand's padding rows (pad_row).
 // MEASURE: only red[c][blk] = Σ_i x (the column sums that give the means), nothing stored.
 // Otherwise, with mparts (those sums), x − μ_c is stored, μ_c = (float)(Σ/n) as in column_mean.
 __device__ __forceinline__ float column_mean(const double* __restrict__ mparts, int nblk, int c, double inv_n)
@@ -260,30 +337,44 @@ __device__ __forceinline__ float column_mean(const double* __restrict__ mparts, 
   return (float)(sum_partials(mparts + (int64_t)c * nblk, nblk) * inv_n);
 }
 
-template <int V, bool MEASURE>
+// F16: the operand is stored as FP16 pieces of (x − μ)·2^e, e from the MEASURE pass's signed
+// extremes (f16_col_exp).  MEASURE also writes xmax[c][blk][2] = {max x, max −x} over the valid
+// rows when xmax != nullptr.
+template <int V, bool MEASURE, bool F16 = false>
 __global__ void __launch_bounds__(kRedThreads)
-prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64_t n_pad, int k,
+prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64_t n_pad, int k, int kp,
                       const float* __restrict__ Q, int64_t ldq, int cq, const double* __restrict__ qparts,
                       int nblkq, int nq, const float* __restrict__ rr, int npieces, void* B,
-                      double* __restrict__ red, int nblk, const double* __restrict__ mparts)
+                      double* __restrict__ red, int nblk, const double* __restrict__ mparts,
+                      double* __restrict__ xmax)
 {
   __shared__ double sh[32];
+  __shared__ float shf[32];
   __shared__ float2 qt[64];
-  __shared__ float smu;
+  __shared__ float smu, ssc[2];
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n_pad, i0 + kRowsPerBlock);
   if (c >= k) {
-    if (!MEASURE) zero_pad_row(B, n_pad, npieces * k + (c - k), i0, i1);
+    if (!MEASURE) zero_pad_row(B, n_pad, pad_row(c - k, k, kp, npieces), i0, i1);
     return;
   }
   const bool proj = qparts != nullptr && c < nq;
   if (proj) load_qt(qparts, nblkq, cq, nq, c, qt);
-  if (!MEASURE && mparts != nullptr) {
-    if (threadIdx.x == 0) smu = column_mean(mparts, nblk, c, 1.0 / (double)n);
+  if (!MEASURE && (mparts != nullptr || F16)) {
+    if (threadIdx.x == 0) {
+      smu = mparts != nullptr ? column_mean(mparts, nblk, c, 1.0 / (double)n) : 0.f;
+      if (F16) {
+        const int e = f16_col_exp(xmax, nblk, c, smu);
+        ssc[0] = ldexpf(1.f, e);
+        ssc[1] = ldexpf(1.f, -e);
+      }
+    }
     __syncthreads();
   }
   const float mu = (!MEASURE && mparts != nullptr) ? smu : 0.f;
+  const float sc = (!MEASURE && F16) ? ssc[0] : 1.f, isc = (!MEASURE && F16) ? ssc[1] : 1.f;
   DF acc;
+  float xhi = -INFINITY, nxlo = -INFINITY;   // MEASURE: max x and max −x over the valid rows
   const float one[V] = {};
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
     float x[V] = {};
@@ -307,66 +398,89 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
     }
     if (MEASURE) {
 #pragma unroll
-      for (int u = 0; u < V; ++u) df_add(acc, x[u]);
+      for (int u = 0; u < V; ++u) {
+        df_add(acc, x[u]);
+        if (i + u < n) {
+          xhi = fmaxf(xhi, x[u]);
+          nxlo = fmaxf(nxlo, -x[u]);
+        }
+      }
     } else {
-      store_operand<V, false>(x, npieces, B, n_pad, k, c, i, acc, one);
+      store_operand<V, false, F16>(x, npieces, B, n_pad, kp, c, i, acc, one, sc, isc);
     }
   }
   const double s = block_sum_d(df_value(acc), sh);
-  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+  if (threadIdx.x == 0 && red != nullptr) red[(int64_t)c * nblk + blockIdx.x] = s;
+  if (MEASURE && xmax != nullptr) {   // signed extremes [c][blk][2] (f16_col_exp)
+    const float mx = block_max_f(xhi, shf);
+    const float mn = block_max_f(nxlo, shf);
+    if (threadIdx.x == 0) {
+      xmax[((int64_t)c * nblk + blockIdx.x) * 2] = (double)mx;
+      xmax[((int64_t)c * nblk + blockIdx.x) * 2 + 1] = (double)mn;
+    }
+  }
 }
 
-// Sum over split-K partials and BF16 pieces of column c, rows r … r+V−1.
+// Sum over the split-K partials ([splits][kp][M_pad]) of column c, rows r … r+V−1, times isc
+// (2^−e of an FP16 operand column, else 1).
 template <int V>
-__device__ __forceinline__ void gather_D(const float* __restrict__ D, int splits, int N, int64_t M_pad,
-                                         int pieces, int k, int c, int64_t r, float (&acc)[V])
+__device__ __forceinline__ void gather_D(const float* __restrict__ D, int splits, int kp, int64_t M_pad,
+                                         int c, int64_t r, float isc, float (&acc)[V])
 {
 #pragma unroll
   for (int u = 0; u < V; ++u) acc[u] = 0.f;
-  for (int s = 0; s < splits; ++s)
-    for (int p = 0; p < pieces; ++p) {
-      float t[V];
-      ldv<V>(D + ((int64_t)s * N + p * k + c) * M_pad + r, t);
+  for (int s = 0; s < splits; ++s) {
+    float t[V];
+    ldv<V>(D + ((int64_t)s * kp + c) * M_pad + r, t);
 #pragma unroll
-      for (int u = 0; u < V; ++u) acc[u] = __fadd_rn(acc[u], t[u]);
-    }
+    for (int u = 0; u < V; ++u) acc[u] = __fadd_rn(acc[u], t[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < V; ++u) acc[u] = __fmul_rn(acc[u], isc);
 }
 
-// Direction-1 finalize (rows = SNPs): val = raw − gm_j·colsum_c (colsum from the prologue's
-// partials), times w_j when w != nullptr.  mode 0: out[j,c] = val (j < m).  mode 1: val becomes
-// the direction-2 operand (K = SNPs) and red[c][blk] = Σ_j gm_j·stored(val); blocks with c ≥ k
-// zero BF16 padding row npieces2·k + (c − k).
+// Direction-1 finalize (rows = SNPs): val = raw·2^−e1 − gm_j·colsum_c (colsum from the prologue's
+// partials; e1 the FP16 scale of operand column c when xmax1 != nullptr), plus μ·gcorr_j for the
+// mean the prologue removed, times w_j when w != nullptr.  mode 0: out[j,c] = val (j < m).
+// mode 1: val becomes the direction-2 operand (K = SNPs) and red[c][blk] = Σ_j gm_j·stored(val);
+// with V2 != nullptr (FP16 operand) val goes to V2[c][j] in FP32 with its block maxima in xmax2,
+// for convert_snp_kernel to scale and split.  Blocks with c ≥ k zero the operand's padding rows.
 template <int V>
 __global__ void __launch_bounds__(kRedThreads)
-finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pad, int pieces, int k,
-                    int64_t m, const float* __restrict__ gm, const float* __restrict__ w,
-                    const double* __restrict__ cparts, int nblkc, int mode, float* __restrict__ out,
-                    int64_t ldo, int npieces2, void* B2, double* __restrict__ red, int nblk,
-                    const double* __restrict__ mparts, const float* __restrict__ gcorr, int64_t n_rows)
+finalize_snp_kernel(const float* __restrict__ D, int splits, int kp1, int64_t m_pad, int k, int64_t m,
+                    const float* __restrict__ gm, const float* __restrict__ w, const double* __restrict__ cparts,
+                    int nblkc, int mode, float* __restrict__ out, int64_t ldo, int npieces2, int kp2, void* B2,
+                    double* __restrict__ red, int nblk, const double* __restrict__ mparts,
+                    const float* __restrict__ gcorr, int64_t n_rows, const double* __restrict__ xmax1,
+                    float* __restrict__ V2, double* __restrict__ xmax2)
 {
   __shared__ double sh[32];
+  __shared__ float shf[32];
   __shared__ float sb[2];
-  __shared__ float smu;
+  __shared__ float smu, sisc;
   const int c = blockIdx.y;
   const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
   if (c >= k) {
-    zero_pad_row(B2, m_pad, npieces2 * k + (c - k), j0, j1);
+    zero_pad_row(B2, m_pad, pad_row(c - k, k, kp2, npieces2), j0, j1);
     return;
   }
   float ch, cl;
   block_scalar([&] { return sum_partials(cparts + (int64_t)c * nblkc, nblkc); }, sb, ch, cl);
-  if (mparts != nullptr) {   // the mean the prologue removed, added back as μ·(pc_j − n·gm_j)
-    if (threadIdx.x == 0) smu = column_mean(mparts, nblkc, c, 1.0 / (double)n_rows);
-    __syncthreads();
+  if (threadIdx.x == 0) {   // the mean the prologue removed, added back as μ·(pc_j − n·gm_j)
+    smu = mparts != nullptr ? column_mean(mparts, nblkc, c, 1.0 / (double)n_rows) : 0.f;
+    sisc = xmax1 != nullptr ? ldexpf(1.f, -f16_col_exp(xmax1, nblkc, c, smu)) : 1.f;
   }
+  __syncthreads();
   const float mu = mparts != nullptr ? smu : 0.f;
+  const float isc = sisc;
   DF acc;
+  float amax = 0.f;
   for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
     float val[V] = {}, g[V], e[V] = {};
     ldv<V>(gm + j, g);   // gm is zero-padded to m_pad
     if (mparts != nullptr) ldv<V>(gcorr + j, e);
     if (j < m) {
-      gather_D<V>(D, splits, N, m_pad, pieces, k, c, j, val);
+      gather_D<V>(D, splits, kp1, m_pad, c, j, isc, val);
       float ws[V];
       if (w) ldv<V>(w + j, ws);
 #pragma unroll
@@ -379,58 +493,124 @@ finalize_snp_kernel(const float* __restrict__ D, int splits, int N, int64_t m_pa
     }
     if (mode == 0) {
       if (j < m) stv<V>(out + (int64_t)c * ldo + j, val);
+    } else if (V2 != nullptr) {
+      stv<V>(V2 + (int64_t)c * m_pad + j, val);
+#pragma unroll
+      for (int u = 0; u < V; ++u) amax = fmaxf(amax, fabsf(val[u]));
     } else {
-      store_operand<V, true>(val, npieces2, B2, m_pad, k, c, j, acc, g);
+      store_operand<V, true>(val, npieces2, B2, m_pad, kp2, c, j, acc, g);
     }
   }
   if (mode == 1) {
-    const double s = block_sum_d(df_value(acc), sh);
-    if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+    if (V2 != nullptr) {
+      const float mx = block_max_f(amax, shf);
+      if (threadIdx.x == 0) xmax2[(int64_t)c * nblk + blockIdx.x] = (double)mx;
+    } else {
+      const double s = block_sum_d(df_value(acc), sh);
+      if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+    }
   }
 }
 
-// Direction-2 operand straight from an m×k input (matvec): stored(in) and red = Σ gm·stored;
-// blocks with c ≥ k zero BF16 padding rows.
+// FP16 direction-2 operand from the FP32 values V2[c][j] (finalize_snp_kernel, mode 1): pieces of
+// V2·2^e2, e2 from the block maxima xmax2, and red[c][blk] = Σ_j gm_j·stored(val).
 template <int V>
 __global__ void __launch_bounds__(kRedThreads)
-prologue_snp_kernel(const float* __restrict__ in, int64_t ld, int64_t m, int64_t m_pad, int k,
-                    const float* __restrict__ gm, int npieces, void* B, double* __restrict__ red, int nblk)
+convert_snp_kernel(const float* __restrict__ V2, int64_t m_pad, int k, int kp2, const float* __restrict__ gm,
+                   int npieces, void* B, double* __restrict__ red, int nblk, const double* __restrict__ xmax2)
 {
   __shared__ double sh[32];
+  __shared__ float ssc[2];
   const int c = blockIdx.y;
   const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
-  if (c >= k) {
-    zero_pad_row(B, m_pad, npieces * k + (c - k), j0, j1);
-    return;
+  if (threadIdx.x == 0) {
+    const int e = f16_exp(max_partials(xmax2, nblk, c));
+    ssc[0] = ldexpf(1.f, e);
+    ssc[1] = ldexpf(1.f, -e);
   }
+  __syncthreads();
   DF acc;
   for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
-    float x[V] = {}, g[V];
-    if (j < m) ldv<V>(in + (int64_t)c * ld + j, x);
+    float x[V], g[V];
+    ldv<V>(V2 + (int64_t)c * m_pad + j, x);
     ldv<V>(gm + j, g);
-    store_operand<V, true>(x, npieces, B, m_pad, k, c, j, acc, g);
+    store_operand<V, true, true>(x, npieces, B, m_pad, kp2, c, j, acc, g, ssc[0], ssc[1]);
   }
   const double s = block_sum_d(df_value(acc), sh);
   if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
 }
 
-// Direction-2 finalize (rows = individuals): val = raw − t_c (t from the direction-1 partials),
-// times rr_i when rr != nullptr, plus tau0·Vin for columns c ≥ nq when Vin != nullptr.
+// Direction-2 operand straight from an m×k input (matvec): stored(in) and red = Σ gm·stored;
+// blocks with c ≥ k zero the padding rows.  F16: MEASURE writes the block maxima of |in| to
+// xmax, and the store pass scales each column by 2^e from them.
+template <int V, bool MEASURE = false, bool F16 = false>
+__global__ void __launch_bounds__(kRedThreads)
+prologue_snp_kernel(const float* __restrict__ in, int64_t ld, int64_t m, int64_t m_pad, int k, int kp,
+                    const float* __restrict__ gm, int npieces, void* B, double* __restrict__ red, int nblk,
+                    double* __restrict__ xmax)
+{
+  __shared__ double sh[32];
+  __shared__ float shf[32];
+  __shared__ float ssc[2];
+  const int c = blockIdx.y;
+  const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
+  if (c >= k) {
+    if (!MEASURE) zero_pad_row(B, m_pad, pad_row(c - k, k, kp, npieces), j0, j1);
+    return;
+  }
+  if (F16 && !MEASURE) {
+    if (threadIdx.x == 0) {
+      const int e = f16_exp(max_partials(xmax, nblk, c));
+      ssc[0] = ldexpf(1.f, e);
+      ssc[1] = ldexpf(1.f, -e);
+    }
+    __syncthreads();
+  }
+  DF acc;
+  float amax = 0.f;
+  for (int64_t j = j0 + threadIdx.x * V; j < j1; j += kRedThreads * V) {
+    float x[V] = {}, g[V];
+    if (j < m) ldv<V>(in + (int64_t)c * ld + j, x);
+    if (MEASURE) {
+#pragma unroll
+      for (int u = 0; u < V; ++u) amax = fmaxf(amax, fabsf(x[u]));
+      continue;
+    }
+    ldv<V>(gm + j, g);
+    if (F16) store_operand<V, true, true>(x, npieces, B, m_pad, kp, c, j, acc, g, ssc[0], ssc[1]);
+    else store_operand<V, true>(x, npieces, B, m_pad, kp, c, j, acc, g);
+  }
+  if (MEASURE) {
+    const float mx = block_max_f(amax, shf);
+    if (threadIdx.x == 0) xmax[(int64_t)c * nblk + blockIdx.x] = (double)mx;
+    return;
+  }
+  const double s = block_sum_d(df_value(acc), sh);
+  if (threadIdx.x == 0) red[(int64_t)c * nblk + blockIdx.x] = s;
+}
+
+// Direction-2 finalize (rows = individuals): val = raw·2^−e2 − t_c (t from the direction-1
+// partials; e2 the FP16 scale of operand column c when xmax2 != nullptr), times rr_i when
+// rr != nullptr, plus tau0·Vin for columns c ≥ nq when Vin != nullptr.
 template <int V>
 __global__ void __launch_bounds__(kRedThreads)
-finalize_indiv_kernel(const float* __restrict__ D, int splits, int N, int64_t n_pad, int pieces, int k,
+finalize_indiv_kernel(const float* __restrict__ D, int splits, int kp2, int64_t n_pad, int k,
                       int64_t n, const double* __restrict__ tparts, int nblkt, const float* __restrict__ rr,
                       const float* __restrict__ Vin, int64_t ld_v, float tau0, int nq, float* __restrict__ out,
-                      int64_t ldo)
+                      int64_t ldo, const double* __restrict__ xmax2)
 {
   __shared__ float sb[2];
+  __shared__ float sisc;
   const int c = blockIdx.y;
   float th, tl;
   block_scalar([&] { return sum_partials(tparts + (int64_t)c * nblkt, nblkt); }, sb, th, tl);
+  if (threadIdx.x == 0) sisc = xmax2 != nullptr ? ldexpf(1.f, -f16_exp(max_partials(xmax2, nblkt, c))) : 1.f;
+  __syncthreads();
+  const float isc = sisc;
   const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
   if (i >= n) return;
   float val[V];
-  gather_D<V>(D, splits, N, n_pad, pieces, k, c, i, val);
+  gather_D<V>(D, splits, kp2, n_pad, c, i, isc, val);
   float r[V], v[V];
   if (rr) ldv<V>(rr + i, r);
   const bool addv = Vin != nullptr && c >= nq;
@@ -448,8 +628,10 @@ finalize_indiv_kernel(const float* __restrict__ D, int splits, int N, int64_t n_
 // ---- one packed pass ---------------------------------------------------------------------------------
 struct PassPlan {
   bool tc;
-  int pieces;   // BF16 pieces (tc) or 1 (simt)
-  int N;        // columns of D
+  bool f16;     // FP16 pieces with per-column scales (tc)
+  int pieces;   // 16-bit pieces per column (tc) or 1 (simt)
+  int kp;       // rows between a column's pieces (k rounded up to 8) and columns of D per split
+  int N;        // columns of the product
   int splits;
 };
 
@@ -468,8 +650,10 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
 {
   PassPlan p;
   p.tc = g->prec != SLEMM_PREC_FP32;
-  p.pieces = g->prec == SLEMM_PREC_BF16X3 ? 3 : (g->prec == SLEMM_PREC_BF16X2 ? 2 : 1);
-  p.N = p.tc ? (int)round_up((int64_t)p.pieces * k, 16) : k;
+  p.f16 = g->prec == SLEMM_PREC_FP16X2;
+  p.pieces = g->prec == SLEMM_PREC_BF16X3 ? 3 : (p.tc ? 2 : 1);
+  p.kp = p.tc ? (int)round_up(k, 8) : k;
+  p.N = p.tc ? (int)round_up((int64_t)p.pieces * p.kp, 16) : k;
   const int64_t M_tiles = M_pad / kTileM, K_tiles = K_pad / kTileK;
   p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(),
                                   tc_min_splits(K_tiles, p.N))
@@ -480,7 +664,7 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
 static int max_group(const slemm_geno* g)
 {
   if (g->per_vector) return 1;
-  if (g->prec == SLEMM_PREC_BF16X2) return 128;
+  if (g->prec == SLEMM_PREC_BF16X2 || g->prec == SLEMM_PREC_FP16X2) return 128;
   if (g->prec == SLEMM_PREC_BF16X3) return 80;
   return 64;
 }
@@ -522,7 +706,7 @@ void profile_collect(slemm_geno* g)
 static void run_gemm(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t M_pad,
                      int64_t K_pad, const void* B, float* D, int* err, int k, int dir)
 {
-  GemmArgs a{A, M_pad, K_pad, B, p.N, D, p.splits, err};
+  GemmArgs a{A, M_pad, K_pad, B, p.N, D, p.splits, err, p.kp, p.pieces, p.f16};
   slemm_geno::GemmRecord rec{};
   if (g->profiling) {
     if (g->prof_pending.size() >= 512) profile_collect(g);
@@ -554,28 +738,37 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   const PassPlan p1 = plan_pass(g, k, g->m_pad, g->n_pad);             // M = SNPs, K = indiv
   const PassPlan p2 = plan_pass(g, k, g->n_pad, g->m_pad);             // M = indiv, K = SNPs
   const int np1 = p1.tc ? p1.pieces : 0, np2 = p2.tc ? p2.pieces : 0;
-  const int pad1 = p1.tc ? p1.N - p1.pieces * k : 0;                   // BF16 padding rows
+  const int pad1 = p1.tc ? p1.N - p1.pieces * k : 0;                   // padding rows of the operands
   const int pad2 = p2.tc ? p2.N - p2.pieces * k : 0;
+  const bool f16 = p1.f16;
   const size_t b1 = dir1 ? (p1.tc ? (size_t)p1.N * g->n_pad * 2 : (size_t)k * g->n_pad * 4) : 0;
   const size_t b2 = dir2 ? (p2.tc ? (size_t)p2.N * g->m_pad * 2 : (size_t)k * g->m_pad * 4) : 0;
-  uint8_t* Bbuf = (uint8_t*)g->ws_B.ensure(b1 + b2);
+  // FP16: the direction-2 values in FP32 before they are scaled and split
+  const size_t bv2 = (dir1 && dir2 && f16) ? (size_t)k * g->m_pad * 4 : 0;
+  uint8_t* Bbuf = (uint8_t*)g->ws_B.ensure(b1 + b2 + bv2);
   void* B1 = Bbuf;
   void* B2 = Bbuf + b1;
-  const size_t d1 = dir1 ? (size_t)p1.splits * p1.N * g->m_pad : 0;
-  const size_t d2 = dir2 ? (size_t)p2.splits * p2.N * g->n_pad : 0;
+  float* V2 = bv2 ? (float*)(Bbuf + b1 + b2) : nullptr;
+  const size_t d1 = dir1 ? (size_t)p1.splits * p1.kp * g->m_pad : 0;
+  const size_t d2 = dir2 ? (size_t)p2.splits * p2.kp * g->n_pad : 0;
   float* D = (float*)g->ws_D.ensure(std::max(d1, d2) * sizeof(float));
   const int nblk_n = (int)ceil_div(g->n_pad, kRowsPerBlock);
   const int nblk_m = (int)ceil_div(g->m_pad, kRowsPerBlock);
   const int nblk_q = (int)ceil_div(g->n, kRowsPerBlock);
-  // partials: colsum [k][nblk_n] | tsum [k][nblk_m] | QᵀV [c·nq][nblk_q] | QᵀT [c·nq][nblk_q]
+  // partials: colsum [k][nblk_n] | tsum [k][nblk_m] | QᵀV [c·nq][nblk_q] | QᵀT [c·nq][nblk_q] |
+  // column sums for the means [k][nblk_n] | FP16 ranges: operand 1 signed extremes [k][nblk_n][2],
+  // operand 2 maxima of |x| [k][nblk_m]
   const int cq = g->c;
   CHECK_ARG(cq <= 64, "more than 64 covariates");
-  const size_t nred = 2 * (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q;
+  const size_t nred = 2 * (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q +
+                      (f16 ? (size_t)k * (2 * nblk_n + nblk_m) : 0);
   double* r_col = (double*)g->ws_red.ensure(nred * sizeof(double));
   double* r_t = r_col + (size_t)k * nblk_n;
   double* r_qv = r_t + (size_t)k * nblk_m;
   double* r_qt = r_qv + (size_t)std::max(cq, 1) * k * nblk_q;
   double* r_mu = r_qt + (size_t)std::max(cq, 1) * k * nblk_q;   // column sums for the means [k][nblk_n]
+  double* x_max1 = f16 ? r_mu + (size_t)k * nblk_n : nullptr;        // [k][nblk_n][2]
+  double* x_max2 = f16 ? x_max1 + 2 * (size_t)k * nblk_n : nullptr;  // [k][nblk_m]
   int* err = g->err.as<int>();
 
   // H0 operators: the first nq columns are projected (H0_quadform_mv), the rest are not (H0_ldet_mv)
@@ -591,22 +784,36 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     const float* Qp = g->Q.as<float>();
     const double* qp = proj ? r_qv : nullptr;
     double* const mu = g->gcorr.p ? r_mu : nullptr;   // mean removal needs Z_cᵀ1 (set with the weights)
-    if (vin) {
-      if (mu) {
+    if (mu || f16) {
+      // measure pass: column sums (for the means) and, for FP16 operands, the column maxima
+      if (vin)
         prologue_indiv_kernel<4, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
-            in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_mu, nblk_n, nullptr);
-        LAUNCH_CHECK();
-      }
-      prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp,
-                                                                    nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu);
-    } else {
-      if (mu) {
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, mu, nblk_n, nullptr,
+            x_max1);
+      else
         prologue_indiv_kernel<1, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
-            in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_mu, nblk_n, nullptr);
-        LAUNCH_CHECK();
-      }
-      prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(in, ld_in, g->n, g->n_pad, k, Qp, g->n_pad, cq, qp,
-                                                                    nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu);
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, mu, nblk_n, nullptr,
+            x_max1);
+      LAUNCH_CHECK();
+    }
+    if (f16) {
+      if (vin)
+        prologue_indiv_kernel<4, false, true><<<grid, kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
+            x_max1);
+      else
+        prologue_indiv_kernel<1, false, true><<<grid, kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
+            x_max1);
+    } else {
+      if (vin)
+        prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
+            nullptr);
+      else
+        prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(
+            in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
+            nullptr);
     }
     LAUNCH_CHECK();
     // ---- pass 1: Cntᵀ over individuals ----
@@ -615,30 +822,54 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
     const float* wsc = (kind == SLEMM_OP_RMATVEC) ? nullptr : g->w.as<float>();
     if (h0) {
       finalize_snp_kernel<4><<<dim3(nblk_m, k + pad2), kRedThreads, 0, st>>>(
-          D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 1, nullptr, 0,
-          np2, B2, r_t, nblk_m, mu, g->gcorr.as<float>(), g->n);
+          D, p1.splits, p1.kp, g->m_pad, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 1, nullptr, 0, np2, p2.kp,
+          B2, r_t, nblk_m, mu, g->gcorr.as<float>(), g->n, x_max1, V2, x_max2);
       LAUNCH_CHECK();
+      if (f16) {
+        convert_snp_kernel<4><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(V2, g->m_pad, k, p2.kp, g->gm.as<float>(),
+                                                                        np2, B2, r_t, nblk_m, x_max2);
+        LAUNCH_CHECK();
+      }
     } else {
       if (vec4_ok(g->m, ld_out, out))
         finalize_snp_kernel<4><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
-            D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
-            0, nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n);
+            D, p1.splits, p1.kp, g->m_pad, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out, 0, 8,
+            nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n, x_max1, nullptr, nullptr);
       else
         finalize_snp_kernel<1><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
-            D, p1.splits, p1.N, g->m_pad, p1.pieces, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out,
-            0, nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n);
+            D, p1.splits, p1.kp, g->m_pad, k, g->m, g->gm.as<float>(), wsc, r_col, nblk_n, 0, out, ld_out, 0, 8,
+            nullptr, nullptr, 0, mu, g->gcorr.as<float>(), g->n, x_max1, nullptr, nullptr);
       LAUNCH_CHECK();
       return;
     }
   } else {
     // matvec: operand straight from the m×k input
     dim3 gridm(nblk_m, k + pad2);
-    if (vec4_ok(g->m, ld_in, in))
-      prologue_snp_kernel<4><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, g->gm.as<float>(), np2, B2,
-                                                            r_t, nblk_m);
-    else
-      prologue_snp_kernel<1><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, g->gm.as<float>(), np2, B2,
-                                                            r_t, nblk_m);
+    const bool v4 = vec4_ok(g->m, ld_in, in);
+    if (f16) {
+      if (v4) {
+        prologue_snp_kernel<4, true, true><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
+            in, ld_in, g->m, g->m_pad, k, p2.kp, g->gm.as<float>(), np2, B2, r_t, nblk_m, x_max2);
+        LAUNCH_CHECK();
+        prologue_snp_kernel<4, false, true><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, p2.kp,
+                                                                           g->gm.as<float>(), np2, B2, r_t, nblk_m,
+                                                                           x_max2);
+      } else {
+        prologue_snp_kernel<1, true, true><<<dim3(nblk_m, k), kRedThreads, 0, st>>>(
+            in, ld_in, g->m, g->m_pad, k, p2.kp, g->gm.as<float>(), np2, B2, r_t, nblk_m, x_max2);
+        LAUNCH_CHECK();
+        prologue_snp_kernel<1, false, true><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, p2.kp,
+                                                                           g->gm.as<float>(), np2, B2, r_t, nblk_m,
+                                                                           x_max2);
+      }
+    } else {
+      if (v4)
+        prologue_snp_kernel<4><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, p2.kp, g->gm.as<float>(),
+                                                              np2, B2, r_t, nblk_m, nullptr);
+      else
+        prologue_snp_kernel<1><<<gridm, kRedThreads, 0, st>>>(in, ld_in, g->m, g->m_pad, k, p2.kp, g->gm.as<float>(),
+                                                              np2, B2, r_t, nblk_m, nullptr);
+    }
     LAUNCH_CHECK();
   }
   // ---- pass 2: Cnt over SNPs ----
@@ -650,12 +881,12 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   const int nq2 = (kind == SLEMM_OP_MATVEC) ? 0 : nq;
   if (vec4_ok(g->n, ld_out, out) && (!v2 || vin)) {
     dim3 grid((unsigned)ceil_div(g->n, 4 * kRedThreads), k);
-    finalize_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n, r_t,
-                                                           nblk_m, rr2, v2, ld_in, tau0, nq2, out, ld_out);
+    finalize_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.kp, g->n_pad, k, g->n, r_t, nblk_m, rr2,
+                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2);
   } else {
     dim3 grid((unsigned)ceil_div(g->n, kRedThreads), k);
-    finalize_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.N, g->n_pad, p2.pieces, k, g->n, r_t,
-                                                           nblk_m, rr2, v2, ld_in, tau0, nq2, out, ld_out);
+    finalize_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.kp, g->n_pad, k, g->n, r_t, nblk_m, rr2,
+                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2);
   }
   LAUNCH_CHECK();
   // quadform columns 0 … nq−1: out = T + τ0 v − QQᵀT
@@ -688,12 +919,14 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     const int kc = std::min(grp, k - c0);
     PassPlan p;
     p.tc = true;
+    p.f16 = false;
     p.pieces = pieces;
-    p.N = (int)round_up((int64_t)pieces * kc, 16);
+    p.kp = (int)round_up(kc, 8);
+    p.N = (int)round_up((int64_t)pieces * p.kp, 16);
     p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(), tc_min_splits(K_tiles, p.N));
     const int pad = p.N - pieces * kc;
     void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
-    float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.N * rows * sizeof(float));
+    float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.kp * rows * sizeof(float));
     double* r_col = (double*)g->ws_red.ensure(2 * (size_t)kc * nblk_n * sizeof(double));
     double* r_mu = r_col + (size_t)kc * nblk_n;
     double* const mu = g->gcorr.p ? r_mu : nullptr;
@@ -701,31 +934,35 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     if (vec4_ok(g->n, ldu, in)) {
       if (mu) {
         prologue_indiv_kernel<4, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
-            in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n, nullptr);
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n,
+            nullptr, nullptr);
         LAUNCH_CHECK();
       }
       prologue_indiv_kernel<4, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu);
+          in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+          nullptr);
     } else {
       if (mu) {
         prologue_indiv_kernel<1, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
-            in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n, nullptr);
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n,
+            nullptr, nullptr);
         LAUNCH_CHECK();
       }
       prologue_indiv_kernel<1, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu);
+          in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+          nullptr);
     }
     LAUNCH_CHECK();
     run_gemm(g, p, A, rows, K_pad, B1, D, g->err.as<int>(), kc, 1);
     float* o = out + (int64_t)c0 * ldo;
     if (vec4_ok(m_valid, ldo, o))
       finalize_snp_kernel<4><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
-          D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
-          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n);
+          D, p.splits, p.kp, rows, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0, 8,
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, nullptr, nullptr, nullptr);
     else
       finalize_snp_kernel<1><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
-          D, p.splits, p.N, rows, pieces, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0,
-          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n);
+          D, p.splits, p.kp, rows, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0, 8,
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, nullptr, nullptr, nullptr);
     LAUNCH_CHECK();
   }
 }

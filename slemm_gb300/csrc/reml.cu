@@ -283,6 +283,16 @@ static void upload(slemm_geno* g, float* d, const float* h, size_t cnt)
   CUDA_TRY(cudaMemcpyAsync(d, h, cnt * sizeof(float), cudaMemcpyHostToDevice, g->stream));
 }
 
+// The search's evaluation points and criterion values into the result (the first SLEMM_TRACE_MAX).
+static void store_trace(slemm_reml_result* res, const std::vector<std::pair<float, double>>& tr)
+{
+  res->n_points = (int)std::min<size_t>(tr.size(), SLEMM_TRACE_MAX);
+  for (int q = 0; q < res->n_points; ++q) {
+    res->h2_points[q] = tr[q].first;
+    res->f_points[q] = tr[q].second;
+  }
+}
+
 // ================================================================================================
 // DF-REML
 // ================================================================================================
@@ -377,6 +387,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   lanczos_moments(seed, pairs, Jm, mom);
   const double ySy = mom[0];
   int n_eval = 0;
+  std::vector<std::pair<float, double>> trace;
   // REML_criterion (src/reml.cpp:457-489)
   auto criterion = [&](float ss) -> Criterion {
     ++n_eval;
@@ -400,6 +411,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
         for (int l = 0; l < c; ++l)
           M[(size_t)k * c + l] += cq[(size_t)i * c + l] * mom[(size_t)i * npairs + 1 + k * c + l];
     r.slogLL = (double)(n - c) * std::log(ySy / yPy) - logabsdet(M, c) - ldet_H;
+    trace.push_back({ss, r.slogLL});
     return r;
   };
   // REML_GSS (src/reml.cpp:493-547)
@@ -516,6 +528,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     res->iters_Q = lseed_iters(seed, GQ);
     res->iters_V = nld;
     res->n_criterion = n_eval;
+    store_trace(res, trace);
     res->seconds = stamp();
     res->t_setup = t_a;
     res->t_seed = t_b - t_a;
@@ -586,6 +599,7 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
                                             o.maxit, verbose, {}, 5);
   std::unique_ptr<slemm_lseed, void (*)(slemm_lseed*)> hold(seed_V, lseed_free);
   int n_eval = 0;
+  std::vector<std::pair<float, double>> trace;
   // REML_first_order (src/reml.cpp:696-728); leaves rr-scaled Py in d_Py
   auto first_order = [&](float ss) -> float {
     ++n_eval;
@@ -608,7 +622,9 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
       es += h[q];
       us += h[1 + n_MC + q];
     }
-    return (float)std::log((u0 / e0) / (us / es));
+    const float f = (float)std::log((u0 / e0) / (us / es));
+    trace.push_back({ss, (double)f});
+    return f;
   };
   const double t_b = stamp();
   if (verbose) printf("\nSecant iterations:\n");
@@ -696,6 +712,7 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
     res->iters_y = res->iters_Q = 0;
     res->iters_V = lseed_iters(seed_V, 0);
     res->n_criterion = n_eval;
+    store_trace(res, trace);
     res->seconds = stamp();
     res->t_setup = t_a;
     res->t_seed = t_b - t_a;

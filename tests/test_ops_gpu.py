@@ -6,6 +6,7 @@ error ‖out − ref‖/‖ref‖:
   FP32 CUDA-core path              ≤ 2e-6
   BF16 hi+lo tensor-core path      ≤ 4e-5
   BF16 hi+mid+lo tensor-core path  ≤ 2e-6
+  FP16 hi+lo (column-scaled) path  ≤ 2e-6
 """
 import numpy as np
 import pytest
@@ -16,7 +17,7 @@ from slemm_gb300 import _lib, api
 
 pytestmark = pytest.mark.gpu
 
-TOL = {_lib.PREC_FP32: 2e-6, _lib.PREC_BF16X2: 4e-5, _lib.PREC_BF16X3: 2e-6}
+TOL = {_lib.PREC_FP32: 2e-6, _lib.PREC_BF16X2: 4e-5, _lib.PREC_BF16X3: 2e-6, _lib.PREC_FP16X2: 2e-6}
 
 
 def relerr(a, b):
@@ -59,7 +60,43 @@ def _setup(n_fam, m, seed, keep=1.0, c=2):
 CASES = [(1000, 700, 1.0), (1537, 1300, 0.9)]
 
 
-@pytest.mark.parametrize("prec", [_lib.PREC_FP32, _lib.PREC_BF16X2, _lib.PREC_BF16X3])
+@pytest.mark.parametrize("prec", [_lib.PREC_FP16X2, _lib.PREC_BF16X2, _lib.PREC_BF16X3])
+@pytest.mark.parametrize("k", [1, 7, 66, 130])
+def test_column_scales_and_piece_layout(gpu, prec, k):
+    """Columns of very different magnitudes (1e-30 … 1e30, a zero column, a column with a large
+    mean) in one block: FP16 pieces are scaled per column by a power of two, so every column keeps
+    its own relative accuracy; k not a multiple of 8 exercises the padding rows between pieces and
+    the epilogue's sum of a column's pieces.  Per-column relative error ≤ the path's tolerance."""
+    rows, keep_idx, dec, gm, w, rr, Q = _setup(900, 650, seed=19)
+    n, m = dec.shape[1], dec.shape[0]
+    ref = orc.Operators(dec, gm, w, rr, Q, dtype=np.float64)
+    rng = np.random.default_rng(23)
+    # BF16 shares FP32's exponent range but its lo piece of a 1e-30 value is near FP32's
+    # smallest normal; FP16 columns are rescaled, so they take the whole range
+    exps = (-30, -12, -3, 0, 4, 12, 30) if prec == _lib.PREC_FP16X2 else (-12, -3, 0, 4, 12)
+    scales = np.array([10.0 ** e for e in exps])
+    v = rng.standard_normal((n, k)) * scales[np.arange(k) % scales.size]
+    if k > 3:
+        v[:, 2] = 0.0
+        v[:, 3] += 50.0   # large mean
+    u = rng.standard_normal((m, k)) * scales[(np.arange(k) + 3) % scales.size]
+    v = v.astype(np.float32)
+    u = u.astype(np.float32)
+    with api.Genotypes(rows, 900, keep_idx) as g:
+        g.set_weights(gm, w, rr)
+        g.set_projection(Q)
+        g.set_precision(prec)
+        tol = TOL[prec]
+        for got, want in ((g.rmatvec(v), ref.rmatvec(v)), (g.matvec(u), ref.matvec(u)),
+                          (g.H0_ldet_mv(0.5, v), ref.H0_ldet_mv(0.5, v))):
+            for c in range(k):
+                if np.any(want[:, c] != 0):
+                    assert relerr(got[:, c], want[:, c]) < tol, (c, relerr(got[:, c], want[:, c]))
+                else:
+                    assert np.all(got[:, c] == 0)
+
+
+@pytest.mark.parametrize("prec", [_lib.PREC_FP32, _lib.PREC_BF16X2, _lib.PREC_BF16X3, _lib.PREC_FP16X2])
 @pytest.mark.parametrize("n_fam,m,keep", CASES)
 def test_operators_vs_oracle(gpu, prec, n_fam, m, keep):
     rows, keep_idx, dec, gm, w, rr, Q = _setup(n_fam, m, seed=7, keep=keep)

@@ -45,6 +45,7 @@ def test_noalloc_matches_allocating_entry_point_twice(gpu):
                             generator=torch.Generator("cuda").manual_seed(call))
             ref = torch.zeros(k, m, device="cuda", dtype=torch.float32)
             out = torch.full((k, m), float("nan"), device="cuda", dtype=torch.float32)
+            torch.cuda.synchronize()   # v, ref and out are written on torch's stream, read on the handle's
             g.op_device(_lib.OP_RMATVEC, v, ref)
             torch.cuda.synchronize()
             st = noalloc(g.h, ctypes.c_void_p(v.data_ptr()), n, k, ctypes.c_void_p(out.data_ptr()), m)
@@ -71,6 +72,7 @@ def test_noalloc_constant_column_is_exact(gpu):
         stream = torch.cuda.ExternalStream(g.stream())
         v = torch.full((1, n), 0.37, device="cuda", dtype=torch.float32)
         out = torch.zeros(1, m, device="cuda", dtype=torch.float32)
+        torch.cuda.synchronize()   # written on torch's stream, read on the handle's
         _lib.check(noalloc(g.h, ctypes.c_void_p(v.data_ptr()), n, 1, ctypes.c_void_p(out.data_ptr()), m))
         stream.synchronize()
     want = np.float32(0.37) * (pc.astype(np.float64) - n * gm.astype(np.float64))
