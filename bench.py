@@ -1,24 +1,30 @@
-"""Benchmark of the GB300 engine on SLEMM's DF-REML + SNP-BLUP path.
+"""Benchmark of the GB300 engine on SLEMM's REML + SNP-BLUP path.
 
-Workload (the benchmark's plain-FP32-vs-batched configuration): n = 100,000 individuals,
-m = 50,000 SNPs in a packed PLINK .bed (Binomial(2, p), p ~ U(0.05, 0.5), LD-free), h² = 0.4,
-one trait, intercept only; `slemm --reml --lrt` with 64 Rademacher probes (DF-REML: Lanczos seeds
-for y and [Q V], golden-section search on h², BLUP, BLUE).  Synthetic data, seed 1.
+Default workload (the metric's own configuration): n = 500,000 individuals, m = 60,000 SNPs in a
+packed PLINK .bed with block LD (AR(1) latent correlation 0.6 within 50-SNP blocks, thresholded to
+0/1/2), h² = 0.3, one trait, intercept only; `slemm --reml --lrt --iter_weighting
+--window_size 50` with 64 Rademacher probes: an MC-REML equal-weight stage, window weights from
+its SNP-BLUP (1,200 windows), fixed-effect SNPs by clumping, then the window-weighted DF-REML
+(Lanczos seeds for y, Q and the probe block, golden-section search on h²), BLUP and BLUE.
+Synthetic data, seed 1.  `--config N` selects the other workloads (see CONFIGS).
 
-One step = one REML + BLUP fit through the C ABI.
+One step = one whole fit through the C ABI.
   value  — device-timed (CUDA events on the library stream) wall time of one fit with the
-           packed genotypes already resident in HBM (packed Z is 1.25 GB ≫ the 129 MB L2, so
-           every pass streams from HBM);
+           packed genotypes already resident in HBM (each packed pass streams Z from HBM: the
+           packed matrix is far larger than the 129 MB L2);
   e2e    — the same fit through the reference-facing calls with HOST buffers: genotype upload
-           from pinned host memory + fit + results back to the host, timed on the host;
+           from pinned staging + fit + results back to the host, timed on the host;
+  fp32_* — the plain FP32 GPU path (CUDA-core FP32 products, per vector by default) on the same
+           fit: its time (the speed-up) and its h² (dh2_vs_fp32, the metric's precision bar);
   roofline — the dominant packed-product kernel, measured per launch with CUDA events during
            the timed steps;
-  cpu_baseline — the NumPy FP32 restatement of the reference operators on this host's cores,
-           timed on a bounded sample and extrapolated with the fit's Lanczos step counts.
+  cpu_baseline — the reference's operator loop restated on this host's cores (threaded C
+           decode of each 1000-SNP subset + OpenBLAS SGEMMs) timed at full n on a bounded sample
+           of subsets, times this fit's operator applications.
   integer_stages — decode, popcounts and class counts: the GPU pack from rows in HBM vs the C
            restatement on this host's cores (bounded sample, scaled).
-`--impl reference` times the reference's CPU path (the oracle port; the reference itself does
-not build here) on the same workload, on this host's cores.
+`--impl reference` times that CPU loop on the same workload on this host's cores, with the step
+counts of the FP32 GPU fit (REF_STEPS).
 """
 from __future__ import annotations
 
@@ -234,29 +240,98 @@ def make_inputs(cfg, device="cuda"):
 
 
 # ------------------------------------------------------------------------------------------------
-# CPU path (oracle port): bounded sample of operator applications, extrapolated
+# CPU path (oracle port): the reference's subset loop timed at full n, one cost model for both the
+# reference arm and the GPU arm's cpu_baseline
 # ------------------------------------------------------------------------------------------------
-def cpu_operator_sample(rows_np, n, m, probes, subsets=4):
-    """Times H0_ldet_mv on the [Q V] block (1 + probes columns) and H0_quadform_mv on y over
-    `subsets` SNP subsets of 1000 and scales to all m SNPs.  Returns (s_ldet, s_quad, info)."""
+SUBSET = 1000   # the reference's SNP subset size (--subset_size default, src/option.cpp:53-78)
+
+# Lanczos step counts and criterion evaluations of the plain FP32 path (CUDA-core FP32 products,
+# the reference's arithmetic) on each workload, as the GPU arm's `fp32_*.counts` reports them: the
+# reference arm multiplies its measured per-application times by these.
+REF_STEPS = {
+    2: None,
+    3: None,
+}
+
+
+def cpu_app_model(rows_np, n, probes, subsets, start=0, threads=None):
+    """Per-subset cost of the reference's operator loop (src/reml.cpp:28-47: decode 1000 SNPs of
+    kmat into a centred FP32 block, then SGEMMs) at full n, measured on `subsets` consecutive
+    subsets of 1000 packed .bed rows from subset `start`: H0_ldet_mv on 1 + probes columns and
+    H0_quadform_mv on one column, fitted as t = a + passes·b·k per subset (a: the decode, b: SGEMM
+    time per column and pass).  Returns (a, b, measured seconds, description)."""
     from oracle import slemm_np as orc
+    threads = threads or os.cpu_count() or 1
+    nsub = max(1, rows_np.shape[0] // SUBSET)
+    subsets = max(1, min(subsets, nsub))
+    s0 = start % (nsub - subsets + 1)
+    rows_s = rows_np[s0 * SUBSET:(s0 + subsets) * SUBSET]   # a view: consecutive rows
     rng = np.random.default_rng(0)
-    gm = rng.uniform(0.1, 0.9, m).astype(np.float32)     # values do not change the timing
-    w = np.full(m, 1.0 / m, np.float32)
+    ms = rows_s.shape[0]
+    gm = rng.uniform(0.1, 0.9, ms).astype(np.float32)        # values do not change the timing
+    w = np.full(ms, 1.0 / ms, np.float32)
     Q = np.full((n, 1), 1.0 / np.sqrt(n), np.float32)
-    ops = orc.PackedOperators(rows_np, n, gm, w, None, Q, subset_size=1000, dtype=np.float32)
-    ops.subset_limit = subsets
-    scale = (m / 1000.0) / subsets
+    ops = orc.PackedOperators(rows_s, n, gm, w, None, Q, subset_size=SUBSET, dtype=np.float32, threads=threads)
     V = rng.standard_normal((n, 1 + probes)).astype(np.float32)
     t0 = time.perf_counter()
     ops.H0_ldet_mv(0.4285714, V)
-    s_ldet = (time.perf_counter() - t0) * scale
-    v = V[:, :1].copy()
+    t_wide = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ops.H0_quadform_mv(0.4285714, v)
-    s_quad = (time.perf_counter() - t0) * scale
-    info = f"{subsets} subsets of 1000 SNPs × {n} individuals per operator, scaled ×{scale:.1f}"
-    return s_ldet, s_quad, info
+    ops.H0_quadform_mv(0.4285714, V[:, :1].copy())
+    t_one = time.perf_counter() - t0
+    b = max((t_wide - t_one) / subsets / (2.0 * probes), 0.0)
+    a = max(t_one / subsets - 2.0 * b, 0.0)
+    info = (f"subsets {s0}..{s0 + subsets - 1} of {SUBSET} SNPs x {n} individuals on {threads} threads: H0_ldet_mv "
+            f"on {1 + probes} columns {t_wide:.2f} s, H0_quadform_mv on 1 column {t_one:.2f} s; per subset "
+            f"a={a:.4f} s (decode) + passes*k*{b:.6f} s (SGEMM)")
+    return a, b, t_wide + t_one, info
+
+
+def mc_samples(n):
+    """MC samples of an MC-REML first stage: max(min(4e9/n², 30), 3) (src/option.cpp:445)."""
+    return max(min(int(4e9 / n / n), 30), 3)
+
+
+def reference_applications(cfg, st):
+    """(what, passes, columns, count) of the operator applications the reference's algorithm makes
+    in one fit of the workload, from the step counts `st`: each Lanczos step of a seed applies its
+    operator to the seed's block (src/reml.cpp:293-322) and each application runs the whole subset
+    loop (quadform and ldet: decode once, two SGEMMs; matvec and rmatvec: one)."""
+    probes, c = cfg["probes"], st["c"]
+    apps = []
+    if cfg.get("window"):   # --iter_weighting, n ≥ 5000: MC-REML first stage (src/option.cpp:437-470)
+        k = st["n_mc"]
+        apps += [("MC-REML matvec of the MC draws", 1, k, 1),
+                 ("MC-REML L_Seed quadform [y|Zu|e]", 2, 1 + 2 * k, st["first_iters_V"]),
+                 ("MC-REML first-order rmatvec", 1, 1 + k, st["first_n_criterion"]),
+                 ("MC-REML SNP-BLUP + BLUE", 1, 1, 2)]
+    apps += [("DF-REML L_Seed quadform y", 2, 1, st["iters_y"]),
+             ("DF-REML L_Seed ldet Q", 2, c, st["iters_Q"]),
+             ("DF-REML L_Seed ldet V", 2, probes, st["iters_V"]),
+             ("DF-REML SNP-BLUP + BLUE", 1, 1, 2)]
+    return apps
+
+
+def reference_seconds(a, b, m, apps):
+    """Whole-fit seconds of the reference's loop: Σ count · (m/1000) · (a + passes·b·k)."""
+    return sum(cnt * (m / SUBSET) * (a + p * b * k) for _, p, k, cnt in apps)
+
+
+def fit_counts(cfg, res):
+    """Step counts of a GPU fit in the form reference_applications takes."""
+    st = dict(iters_y=int(res["iters"][0]), iters_Q=int(res["iters"][1]), iters_V=int(res["iters"][2]),
+              c=1 + len(res.get("fixed", [])))
+    if cfg.get("window"):
+        st.update(first_iters_V=int(res["first_stage"]["iters_V"]),
+                  first_n_criterion=int(res["first_stage"]["n_criterion"]), n_mc=mc_samples(cfg["n"]))
+    return st
+
+
+def cpu_operator_sample(rows_np, n, m, probes, subsets=4):
+    """Seconds of one full-m H0_ldet_mv on 1 + probes columns and one H0_quadform_mv on a column,
+    from cpu_app_model on `subsets` subsets.  Returns (s_ldet, s_quad, info)."""
+    a, b, _, info = cpu_app_model(rows_np, n, probes, subsets)
+    return (m / SUBSET) * (a + 2 * b * (1 + probes)), (m / SUBSET) * (a + 2 * b), info
 
 
 def cpu_integer_sample(rows_np, n, m, threads, rows_max=4000):
@@ -281,55 +356,71 @@ def cpu_integer_sample(rows_np, n, m, threads, rows_max=4000):
 
 
 def cpu_threads():
-    try:
-        from threadpoolctl import threadpool_info
-        return max(i.get("num_threads", 1) for i in threadpool_info()) or os.cpu_count()
-    except Exception:
-        return os.cpu_count()
+    return os.cpu_count() or 1
+
+
+def l2_note(n, m):
+    """How the timed passes relate to the 129 MB L2: every packed pass streams Z from HBM."""
+    return (f"inputs larger than L2: each packed pass streams Z ({m * ((n + 3) // 4) / 1e9:.2f} GB packed) "
+            f"from HBM, 129 MB L2")
+
+
+def gpu_config(cfg, precision):
+    """The `config` object both arms print for the workload."""
+    n, m = cfg["n"], cfg["m"]
+    out = {"workload": cfg["name"], "n": n, "m": m, "probes": cfg["probes"], "h2_sim": cfg["h2"]}
+    if cfg.get("window"):
+        out.update(ld_rho=cfg["ld_rho"], ld_block=cfg["ld_block"], window_size=cfg["window"])
+    out.update(precision=precision, l2=l2_note(n, m), parallelism="replicas")
+    return out
 
 
 def run_reference(args, cfg):
-    """CPU reference arm: the oracle port of the reference's DF-REML on this host."""
+    """CPU reference arm: the oracle port of the reference's operator loop (threaded C decode of
+    each 1000-SNP subset + OpenBLAS SGEMMs, the structure of src/reml.cpp:28-47) timed at full n on
+    this host's cores.  Each timed step measures the loop on a block of consecutive subsets (the
+    blocks rotate over the whole .bed across the steps) and turns it into the whole fit's seconds
+    with the workload's application counts (reference_applications, REF_STEPS)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle import slemm_np as orc
-    from slemm_gb300 import synth
     n, m, probes = cfg["n"], cfg["m"], cfg["probes"]
-    # packed rows for the timing sample (NumPy generator; values do not affect CPU time)
+    st = REF_STEPS.get(args.config)
+    if st is None:
+        print(json.dumps({"impl": "reference", "unavailable": "no FP32 step counts recorded for this workload"}),
+              flush=True)
+        return
+    apps = reference_applications(cfg, st)
     rng = np.random.default_rng(1)
-    nb = (n + 3) // 4
-    rows_np = rng.integers(0, 256, size=(min(m, 4000), nb), dtype=np.uint8)   # timing only
-    # Lanczos step counts of the reference algorithm from a ratio-preserving 1/10 problem
-    small_n, small_m = max(n // 10, 500), max(m // 10, 500)
-    counts, _ = synth.simulate_counts(small_n, small_m, seed=1)
-    y, _, _ = synth.simulate_phenotype(counts, cfg["h2"], n_causal=min(1000, small_m), seed=1)
-    t0 = time.perf_counter()
-    rr = orc.SLDF_REML(counts, None, np.ones((small_n, 1)), y, np.ones(small_m), seed=0, n_V=probes,
-                       dtype=np.float32)
-    it_y, it_q, it_v = rr["iters"]
-    vals = []
-    for s in range(args.warmup + args.steps):
-        s_ldet, s_quad, info = cpu_operator_sample(rows_np, n, min(m, 4000), probes, subsets=2)
-        s_ldet *= m / min(m, 4000)
-        s_quad *= m / min(m, 4000)
-        est = max(it_q, it_v) * s_ldet + it_y * s_quad
-        if cfg.get("traits"):   # one fit per trait on its own individuals
-            est *= sum(k.size for k in trait_keeps(cfg)[0]) / n
-        if s >= args.warmup:
-            vals.append(est)
+    rows_np = rng.integers(0, 256, size=(m, (n + 3) // 4), dtype=np.uint8)   # timing only
+    nsub = m // SUBSET
+    spent = 1.0
+    for _ in range(args.warmup):   # warm-up: one subset
+        _, _, spent, _ = cpu_app_model(rows_np, n, probes, 1)
+    # size each timed step so that the K steps take about args.ref_budget seconds of CPU work
+    S = int(max(1, min(nsub, args.ref_budget / max(args.steps, 1) / max(spent, 1e-3))))
+    vals, walls, infos = [], [], []
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        a, b, _, info = cpu_app_model(rows_np, n, probes, S, start=s * S)
+        walls.append(time.perf_counter() - t0)
+        vals.append(reference_seconds(a, b, m, apps))
+        infos.append(info)
     value = statistics.mean(vals)
+    covered = min(nsub, S * args.steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes},
+        "data": "synthetic (random packed bytes of the workload's shape: the loop's time does not depend on the values)",
+        "config": gpu_config(cfg, "FP32 (the reference's float arithmetic)"),
+        "steps_are": f"each timed step runs the reference's full-n subset loop on {S} of the {nsub} subsets "
+                     f"({covered} subsets covered over the {args.steps} steps) and converts it to one whole fit; "
+                     f"ms_per_step is that step's measured wall time",
+        "applications": [{"what": w, "passes": p, "columns": k, "count": c} for w, p, k, c in apps],
+        "step_counts": st,
         "cpu_baseline": {"value": value, "unit": "s", "cores": cpu_threads(), "kind": "port",
-                         "sample": f"{info}; Lanczos steps (y {it_y}, Q {it_q}, V {it_v}) from the "
-                                   f"reference algorithm run in full on an n={small_n}, m={small_m} "
-                                   f"problem with the same n/m ratio"
-                                   + (f"; summed over {cfg['traits']} traits in proportion to their individuals "
-                                      f"(GWAS score terms not included)" if cfg.get("traits") else "")},
+                         "sample": infos[-1] + "; whole fit = sum over the applications of count*(m/1000)*(a+passes*b*k)"},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -338,6 +429,21 @@ def run_reference(args, cfg):
 # ------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------
+PRECISIONS = {
+    "fp16x2": ("FP16 hi+lo pieces of each dense column scaled by a power of two (integer hi piece, exact FP32 "
+               "accumulation of count*hi), tcgen05 MMA with FP32 accumulation, FP64 Lanczos scalars"),
+    "bf16x2": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars",
+    "bf16x3": "BF16 hi+mid+lo products, FP32 accumulation, FP64 Lanczos scalars",
+    "fp32": "CUDA-core FP32 products on exact integer counts, FP64 Lanczos scalars",
+}
+
+
+def prec_code(name):
+    from slemm_gb300 import _lib
+    return {"fp16x2": _lib.PREC_FP16X2, "bf16x2": _lib.PREC_BF16X2, "bf16x3": _lib.PREC_BF16X3,
+            "fp32": _lib.PREC_FP32}[name]
+
+
 def run_gpu(args, cfg):
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -354,6 +460,7 @@ def run_gpu(args, cfg):
     rows, y, X, persnp = make_inputs(cfg)
     rows_np = rows.numpy()
     opts = dict(seed=0, n_V=probes)
+    prec = prec_code(args.prec)
 
     def barrier():
         torch.cuda.synchronize()
@@ -364,8 +471,8 @@ def run_gpu(args, cfg):
 
     def fit(gh):
         """One REML + BLUP through the reference-facing calls: DF-REML, or for the windowed
-        workload `--iter_weighting` (MAF from the handle, equal-weight GREML, window weights,
-        weighted GREML)."""
+        workload `--iter_weighting` (MAF from the handle, MC-REML equal-weight stage, window
+        weights, window-weighted DF-REML)."""
         if window:
             maf = gh.marker_qc()[0]
             return gh.REML_iter_weighting(None, X, y, persnp, maf, lrt=True, window_size=window, **opts)
@@ -373,13 +480,13 @@ def run_gpu(args, cfg):
 
     g = api.Genotypes(rows_np, n)
     stream = torch.cuda.ExternalStream(g.stream())
-    g.set_precision(_lib.PREC_BF16X2)
+    g.set_precision(prec)
     # clock samplers start before the warm-up (their start-up stays out of the timed steps) and
     # keep only the samples of the timed window
     nvml = NvmlSampler(local).__enter__()
     clocks = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
-        r = fit(g)
+        fit(g)
     # ---- timed: REML + BLUP with genotypes resident ----
     launches0 = api.launch_count()
     _prof(g, 1)
@@ -403,43 +510,55 @@ def run_gpu(args, cfg):
     launches = api.launch_count() - launches0
     prof = _prof(g, 0)
     mean_step = max_over_ranks(statistics.mean(times), dist)
-    # ---- e2e: host buffers through the reference-facing calls ----
+    # ---- e2e: host buffers through the reference-facing calls (the first call grows the pool) ----
     e2e_times = []
-    for _ in range(0 if args.skip_e2e else max(2, args.steps)):
+    for _ in range(0 if args.skip_e2e else args.e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with api.Genotypes(rows_np, n) as g2:
-            g2.set_precision(_lib.PREC_BF16X2)
-            r2 = fit(g2)
+            g2.set_precision(prec)
+            fit(g2)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    e2e = (statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else e2e_times[0]) if e2e_times else None
+    e2e = statistics.mean(e2e_times[1:]) if len(e2e_times) > 1 else None
     e2e = max_over_ranks(e2e, dist)
     h2d = rows_np.nbytes + y.nbytes + X.nbytes + persnp.nbytes
     d2h = (n + m + 1 + 1) * 4 + (4 * m if window else 0)
-    # ---- plain FP32 per-vector GPU path (the comparison the metric names), one fit ----
+    # ---- plain FP32 GPU path (the comparison the metric names), one fit ----
     fp32 = None
-    if not args.skip_fp32:
+    if args.fp32 != "skip":
         g.set_precision(_lib.PREC_FP32)
-        g.set_per_vector(True)
+        g.set_per_vector(args.fp32 == "per_vector")
+        _prof(g, 1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rf = fit(g)
         torch.cuda.synchronize()
-        fp32 = {"s": time.perf_counter() - t0, "h2": rf["h2"], "iters": list(rf["iters"])}
+        t_fp32 = time.perf_counter() - t0
+        pf = _prof(g, 0)
+        packed = m * ((n + 3) // 4)
+        one = [s_ for s_ in pf if s_["k"] == 1]
+        passes = sum(s_["launches"] for s_ in one)
+        avg = sum(s_["ms"] for s_ in one) / max(passes, 1) / 1e3
+        fp32 = {"mode": args.fp32, "s": t_fp32, "h2": rf["h2"], "iters": list(rf["iters"]),
+                "counts": fit_counts(cfg, rf),
+                "k1_pass": {"launches": passes, "avg_ms": avg * 1e3,
+                            "packed_gbs": packed / avg / 1e9 if passes else None,
+                            "frac_hbm": packed / avg / 1e9 / peaks()["hbm"] if passes else None}}
         g.set_per_vector(False)
-        g.set_precision(_lib.PREC_BF16X2)
+        g.set_precision(prec)
     # ---- roofline of the dominant packed-product launch shape ----
-    roof, matvec_gbs = roofline(prof, n, m)
-    # ---- CPU baseline (oracle port), rank 0, N = 1 only ----
+    roof, matvec_gbs = roofline(prof, n, m, sustained=min(times) > 1.0)
+    # ---- CPU baseline (oracle port, this fit's step counts), rank 0, N = 1 only ----
     cpu = None
+    counts = fit_counts(cfg, res)
     if rank == 0 and world == 1 and not args.skip_cpu:
-        s_ldet, s_quad, info = cpu_operator_sample(rows_np, n, m, probes, subsets=args.cpu_subsets)
-        it_y, it_q, it_v = res["iters"]
-        est = max(it_q, it_v) * s_ldet + it_y * s_quad
-        cpu = {"value": est, "unit": "s", "cores": cpu_threads(), "kind": "port",
-               "sample": f"{info}; REML time = {max(it_q, it_v)}·t(ldet, {1 + probes} cols) + "
-                         f"{it_y}·t(quadform, 1 col) with this fit's Lanczos step counts"}
+        a, b, spent, info = cpu_app_model(rows_np, n, probes, args.cpu_subsets)
+        apps = reference_applications(cfg, counts)
+        cpu = {"value": reference_seconds(a, b, m, apps), "unit": "s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"{info} ({spent:.1f} s of CPU work); whole fit = sum over the reference's operator "
+                         f"applications (this fit's Lanczos steps) of count*(m/1000)*(a+passes*b*k)",
+               "applications": [{"what": w, "passes": p, "columns": k, "count": c} for w, p, k, c in apps]}
     # ---- integer stages (decode, popcounts, class counts): GPU pack from HBM vs the C oracle ----
     integer = None
     if rank == 0 and world == 1 and not args.skip_cpu:
@@ -462,21 +581,19 @@ def run_gpu(args, cfg):
     line = {
         "metric": METRIC, "value": mean_step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "h2_sim": cfg["h2"],
-                   **({"ld_rho": cfg["ld_rho"], "ld_block": cfg["ld_block"], "window_size": window}
-                      if window else {}),
-                   "precision": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars",
-                   "l2": "inputs larger than L2 (packed Z 1.25 GB per pass)", "parallelism": "replicas"},
+        "config": gpu_config(cfg, PRECISIONS[args.prec]),
         "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
         "lanczos_steps": {"y": res["iters"][0], "Q": res["iters"][1], "V": res["iters"][2]},
+        "counts": counts,
         "phases_s": res.get("phases"),
         "step_ms": [round(t * 1e3, 3) for t in times],
         "matvec_gbs": matvec_gbs,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "step_ms": [round(t * 1e3, 3) for t in e2e_times],
-                "note": "mean of the steps after the first (the first grows the device memory pool)"},
+                "note": "host .bed rows uploaded (pinned staging) + fit + results to the host, timed on the host; "
+                        "mean of the steps after the first (the first grows the device memory pool)"},
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches / max(args.steps, 1)),
         "roofline": roof,
@@ -485,9 +602,11 @@ def run_gpu(args, cfg):
         "clocks": nvml.summary() or clocks.summary(),
         "clocks_nvidia_smi": clocks.summary(),
     }
+    if window:
+        line["fixed_snps"] = len(res.get("fixed", []))
     if fp32:
-        line["fp32_per_vector"] = fp32
-        line["speedup_vs_fp32_per_vector"] = fp32["s"] / mean_step
+        line["fp32_" + args.fp32] = fp32
+        line["speedup_vs_fp32_" + args.fp32] = fp32["s"] / mean_step
         line["dh2_vs_fp32"] = abs(fp32["h2"] - res["h2"])
     g.close()
     if rank == 0:
@@ -496,9 +615,10 @@ def run_gpu(args, cfg):
         dist.destroy_process_group()
 
 
-def roofline(prof, n, m):
+def roofline(prof, n, m, sustained=False):
     """Roofline object of the dominant packed-product launch shape (most device time in the
-    timed region) and the packed bytes per second it streamed."""
+    timed region) and the packed bytes per second it streamed.  sustained: the launches run
+    inside a fit of seconds, so the measured sustained BF16 figure is the peak (else the burst)."""
     pk = peaks()
     dom = max(prof, key=lambda r: r["ms"]) if prof else None
     if not dom:
@@ -511,29 +631,31 @@ def roofline(prof, n, m):
     ach_tf = flops_alg / t_launch / 1e12
     exe_tf = 2.0 * n * m * dom["N"] / t_launch / 1e12 if dom["tc"] else ach_tf
     gbs = bytes_alg / t_launch / 1e9
-    tensor = dom["tc"] == 1
-    # The packed product runs at the full 2070 MHz SM clock without power capping inside the
-    # fits, the condition of the measured burst cuBLAS figure; the sustained figure was taken at
-    # ~1450 MHz under the power cap and is reported beside it.
+    # wide tensor-core shapes are tensor-bound; the narrow shape (N = 16, one to seven columns) is
+    # bound by its count decode and reported against HBM, like the CUDA-core kernel
+    tensor = dom["tc"] == 1 and dom["N"] > 16
+    tc_peak = pk["bf16_sus"] if sustained else pk["bf16"]
     roof = {
         "bound": "tensor" if tensor else "hbm",
         "achieved": ach_tf if tensor else gbs,
-        "peak": pk["bf16"] if tensor else pk["hbm"],
+        "peak": tc_peak if tensor else pk["hbm"],
         "unit": "TFLOP/s" if tensor else "GB/s",
-        "frac": (ach_tf / pk["bf16"]) if tensor else gbs / pk["hbm"],
-        "frac_of_sustained": ach_tf / pk["bf16_sus"] if tensor else None,
-        # a split into P BF16 pieces executes P products per algorithmic one, so the algorithmic
-        # ceiling of this kernel is the BF16 peak over P (TC_peak_eff of the workload's spec)
-        "tc_peak_eff": pk["bf16"] / dom["pieces"] if tensor else None,
-        "frac_eff": ach_tf / (pk["bf16"] / dom["pieces"]) if tensor else None,
+        "frac": (ach_tf / tc_peak) if tensor else gbs / pk["hbm"],
+        "peak_source": (("measured " + ("sustained" if sustained else "burst") + " cuBLAS BF16 (MEASURED_PEAKS.json)")
+                        if tensor else "measured HBM copy (MEASURED_PEAKS.json)") if pk["src"] == "measured"
+        else "fallback",
+        # a split into P 16-bit pieces executes P products per algorithmic one, so the algorithmic
+        # ceiling of this kernel is the 16-bit peak over P
+        "tc_peak_eff": tc_peak / dom["pieces"] if dom["tc"] else None,
+        "frac_eff": ach_tf / (tc_peak / dom["pieces"]) if dom["tc"] else None,
         "traffic": _traffic(dom, n, m),
-        "kernel": "gemm_tc_kernel" if tensor else "gemm_simt_kernel",
+        "kernel": "gemm_tc_kernel" if dom["tc"] else "gemm_simt_kernel",
         "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],
                    "direction": "Z^T U (M=SNPs)" if dom["dir"] == 1 else "Z V (M=individuals)",
-                   "avg_ms": t_launch * 1e3, "launches": dom["launches"]},
-        "executed_tflops": exe_tf, "frac_executed": exe_tf / pk["bf16"],
+                   "avg_ms": t_launch * 1e3, "launches": dom["launches"],
+                   "algorithmic_flops": flops_alg, "algorithmic_bytes": bytes_alg},
+        "executed_tflops": exe_tf, "frac_executed": exe_tf / tc_peak,
         "algorithmic_gbs": gbs, "frac_hbm": gbs / pk["hbm"],
-        "peak_source": "measured burst cuBLAS BF16 (MEASURED_PEAKS.json)" if pk["src"] == "measured" else "fallback",
         "shapes": prof,
     }
     return roof, packed / t_launch / 1e9
@@ -578,7 +700,7 @@ def run_grad(args, cfg):
 
     g = api.Genotypes(rows_np, n)
     stream = torch.cuda.ExternalStream(g.stream())
-    g.set_precision(_lib.PREC_BF16X2)
+    g.set_precision(prec_code(args.prec))
     nvml = NvmlSampler(local).__enter__()
     clocks = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
@@ -610,7 +732,7 @@ def run_grad(args, cfg):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with api.Genotypes(rows_np, n) as g2:
-            g2.set_precision(_lib.PREC_BF16X2)
+            g2.set_precision(prec_code(args.prec))
             step(g2)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
@@ -620,7 +742,7 @@ def run_grad(args, cfg):
     d2h = 8 * (2 + wwin.size)
     # the same gradient with FP32 products throughout the Lanczos solves
     fp32 = None
-    if not args.skip_fp32:
+    if args.fp32 != "skip":
         g.set_precision(_lib.PREC_FP32)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -631,7 +753,7 @@ def run_grad(args, cfg):
                 "rel_diff": {"d_sigma_g2": abs(rf["d_sigma_g2"] - r["d_sigma_g2"]) / abs(rf["d_sigma_g2"]),
                              "d_sigma_e2": abs(rf["d_sigma_e2"] - r["d_sigma_e2"]) / abs(rf["d_sigma_e2"]),
                              "d_w_max_over_max": float(dw)}}
-        g.set_precision(_lib.PREC_BF16X2)
+        g.set_precision(prec_code(args.prec))
     roof, matvec_gbs = roofline(prof, n, m)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
@@ -652,13 +774,13 @@ def run_grad(args, cfg):
     line = {
         "metric": "REML log-likelihood gradient wall time", "value": mean_step, "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "windows": int(wwin.size),
                    "sigma_g2": sg2, "sigma_e2": se2,
-                   "precision": "BF16 hi+lo products in the Lanczos solves, hi+mid+lo in the closing "
-                                "Z^T pass, FP32 accumulation, FP64 scalars and reductions",
-                   "l2": "inputs larger than L2 (packed Z 5.0 GB per pass)", "parallelism": "replicas"},
+                   "precision": PRECISIONS[args.prec] + " in the Lanczos solves; column-scaled FP16 hi+lo in "
+                                "the closing Z^T pass; FP64 reductions",
+                   "l2": l2_note(n, m), "parallelism": "replicas"},
         "gradient": h,
         "step_ms": [round(t * 1e3, 3) for t in times],
         "matvec_gbs": matvec_gbs,
@@ -749,7 +871,7 @@ def run_multi(args, cfg):
         res = []
         for t in range(T):
             with api.Genotypes(rows, n, keep_idx=keeps[t]) as gt:
-                gt.set_precision(_lib.PREC_BF16X2)
+                gt.set_precision(prec_code(args.prec))
                 res.append(gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes))
         if gwas_handle is not None:
             sc = gwas(gwas_handle, res[0]["Py"])
@@ -796,7 +918,7 @@ def run_multi(args, cfg):
         gt = api.Genotypes(rows_dev, n, keep_idx=keeps[t])
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        gt.set_precision(_lib.PREC_BF16X2)
+        gt.set_precision(prec_code(args.prec))
         if t == 0:
             _prof(gt, 1)
         gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes)
@@ -840,7 +962,7 @@ def run_multi(args, cfg):
     d2h = sum((k.size + m + 1 + 1) * 4 for k in keeps) + 2 * 4 * m2
     # plain FP32 per-vector fit of the first trait (the comparison the metric names)
     fp32 = None
-    if not args.skip_fp32:
+    if args.fp32 != "skip":
         with api.Genotypes(rows_dev, n, keep_idx=keeps[0]) as gt:
             gt.set_precision(_lib.PREC_FP32)
             gt.set_per_vector(True)
@@ -878,12 +1000,12 @@ def run_multi(args, cfg):
     line = {
         "metric": METRIC, "value": mean_step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2",
+        "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "traits": T,
                    "missing_fraction": [round(float(f), 4) for f in frac], "gwas_m": m2,
-                   "precision": "BF16 hi+lo products, FP32 accumulation, FP64 Lanczos scalars; GWAS hi+mid+lo",
-                   "l2": "inputs larger than L2 (packed Z ≥ 7.5 GB per pass)", "parallelism": "replicas",
+                   "precision": PRECISIONS[args.prec] + "; GWAS score pass at column-scaled FP16 hi+lo",
+                   "l2": l2_note(n, m), "parallelism": "replicas",
                    "timing": "host clock around a device synchronisation (each trait handle has its own stream)"},
         "per_trait": [{"n": int(k.size), "h2": r["h2"], "iters": list(r["iters"])} for r, k in zip(res, keeps)],
         "phases_s": ph,
@@ -956,7 +1078,7 @@ def run_kernel_case(args):
     gm = np.full(m, 0.55, np.float32)
     w = np.full(m, 1.0 / m, np.float32)
     g.set_weights(gm, w)
-    g.set_precision(_lib.PREC_BF16X3 if args.kernel_prec == 3 else _lib.PREC_BF16X2)
+    g.set_precision(prec_code(args.prec))
     v = torch.randn(k, n, device="cuda")
     out = torch.empty(k, n, device="cuda")
     for _ in range(3):
@@ -978,18 +1100,26 @@ def run_kernel_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel-case", action="store_true", help="small operator case for ncu captures")
-    ap.add_argument("--kernel-prec", type=int, default=2, choices=[2, 3])
     ap.add_argument("--kernel-k", type=int, default=65, help="columns of the kernel case's block")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2, help="end-to-end fits timed after one pool-growing fit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS))
-    ap.add_argument("--skip-fp32", action="store_true")
+    ap.add_argument("--config", type=int, default=3, choices=sorted(CONFIGS))
+    ap.add_argument("--prec", default="fp16x2", choices=sorted(PRECISIONS),
+                    help="product precision of the timed fits (and of the kernel case)")
+    ap.add_argument("--fp32", default="per_vector", choices=["per_vector", "batched", "skip"],
+                    help="the plain FP32 GPU fit the metric compares with")
+    ap.add_argument("--skip-fp32", action="store_true", help="same as --fp32 skip")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--cpu-subsets", type=int, default=3)
+    ap.add_argument("--cpu-subsets", type=int, default=4)
+    ap.add_argument("--ref-budget", type=float, default=120.0,
+                    help="seconds of CPU work the reference arm's timed steps aim at in total")
     args = ap.parse_args()
+    if args.skip_fp32:
+        args.fp32 = "skip"
     cfg = CONFIGS[args.config]
     if args.kernel_case:
         from slemm_gb300 import build

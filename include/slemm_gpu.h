@@ -201,6 +201,9 @@ typedef struct {
   int    n_points;
   float  h2_points[SLEMM_TRACE_MAX];
   double f_points[SLEMM_TRACE_MAX];
+  /* --iter_weighting only (0 otherwise): the equal-weight first stage's Lanczos steps of its
+   * probe block (iters_V of that fit) and its criterion evaluations. */
+  int    first_iters_V, first_n_criterion;
 } slemm_reml_result;
 
 /* DF-REML with Rademacher probes + golden-section search (src/reml.cpp:549-690).

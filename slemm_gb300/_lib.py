@@ -38,7 +38,8 @@ class RemlResult(ctypes.Structure):
                 ("iters_Q", I32), ("iters_V", I32), ("n_criterion", I32), ("seconds", ctypes.c_double),
                 ("t_setup", ctypes.c_double), ("t_seed", ctypes.c_double), ("t_search", ctypes.c_double),
                 ("t_final", ctypes.c_double), ("n_points", I32), ("h2_points", F32 * TRACE_MAX),
-                ("f_points", ctypes.c_double * TRACE_MAX)]
+                ("f_points", ctypes.c_double * TRACE_MAX), ("first_iters_V", I32),
+                ("first_n_criterion", I32)]
 
     def trace(self):
         """[(h², criterion)] of the search's evaluations, in order."""

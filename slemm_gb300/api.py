@@ -266,7 +266,8 @@ class Genotypes:
         cc = c + k
         out = dict(vg=r.vg, ve=r.ve, h2=r.h2, lrt=r.lrt, Py=Py, snp_blup=b, blue=blue[:cc],
                    fixed=list(fixed[:k]), persnp=p2, iters=(r.iters_y, r.iters_Q, r.iters_V),
-                   trace=r.trace(), seconds=r.seconds)
+                   trace=r.trace(), seconds=r.seconds,
+                   first_stage=dict(iters_V=r.first_iters_V, n_criterion=r.first_n_criterion))
         if lrt:
             out["var_blue"] = vb[:cc * cc].reshape(cc, cc, order="F")
         return out

@@ -144,7 +144,7 @@ extern "C" int slemm_gpu_reml_iter_weighting(slemm_geno* g, const float* rvec, c
                                              int64_t* fixed_idx, int* n_fixed, slemm_reml_result* res)
 {
   return guarded([&] {
-    CHECK_ARG(g && X && y && persnp && maf && opts && wo && Py && snp_blup && blue && n_fixed, "null argument");
+    CHECK_ARG(g && X && y && persnp && maf && opts && wo && Py && snp_blup && blue && n_fixed && res, "null argument");
     CHECK_ARG(ldx >= g->n && c >= 1, "bad covariate matrix");
     const int64_t n = g->n, m = g->m;
     CHECK_ARG(wo->window_size >= 0 && wo->window_size % 2 == 0, "window_size must be even and >= 0");
@@ -192,6 +192,8 @@ extern "C" int slemm_gpu_reml_iter_weighting(slemm_geno* g, const float* rvec, c
       reml_lmc(g, rvec, X2.data(), n, c2, y, p2.data(), o2, Py, snp_blup, blue, res);
     }
     for (int i = 0; i < s; ++i) snp_blup[idx[i]] = blue[c + i];
+    res->first_iters_V = r1.iters_V;
+    res->first_n_criterion = r1.n_criterion;
     *n_fixed = s;
     if (fixed_idx) std::copy(idx.begin(), idx.end(), fixed_idx);
     if (persnp_out) std::copy(p2.begin(), p2.end(), persnp_out);
