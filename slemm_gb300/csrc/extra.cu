@@ -238,7 +238,7 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
     bool one_rr = true;
     for (int64_t i = 0; i < n && one_rr; ++i) one_rr = rr[i] == 1.0f;
     if (one_rr) {
-      // the packed tensor-core product of [y | Q] (hi+mid+lo BF16 pieces, FP32 accumulation);
+      // the packed tensor-core product of [y | Q] (column-scaled FP16 hi+lo pieces, FP32 accumulation);
       // the FP64 per-genotype kernel below serves general rr
       const int k = 1 + c;
       std::vector<float> V((size_t)k * n);
@@ -273,7 +273,7 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
       CUDA_TRY(cudaMemcpyAsync(dn2.p, n2.data(), g->m * sizeof(int32_t), cudaMemcpyHostToDevice, st));
       CUDA_TRY(cudaMemcpyAsync(dsq.p, sum_q.data(), sum_q.size() * sizeof(double), cudaMemcpyHostToDevice, st));
       const int prec = g->prec;
-      g->prec = SLEMM_PREC_BF16X3;
+      g->prec = SLEMM_PREC_FP16X2;
       try {
         op_device(g, SLEMM_OP_RMATVEC, 0.f, dV.as<float>(), n, k, dO.as<float>(), g->m);
       } catch (...) {

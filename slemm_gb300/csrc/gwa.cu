@@ -14,7 +14,7 @@
 //
 // GB300 mapping: the model SNPs are gathered into their own packed copy (16-byte rows of the
 // tiles), so every block is a contiguous row range; BBᵀ and Bx̃ for all the block's tested
-// variants are packed tensor-core products Cc_blockᵀ·U (hi+mid+lo BF16 pieces, ≈ FP32 like the
+// variants are packed tensor-core products Cc_blockᵀ·U (column-scaled FP16 hi+lo, ≈ FP32 like the
 // script's float32 BLAS) with U = rr∘(I − QQᵀ)(rr∘Cc) or rr∘X̃ — no dense B is ever formed.  The
 // blocks' systems are factored together (blocked FP32 Cholesky, one CTA per block), and the
 // quadratic forms come from one batched multi-right-hand-side triangular solve in shared memory.
@@ -128,7 +128,7 @@ struct ModelCopy {
     h.n_pad = g->n_pad;
     h.m = (int64_t)model.size();
     h.m_pad = round_up(h.m, kPadRows);
-    h.prec = SLEMM_PREC_BF16X3;
+    h.prec = SLEMM_PREC_FP16X2;
     h.weights_set = true;
     const int64_t K_tiles = g->n_pad / kTileK;
     const int64_t total = h.m_pad * K_tiles;   // 16-byte tile rows
@@ -278,7 +278,7 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
         proj_apply(M, U, n, bs, qtv);
         scale_rows_rr_kernel<<<dim3((unsigned)ceil_div(n, 256), bs), 256, 0, st>>>(U, n, drr, n);
         LAUNCH_CHECK();
-        rows_product(M, r0, r1 - r0, U, n, bs, gram + (size_t)bi * rows_max * bs, rows_max, 3);
+        rows_product(M, r0, r1 - r0, U, n, bs, gram + (size_t)bi * rows_max * bs, rows_max, SLEMM_PREC_FP16X2);
       }
       // 2. factor every block of the batch (one CTA each)
       float* F = (float*)d_F.ensure((size_t)bn * bs * bs * sizeof(float));
@@ -315,7 +315,7 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
         const int64_t s0 = start[b0 + bi];
         const int64_t r0 = s0 / kPadRows * kPadRows;
         const int64_t r1 = std::min<int64_t>(round_up(s0 + bs, kPadRows), M->m_pad);
-        rows_product(M, r0, r1 - r0, X, n, (int)tb, Zall + (size_t)acc * rows_max, rows_max, 3);
+        rows_product(M, r0, r1 - r0, X, n, (int)tb, Zall + (size_t)acc * rows_max, rows_max, SLEMM_PREC_FP16X2);
         acc += tb;
       }
       // 4. q = ‖L⁻¹z‖² for every tested variant of the batch

@@ -79,9 +79,10 @@ void op_device(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_
 void op_device_mixed(slemm_geno* g, int kind, float tau0, const float* in, int64_t ld_in, int k,
                      float* out, int64_t ld_out, int nq);
 
-// Centred Z_cᵀU over SNP rows [r0, r0 + rows) (multiples of 256) with `pieces` BF16 pieces (ops.cu).
+// Centred Z_cᵀU over SNP rows [r0, r0 + rows) (multiples of 256) on the tensor cores at precision
+// prec (SLEMM_PREC_FP16X2, BF16X2 or BF16X3; ops.cu).
 void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64_t ldu, int k, float* out,
-                  int64_t ldo, int pieces);
+                  int64_t ldo, int prec);
 
 // reml.cu — orthonormal basis (FP64 column-pivoted QR) of an n×c matrix; returns the rank.
 int orthonormal_columns(const std::vector<double>& A, int64_t n, int c, std::vector<double>& Q);

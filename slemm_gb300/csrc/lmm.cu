@@ -14,7 +14,7 @@
 //
 // GB300 mapping: ZᵀZ and z come out of one packed tensor-core product per window,
 // Z_wdᵀ[U | rr∘v] with U = rr∘(I − QQᵀ)(rr∘Cc) — the centred counts Cc are read from the packed
-// copy, never materialised as a dense Z — using hi+mid+lo BF16 pieces (≈ FP32 accuracy, like the
+// copy, never materialised as a dense Z — using column-scaled FP16 hi+lo (≈ FP32 accuracy, like the
 // reference's SGEMM).  The windows' systems are then factored together, one CTA per window:
 // blocked FP32 Cholesky in global memory (L2-resident), then two steps of iterative refinement
 // with FP64 residuals, so the quadratic form is limited by the Gram's own accuracy, not by the
@@ -232,7 +232,7 @@ extern "C" int slemm_gpu_lmm_quadforms(slemm_geno* g, const float* Py, float tau
       LAUNCH_CHECK();
       const int64_t r0 = wds / kPadRows * kPadRows;
       const int64_t r1 = std::min<int64_t>(round_up(wds + ws, kPadRows), g->m_pad);
-      rows_product(g, r0, r1 - r0, U, n, ws + 1, gram + (size_t)c * rows_max * (ws + 1), rows_max, 3);
+      rows_product(g, r0, r1 - r0, U, n, ws + 1, gram + (size_t)c * rows_max * (ws + 1), rows_max, SLEMM_PREC_FP16X2);
       // this window's Gram starts at row wds − r0 of its block
       wstart[c] = wds - r0;
     }

@@ -4,13 +4,13 @@
 //   Z_cᵀu  = Cntᵀu − gm·(1ᵀu)          (direction 1, K = individuals, M = SNPs)
 //   Z_c v  = Cnt v − 1·(gmᵀv)           (direction 2, K = SNPs, M = individuals)
 // where Cnt holds the exact integer counts.  The dense side is prepared once per pass by a
-// prologue (projection, rr scaling, FP32 → BF16 pieces) that also sums exactly what the
+// prologue (projection, rr scaling, FP32 → BF16 or FP16 pieces) that also sums exactly what the
 // tensor cores multiply, in FP64, for the correction term.  Direction 1 first removes each
 // column's mean μ and adds it back exactly: Z_cᵀu = Z_cᵀ(u − μ1) + μ·(pc − n·gm), with pc the
 // integer popcounts.  Without it a column with a large mean (the intercept column of a Lanczos
 // block) leaves Cntᵀu and gm·(1ᵀu) nearly equal and large, and their FP32 accumulation error
 // swamps the true difference: at n = 10⁶ the intercept's Lanczos recurrence never converged.  Finalize kernels reduce the split-K
-// partials and the BF16 pieces, apply the correction and the reference's diagonal scalings,
+// partials, apply the correction and the reference's diagonal scalings,
 // and either write the result or directly build the next pass's dense operand.
 //
 // All reductions are two-stage (per-block FP64 partials, then a fixed-order sum), so results
@@ -901,13 +901,17 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
 }
 
 // out[j, c] = Σ_i (count_ij − gm_j)·U[i, c] for SNP rows j ∈ [r0, r0 + rows) of the G copy (the
-// centred Z_cᵀU of a window of SNPs), with `pieces` BF16 pieces on the tensor cores (3: about
-// FP32 accuracy).  r0 and rows must be multiples of 256; U is n×k (ld ldu), out rows×k (ld ldo).
+// centred Z_cᵀU of a window of SNPs) on the tensor cores at precision prec: SLEMM_PREC_FP16X2
+// (column-scaled FP16 hi+lo, the most accurate at two pieces), SLEMM_PREC_BF16X3 or BF16X2.
+// r0 and rows must be multiples of 256; U is n×k (ld ldu), out rows×k (ld ldo).
 void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64_t ldu, int k, float* out,
-                  int64_t ldo, int pieces)
+                  int64_t ldo, int prec)
 {
   CHECK_ARG(r0 % kPadRows == 0 && rows % kPadRows == 0 && r0 + rows <= g->m_pad, "row range not aligned");
-  CHECK_ARG(pieces >= 2 && pieces <= 3, "pieces must be 2 or 3");
+  CHECK_ARG(prec == SLEMM_PREC_FP16X2 || prec == SLEMM_PREC_BF16X2 || prec == SLEMM_PREC_BF16X3,
+            "rows_product runs on the tensor cores");
+  const bool f16 = prec == SLEMM_PREC_FP16X2;
+  const int pieces = prec == SLEMM_PREC_BF16X3 ? 3 : 2;
   cudaStream_t st = g->stream;
   const int grp = pieces == 3 ? 80 : 128;
   const int64_t K_pad = g->n_pad, K_tiles = K_pad / kTileK;
@@ -919,7 +923,7 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     const int kc = std::min(grp, k - c0);
     PassPlan p;
     p.tc = true;
-    p.f16 = false;
+    p.f16 = f16;
     p.pieces = pieces;
     p.kp = (int)round_up(kc, 8);
     p.N = (int)round_up((int64_t)pieces * p.kp, 16);
@@ -927,30 +931,43 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     const int pad = p.N - pieces * kc;
     void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
     float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.kp * rows * sizeof(float));
-    double* r_col = (double*)g->ws_red.ensure(2 * (size_t)kc * nblk_n * sizeof(double));
+    // partials: column sums [kc][nblk_n] | sums for the means [kc][nblk_n] | FP16 signed extremes [kc][nblk_n][2]
+    double* r_col = (double*)g->ws_red.ensure((size_t)kc * nblk_n * (f16 ? 4 : 2) * sizeof(double));
     double* r_mu = r_col + (size_t)kc * nblk_n;
     double* const mu = g->gcorr.p ? r_mu : nullptr;
+    double* const x_rng = f16 ? r_mu + (size_t)kc * nblk_n : nullptr;
     const float* in = U + (int64_t)c0 * ldu;
-    if (vec4_ok(g->n, ldu, in)) {
-      if (mu) {
+    const bool v4 = vec4_ok(g->n, ldu, in);
+    if (mu || f16) {   // measure pass: sums for the means, signed extremes for the FP16 scales
+      if (v4)
         prologue_indiv_kernel<4, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
-            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n,
-            nullptr, nullptr);
-        LAUNCH_CHECK();
-      }
-      prologue_indiv_kernel<4, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-          nullptr);
-    } else {
-      if (mu) {
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, mu, nblk_n,
+            nullptr, x_rng);
+      else
         prologue_indiv_kernel<1, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
-            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_mu, nblk_n,
-            nullptr, nullptr);
-        LAUNCH_CHECK();
-      }
-      prologue_indiv_kernel<1, false><<<dim3(nblk_n, kc + pad), kRedThreads, 0, st>>>(
-          in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-          nullptr);
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, mu, nblk_n,
+            nullptr, x_rng);
+      LAUNCH_CHECK();
+    }
+    const dim3 grid(nblk_n, kc + pad);
+    if (f16) {
+      if (v4)
+        prologue_indiv_kernel<4, false, true><<<grid, kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+            x_rng);
+      else
+        prologue_indiv_kernel<1, false, true><<<grid, kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+            x_rng);
+    } else {
+      if (v4)
+        prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+            nullptr);
+      else
+        prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(
+            in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
+            nullptr);
     }
     LAUNCH_CHECK();
     run_gemm(g, p, A, rows, K_pad, B1, D, g->err.as<int>(), kc, 1);
@@ -958,11 +975,11 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     if (vec4_ok(m_valid, ldo, o))
       finalize_snp_kernel<4><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
           D, p.splits, p.kp, rows, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0, 8,
-          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, nullptr, nullptr, nullptr);
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, x_rng, nullptr, nullptr);
     else
       finalize_snp_kernel<1><<<dim3(nblk_m, kc), kRedThreads, 0, st>>>(
           D, p.splits, p.kp, rows, kc, m_valid, g->gm.as<float>() + r0, nullptr, r_col, nblk_n, 0, o, ldo, 0, 8,
-          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, nullptr, nullptr, nullptr);
+          nullptr, nullptr, 0, mu, mu ? g->gcorr.as<float>() + r0 : nullptr, g->n, x_rng, nullptr, nullptr);
     LAUNCH_CHECK();
   }
 }

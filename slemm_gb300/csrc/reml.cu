@@ -741,8 +741,8 @@ using namespace slemm;
 //   ∂ℓ/∂σ_g² = −½[Σ_j W_j·b_j/σ_g² − Σ_j W_j·a_j/σ_g⁴]
 //   ∂ℓ/∂σ_e² = −½[tr(P_H)/σ_g² − ‖P_Hỹ‖²/σ_g⁴],   tr(P_H) ≈ (n/n_V)·Σ_v vᵀP_Hv
 //   ∂ℓ/∂w_k  = −½·Σ_{j ∈ window k} gw_j·[b_j − a_j/σ_g²].
-// The per-SNP terms of every window come from one packed product Z̃ᵀ[P_Hỹ | P_HV | V] (hi+mid+lo
-// pieces), the transposed product the operators use, reduced per window on the host in FP64.
+// The per-SNP terms of every window come from one packed product Z̃ᵀ[P_Hỹ | P_HV | V] (column-
+// scaled FP16 hi+lo), the transposed product the operators use, reduced per window on the host in FP64.
 // Per-SNP terms of the gradient from T = Z̃ᵀ[P_Hỹ | P_HV | V] (column-major, m rows):
 // a_j = t_{0,j}², b_j = scale·Σ_v t_{1+v,j}·t_{1+n_V+v,j}, accumulated in FP64 (n_V FMAs per SNP).
 __global__ void grad_terms_kernel(const float* __restrict__ T, int64_t m, int n_V, double scale,
@@ -819,7 +819,7 @@ void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   scale_rows(g, d_U.as<float>(), n, n, k, g->rr.as<float>());
   d_T.ensure((size_t)m * k * sizeof(float));
   const int prec = g->prec;
-  g->prec = SLEMM_PREC_BF16X3;
+  g->prec = SLEMM_PREC_FP16X2;
   try {
     op_device(g, SLEMM_OP_RMATVEC, 0.f, d_U.as<float>(), n, k, d_T.as<float>(), m);
   } catch (...) {

@@ -6,7 +6,7 @@
 //
 // GB300 mapping.  Z̃ᵀZ̃ = Cc ᵀ·U with U = rr∘(I − QQᵀ)(rr∘Cc) (P is a symmetric projection), so the
 // Gram comes, 1024 columns at a time, out of the packed tensor-core product over the SNP rows at or
-// below the block (the lower part is all the factorisation reads) with hi+mid+lo BF16 pieces
+// below the block (the lower part is all the factorisation reads) with column-scaled FP16 hi+lo
 // (≈ FP32, like the reference's SGEMM), and Z̃ᵀy_proj = Ccᵀ(rr∘y_proj) likewise.  The m×m system
 // is factored in place by a tiled right-looking Cholesky (128×128 tiles): one CTA factors the
 // diagonal tile, one CTA per tile below solves the panel, and a shared-memory tiled FP32
@@ -233,12 +233,12 @@ extern "C" int slemm_gpu_wls(slemm_geno* g, const float* rvec, const float* X, i
       scale_rows_rr_kernel<<<dim3((unsigned)ceil_div(n, 256), k), 256, 0, st>>>(U, n, g->rr.as<float>(), n);
       LAUNCH_CHECK();
       const int64_t r0 = j0 / kPadRows * kPadRows;
-      rows_product(g, r0, g->m_pad - r0, U, n, k, Am + j0 * lda + r0, lda, 3);
+      rows_product(g, r0, g->m_pad - r0, U, n, k, Am + j0 * lda + r0, lda, SLEMM_PREC_FP16X2);
     }
     float* dy = (float*)d_y.ensure(n * sizeof(float));
     float* b = (float*)d_b.ensure(g->m_pad * sizeof(float));
     CUDA_TRY(cudaMemcpyAsync(dy, yp.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
-    rows_product(g, 0, g->m_pad, dy, n, 1, b, g->m_pad, 3);
+    rows_product(g, 0, g->m_pad, dy, n, 1, b, g->m_pad, SLEMM_PREC_FP16X2);
     check_device_error(g);
     // ridge: 1e-4·mean(diag) (src/wls.cpp:123)
     float* dd = (float*)d_d.ensure(m * sizeof(float));
