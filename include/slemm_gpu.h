@@ -53,6 +53,10 @@ extern "C" {
 #define SLEMM_PREC_FP16X2  3  /* tcgen05 FP16 MMA, dense side scaled by a power of two per column
                                  and split hi+lo (22 mantissa bits) at the cost of hi+lo BF16     */
 
+/* Largest number of fixed-effect covariates (columns of X, and so of the projection Q) a fit takes,
+ * including the SNPs that --iter_weighting appends as fixed effects. */
+#define SLEMM_MAX_COVARIATES 256
+
 /* ---- memory location flags ---------------------------------------------------------------- */
 #define SLEMM_MEM_HOST     0
 #define SLEMM_MEM_DEVICE   1

@@ -565,7 +565,7 @@ int slemm_gpu_set_projection(slemm_geno* g, const float* Q, int64_t ldq, int c)
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
-    CHECK_ARG(c >= 0 && c <= 64, "projection rank must be in [0, 64]");
+    CHECK_ARG(c >= 0 && c <= SLEMM_MAX_COVARIATES, "projection rank must be in [0, SLEMM_MAX_COVARIATES]");
     g->c = c;
     if (c == 0) return;
     CHECK_ARG(Q != nullptr && ldq >= g->n, "bad Q");

@@ -161,7 +161,7 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
   return guarded([&] {
     CHECK_ARG(g && y && covar && model_idx && beta && se && chisq && pval, "null argument");
     const int64_t n = g->n, m = g->m;
-    CHECK_ARG(c >= 1 && c <= 64 && ldc >= n, "bad covariate matrix");
+    CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES && ldc >= n, "bad covariate matrix");
     CHECK_ARG(n_model >= 2 && test_begin >= 0 && test_end < m && test_begin <= test_end, "bad SNP ranges");
     for (int64_t k = 0; k < n_model; ++k)
       CHECK_ARG(model_idx[k] >= 0 && model_idx[k] < m && (k == 0 || model_idx[k] > model_idx[k - 1]),

@@ -24,6 +24,7 @@
 namespace slemm {
 
 constexpr int kRedThreads = 256;
+static_assert(SLEMM_MAX_COVARIATES <= kRedThreads, "load_qt gives one covariate per thread");
 constexpr int kRowsPerBlock = 4096;   // rows handled by one block of the row-wise kernels
 
 // 4-wide accesses need rows % 4 == 0 (a vector never straddles the end), ld % 4 == 0 and a
@@ -69,7 +70,8 @@ proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __res
   if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.x] = s;
 }
 
-// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ 64, as hi+lo FP32 pairs
+// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ SLEMM_MAX_COVARIATES
+// (≤ the block's threads), as hi+lo FP32 pairs
 __device__ __forceinline__ void load_qt(const double* __restrict__ parts, int nblk, int cq, int k, int c, float2* qt)
 {
   if ((int)threadIdx.x < cq) {
@@ -103,7 +105,7 @@ proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq, float* __res
                   int64_t n, int k, const double* __restrict__ qparts, int nblkq,
                   const float* __restrict__ Vin, int64_t ld_v, float tau0)
 {
-  __shared__ float2 qt[64];
+  __shared__ float2 qt[SLEMM_MAX_COVARIATES];
   const int c = blockIdx.y;
   load_qt(qparts, nblkq, cq, k, c, qt);
   const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
@@ -151,7 +153,7 @@ static void proj_apply_parts(slemm_geno* g, float* X, int64_t ldx, int k, const 
 void proj_coeffs(slemm_geno* g, const float* X, int64_t ldx, int k, double* d_QtX)
 {
   if (g->c == 0) return;
-  CHECK_ARG(g->c <= 64, "more than 64 covariates");
+  CHECK_ARG(g->c <= SLEMM_MAX_COVARIATES, "too many covariates");
   const int nblk = (int)ceil_div(g->n, kRowsPerBlock);
   double* red = (double*)g->ws_red.ensure((size_t)nblk * g->c * k * sizeof(double));
   proj_partials(g, X, ldx, k, red, nblk);
@@ -350,7 +352,7 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
 {
   __shared__ double sh[32];
   __shared__ float shf[32];
-  __shared__ float2 qt[64];
+  __shared__ float2 qt[SLEMM_MAX_COVARIATES];
   __shared__ float smu, ssc[2];
   const int c = blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n_pad, i0 + kRowsPerBlock);
@@ -759,7 +761,7 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   // column sums for the means [k][nblk_n] | FP16 ranges: operand 1 signed extremes [k][nblk_n][2],
   // operand 2 maxima of |x| [k][nblk_m]
   const int cq = g->c;
-  CHECK_ARG(cq <= 64, "more than 64 covariates");
+  CHECK_ARG(cq <= SLEMM_MAX_COVARIATES, "too many covariates");
   const size_t nred = 2 * (size_t)k * nblk_n + (size_t)k * nblk_m + 2 * (size_t)std::max(cq, 1) * k * nblk_q +
                       (f16 ? (size_t)k * (2 * nblk_n + nblk_m) : 0);
   double* r_col = (double*)g->ws_red.ensure(nred * sizeof(double));

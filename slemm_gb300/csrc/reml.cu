@@ -223,7 +223,7 @@ static Setup reml_setup(slemm_geno* g, const float* rvec, const float* X, int64_
                         const float* persnp)
 {
   const int64_t n = g->n, m = g->m;
-  CHECK_ARG(c >= 1 && c <= 64, "number of covariates must be in [1, 64]");
+  CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES, "number of covariates must be in [1, SLEMM_MAX_COVARIATES]");
   Setup S;
   S.rr.resize(n);
   for (int64_t i = 0; i < n; ++i) {
@@ -315,7 +315,7 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   cudaStream_t st = g->stream;
   const int n_V = o.n_V;
   CHECK_ARG(n_V >= 1, "n_V must be >= 1");
-  CHECK_ARG(c >= 1 && c <= 64, "number of covariates must be in [1, 64]");
+  CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES, "number of covariates must be in [1, SLEMM_MAX_COVARIATES]");
   // One block [y_proj | Q | V] (t = 1 + c + n_V) through one Lanczos recurrence: column 0 uses
   // the projected operator (seed_y, H0_quadform_mv), the rest the plain one (seed_Q and seed_V,
   // H0_ldet_mv); each of the three groups keeps its own stopping rule, as the reference's three
@@ -325,7 +325,8 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   d_y.ensure((size_t)n * sizeof(float));
   d_QV.ensure((size_t)n * tQV * sizeof(float));
   d_X.ensure((size_t)n * tQV * sizeof(float));
-  d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + 64 * 64 * sizeof(double));
+  // scalars: projection coefficients (up to c×c) first, one more value from offset c·c
+  d_tmp.ensure((size_t)std::max<int64_t>(n, m) * 4 * sizeof(double) + ((size_t)c * c + 64) * sizeof(double));
   // Rademacher probes (src/reml.cpp:597-605), the reference's mt19937 draws generated on the GPU;
   // launched first so that the host set-up below runs while they are drawn
   rademacher_device(o.seed, n, n_V, d_QV.as<float>() + (size_t)(1 + c) * n, n, g->stream);
@@ -480,8 +481,8 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   }
   std::vector<double> Sty(c);
   for (int l = 0; l < c; ++l) {
-    col_dots(g, d_S + (size_t)l * n, n, d_y.as<float>(), n, n, 1, d_scal + 64 * 64);
-    Sty[l] = d2h(g, d_scal + 64 * 64, 1)[0];
+    col_dots(g, d_S + (size_t)l * n, n, d_y.as<float>(), n, n, 1, d_scal + (size_t)c * c);
+    Sty[l] = d2h(g, d_scal + (size_t)c * c, 1)[0];
   }
   const std::vector<double>& R = S.qr.RPt;   // c×c
   std::vector<double> XtHX((size_t)c * c, 0.0), rhs(c, 0.0), T((size_t)c * c, 0.0);
@@ -577,8 +578,8 @@ void reml_lmc(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, int
   d_PV.ensure((size_t)n * tV * sizeof(float));
   d_Py.ensure((size_t)n * (1 + n_MC) * sizeof(float));
   d_ub.ensure((size_t)m * (1 + n_MC) * sizeof(float));
-  // scratch: c×tV projection coefficients first, then 4·tV norms from offset 64·64 (or later)
-  const size_t scal_off = std::max<size_t>(64 * 64, (size_t)c * tV);
+  // scratch: c×tV projection coefficients first, then 4·tV norms from offset c·tV
+  const size_t scal_off = (size_t)c * tV;
   d_tmp.ensure((scal_off + 4 * (size_t)tV) * sizeof(double));
   double* d_scal = d_tmp.as<double>();
   upload(g, d_V.as<float>(), V.data(), (size_t)n * tV);
@@ -793,7 +794,9 @@ void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   d_U.ensure((size_t)n * k * sizeof(float));
   CUDA_TRY(cudaMemcpyAsync(d_U.as<float>() + (size_t)(1 + n_V) * n, d_B.as<float>() + n, (size_t)n * n_V * sizeof(float),
                            cudaMemcpyDeviceToDevice, st));
-  double* d_scal = (double*)d_s.ensure((size_t)64 * t * sizeof(double) + 2 * (size_t)t * sizeof(double));
+  // scalars: c×t projection coefficients, then the trace and norm dots from offset c·t
+  const size_t qoff = (size_t)std::max(c, 1) * t;
+  double* d_scal = (double*)d_s.ensure(qoff * sizeof(double) + 2 * (size_t)t * sizeof(double));
   proj_coeffs(g, d_B.as<float>() + n, n, n_V, d_scal);
   proj_apply(g, d_B.as<float>() + n, n, n_V, d_scal);
   // P_H[ỹ | V] by one projected Lanczos seed at shift τ, solved at σ = 0 (groups ỹ, probes)
@@ -806,7 +809,7 @@ void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
   proj_coeffs(g, d_X.as<float>(), n, t, d_scal);
   proj_apply(g, d_X.as<float>(), n, t, d_scal);
   // tr(P_H) ≈ (n/n_V)·Σ_v vᵀP_Hv and ‖P_Hỹ‖²
-  double* d_dots = d_scal + (size_t)64 * t;
+  double* d_dots = d_scal + qoff;
   col_dots(g, d_U.as<float>() + (size_t)(1 + n_V) * n, n, d_X.as<float>() + n, n, n, n_V, d_dots);
   col_dots(g, d_X.as<float>(), n, nullptr, 0, n, 1, d_dots + n_V);
   const std::vector<double> dots = d2h(g, d_dots, (size_t)n_V + 1);
@@ -885,7 +888,7 @@ int slemm_gpu_reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_
 {
   return guarded([&] {
     CHECK_ARG(g && X && y && persnp && grad, "null argument");
-    CHECK_ARG(ldx >= g->n && c >= 1 && c <= 64, "bad covariate matrix");
+    CHECK_ARG(ldx >= g->n && c >= 1 && c <= SLEMM_MAX_COVARIATES, "bad covariate matrix");
     CHECK_ARG(n_win >= 0 && (n_win == 0 || (window && wwin)), "windows given without their weights");
     CHECK_ARG(sigma_g2 > 0.0 && sigma_e2 > 0.0 && std::isfinite(sigma_g2) && std::isfinite(sigma_e2),
               "variance components must be positive");

@@ -169,6 +169,8 @@ extern "C" int slemm_gpu_reml_iter_weighting(slemm_geno* g, const float* rvec, c
     clump(g, snpvar, wo->sig_chisq, wo->indep_r2, idx, cols);
     const int s = (int)idx.size();
     CHECK_ARG(s <= wo->max_fixed, "more fixed-effect SNPs (" + std::to_string(s) + ") than max_fixed");
+    CHECK_ARG(c + s <= SLEMM_MAX_COVARIATES,
+              "covariates plus fixed-effect SNPs exceed SLEMM_MAX_COVARIATES (" + std::to_string(c + s) + ")");
     for (int64_t j : idx) wts[j] = 0.0f;
     std::vector<float> p2(m);
     double ps = 0.0;

@@ -180,7 +180,7 @@ extern "C" int slemm_gpu_wls(slemm_geno* g, const float* rvec, const float* X, i
   return guarded([&] {
     CHECK_ARG(g && X && y && snp_blup, "null argument");
     const int64_t n = g->n, m = g->m;
-    CHECK_ARG(c >= 1 && c <= 64 && ldx >= n, "bad covariate matrix");
+    CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES && ldx >= n, "bad covariate matrix");
     cudaStream_t st = g->stream;
     // rr, Q, y_proj on the host (FP64 QR); gm from the exact popcounts
     std::vector<float> rr(n);
