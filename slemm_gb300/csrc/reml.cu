@@ -6,6 +6,7 @@
 // from libstdc++'s std::mt19937 with the reference's distributions and draw order, so the GPU
 // engine sees the reference's probes.
 #include "internal.h"
+#include "reduce.cuh"
 
 #include <chrono>
 #include <memory>
@@ -743,18 +744,86 @@ using namespace slemm;
 //   ∂ℓ/∂σ_e² = −½[tr(P_H)/σ_g² − ‖P_Hỹ‖²/σ_g⁴],   tr(P_H) ≈ (n/n_V)·Σ_v vᵀP_Hv
 //   ∂ℓ/∂w_k  = −½·Σ_{j ∈ window k} gw_j·[b_j − a_j/σ_g²].
 // The per-SNP terms of every window come from one packed product Z̃ᵀ[P_Hỹ | P_HV | V] (column-
-// scaled FP16 hi+lo), the transposed product the operators use, reduced per window on the host in FP64.
-// Per-SNP terms of the gradient from T = Z̃ᵀ[P_Hỹ | P_HV | V] (column-major, m rows):
-// a_j = t_{0,j}², b_j = scale·Σ_v t_{1+v,j}·t_{1+n_V+v,j}, accumulated in FP64 (n_V FMAs per SNP).
-__global__ void grad_terms_kernel(const float* __restrict__ T, int64_t m, int n_V, double scale,
-                                  double* __restrict__ ab)
+// scaled FP16 hi+lo), the transposed product the operators use, reduced per window on the device in
+// FP64 (grad_window_kernel).
+// Per-SNP terms of the gradient from T = Z̃ᵀ[P_Hỹ | P_HV | V] (column-major, m rows), computed in
+// FP64 where they are reduced: a_j = t_{0,j}², b_j = scale·Σ_v t_{1+v,j}·t_{1+n_V+v,j}.
+__device__ __forceinline__ void grad_terms(const float* __restrict__ T, int64_t m, int n_V, double scale, int64_t j,
+                                           double& a, double& b)
 {
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-    const double t0 = T[j];
-    double b = 0.0;
-    for (int v = 0; v < n_V; ++v) b = fma((double)T[(int64_t)(1 + v) * m + j], (double)T[(int64_t)(1 + n_V + v) * m + j], b);
-    ab[j] = t0 * t0;
-    ab[m + j] = b * scale;
+  const double t0 = T[j];
+  double s = 0.0;
+  for (int v = 0; v < n_V; ++v) s = fma((double)T[(int64_t)(1 + v) * m + j], (double)T[(int64_t)(1 + n_V + v) * m + j], s);
+  a = t0 * t0;
+  b = s * scale;
+}
+
+// The adjoint's reduction, fused with the per-SNP terms: blocks [0, n_runs) each reduce one run of
+// consecutive SNPs of one window (runs[3r …] = first SNP, end, window), part[2r …] = Σ gw_j·(a_j, b_j);
+// blocks from n_runs each reduce a chunk of all m SNPs weighted by W_j (the handle's weights,
+// gw·wwin), glob[2b …] = Σ W_j·(a_j, b_j).  The partials are summed in a fixed order afterwards, so
+// the gradient is bit-reproducible.
+constexpr int kGradChunk = 8192;
+__global__ void __launch_bounds__(256)
+grad_window_kernel(const float* __restrict__ T, int64_t m, int n_V, double scale, const float* __restrict__ gw,
+                   const float* __restrict__ W, const int64_t* __restrict__ runs, int n_runs,
+                   double* __restrict__ part, double* __restrict__ glob)
+{
+  __shared__ double sh[32];
+  int64_t j0, j1;
+  const float* wt;
+  double* dst;
+  if ((int)blockIdx.x < n_runs) {
+    j0 = runs[3 * (int64_t)blockIdx.x];
+    j1 = runs[3 * (int64_t)blockIdx.x + 1];
+    wt = gw;
+    dst = part + 2 * (int64_t)blockIdx.x;
+  } else {
+    const int64_t b = (int64_t)blockIdx.x - n_runs;
+    j0 = b * kGradChunk;
+    j1 = min64(m, j0 + kGradChunk);
+    wt = W;
+    dst = glob + 2 * b;
+  }
+  double sa = 0.0, sb = 0.0;
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    double a, b;
+    grad_terms(T, m, n_V, scale, j, a, b);
+    const double w = (double)wt[j];
+    sa = fma(w, a, sa);
+    sb = fma(w, b, sb);
+  }
+  sa = block_sum_d(sa, sh);
+  sb = block_sum_d(sb, sh);
+  if (threadIdx.x == 0) {
+    dst[0] = sa;
+    dst[1] = sb;
+  }
+}
+
+// grad[0] = −½(Σ W·b/σ_g² − Σ W·a/σ_g⁴) from the chunk partials (thread 0), and for window q
+// (thread q + 1) grad[2 + q] = −½(Σ gw·b − Σ gw·a/σ_g²) over its runs, taken in SNP order from the
+// CSR lists wrun_off / wrun.  grad[1] is the host's (it needs no per-SNP term).
+__global__ void grad_window_final_kernel(const double* __restrict__ part, const double* __restrict__ glob, int nglob,
+                                         const int* __restrict__ wrun_off, const int* __restrict__ wrun, int n_win,
+                                         double sg2, double* __restrict__ grad)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int b = 0; b < nglob; ++b) {
+      sa += glob[2 * b];
+      sb += glob[2 * b + 1];
+    }
+    grad[0] = -0.5 * (sb / sg2 - sa / (sg2 * sg2));
+  } else if (t <= n_win) {
+    const int q = t - 1;
+    double ga = 0.0, gb = 0.0;
+    for (int r = wrun_off[q]; r < wrun_off[q + 1]; ++r) {
+      ga += part[2 * (int64_t)wrun[r]];
+      gb += part[2 * (int64_t)wrun[r] + 1];
+    }
+    grad[2 + q] = -0.5 * (gb - ga / sg2);
   }
 }
 
@@ -830,30 +899,54 @@ void reml_grad(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     throw;
   }
   g->prec = prec;
-  // per-SNP a_j, b_j on the device; only these 2m doubles come back
-  double* d_ab = (double*)d_U.p;   // U is free again (n·k floats ≥ 2m doubles is checked below)
-  DevBuf d_abuf(st);
-  if ((size_t)n * k * sizeof(float) < 2 * (size_t)m * sizeof(double))
-    d_ab = (double*)d_abuf.ensure(2 * (size_t)m * sizeof(double));
-  grad_terms_kernel<<<(unsigned)std::min<int64_t>(ceil_div(m, 256), 152 * 8), 256, 0, st>>>(
-      d_T.as<float>(), m, n_V, (double)n / (double)n_V, d_ab);
-  LAUNCH_CHECK();
-  const std::vector<double> ab = d2h(g, d_ab, 2 * (size_t)m);
-  check_device_error(g);
-  double sa = 0.0, sb = 0.0;
-  std::vector<double> ga(std::max(n_win, 1), 0.0), gb(std::max(n_win, 1), 0.0);
-  for (int64_t j = 0; j < m; ++j) {
-    const double a = ab[j], b = ab[m + j];
-    sa += (double)W[j] * a;
-    sb += (double)W[j] * b;
-    if (window && window[j] >= 0) {
-      ga[window[j]] += (double)S.gw[j] * a;
-      gb[window[j]] += (double)S.gw[j] * b;
+  // Per-window reduction on the device, fused with the per-SNP terms: runs of consecutive SNPs of
+  // one window (one run per window when windows are contiguous), reduced by one block each; only
+  // the 2 + n_win gradient entries come back.
+  std::vector<int64_t> runs;   // first SNP, end, window
+  if (window) {
+    for (int64_t j = 0; j < m;) {
+      const int q = window[j];
+      int64_t e = j + 1;
+      while (e < m && window[e] == q) ++e;
+      if (q >= 0) runs.insert(runs.end(), {j, e, (int64_t)q});
+      j = e;
     }
   }
-  grad[0] = -0.5 * (sb / sg2 - sa / (sg2 * sg2));
+  const int n_runs = (int)(runs.size() / 3);
+  std::vector<int> wrun_off((size_t)std::max(n_win, 0) + 1, 0), wrun(n_runs);
+  for (int r = 0; r < n_runs; ++r) ++wrun_off[runs[3 * r + 2] + 1];
+  for (int q = 0; q < n_win; ++q) wrun_off[q + 1] += wrun_off[q];
+  {
+    std::vector<int> fill(wrun_off.begin(), wrun_off.end() - 1);
+    for (int r = 0; r < n_runs; ++r) wrun[fill[runs[3 * r + 2]]++] = r;   // a window's runs in SNP order
+  }
+  const int nglob = (int)ceil_div(m, kGradChunk);
+  DevBuf d_gw(st), d_runs(st), d_wrun(st), d_part(st), d_grad(st);
+  d_gw.ensure((size_t)m * sizeof(float));
+  d_runs.ensure(std::max<size_t>(runs.size(), 1) * sizeof(int64_t));
+  d_wrun.ensure(((size_t)n_win + 1 + n_runs) * sizeof(int));
+  double* part = (double*)d_part.ensure(2 * ((size_t)n_runs + nglob) * sizeof(double));
+  double* d_g = (double*)d_grad.ensure(((size_t)n_win + 2) * sizeof(double));
+  upload(g, d_gw.as<float>(), S.gw.data(), m);
+  if (n_runs) {
+    CUDA_TRY(cudaMemcpyAsync(d_runs.p, runs.data(), runs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_wrun.as<int>() + n_win + 1, wrun.data(), (size_t)n_runs * sizeof(int),
+                             cudaMemcpyHostToDevice, st));
+  }
+  CUDA_TRY(cudaMemcpyAsync(d_wrun.p, wrun_off.data(), ((size_t)n_win + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  grad_window_kernel<<<(unsigned)(n_runs + nglob), 256, 0, st>>>(d_T.as<float>(), m, n_V, (double)n / (double)n_V,
+                                                                   d_gw.as<float>(), g->w.as<float>(),
+                                                                   d_runs.as<int64_t>(), n_runs, part,
+                                                                   part + 2 * (size_t)n_runs);
+  LAUNCH_CHECK();
+  grad_window_final_kernel<<<(unsigned)ceil_div(n_win + 1, 256), 256, 0, st>>>(
+      part, part + 2 * (size_t)n_runs, nglob, d_wrun.as<int>(), d_wrun.as<int>() + n_win + 1, n_win, sg2, d_g);
+  LAUNCH_CHECK();
+  const std::vector<double> gv = d2h(g, d_g, (size_t)n_win + 2);
+  check_device_error(g);
+  grad[0] = gv[0];
   grad[1] = -0.5 * (trP / sg2 - pyy / (sg2 * sg2));
-  for (int q = 0; q < n_win; ++q) grad[2 + q] = -0.5 * (gb[q] - ga[q] / sg2);
+  for (int q = 0; q < n_win; ++q) grad[2 + q] = gv[2 + q];
 }
 
 extern "C" {
