@@ -30,6 +30,39 @@ def gpu(built_lib):
     return built_lib
 
 
+def gss_margins(trace):
+    """|fc − fd| at each golden-section iteration, from the evaluations in order (c₀, d₀, then one
+    new point per iteration), with the reference's bookkeeping (src/reml.cpp:526-541)."""
+    pts = [p for p, _ in trace]
+    f = [v for _, v in trace]
+    c, fc, d, fd = pts[0], f[0], pts[1], f[1]
+    out = []
+    for i in range(2, len(pts)):
+        out.append(abs(fc - fd))
+        if fc > fd:
+            d, fd = c, fc
+            c, fc = pts[i], f[i]
+        else:
+            c, fc = d, fd
+            d, fd = pts[i], f[i]
+    return out
+
+
+def check_gss_branches(got, want, f_tol):
+    """A GPU golden-section trace against the oracle's: the same h² points until the first branch
+    the oracle itself took by a criterion margin of at most 2·f_tol, and 2logLL within f_tol at
+    every common point.  Returns the number of common points."""
+    want = [(float(p), float(v)) for p, v in want]
+    assert len(got) == len(want)
+    margins = gss_margins(want)
+    k = next((i for i, (a, b) in enumerate(zip(got, want)) if a[0] != b[0]), len(want))
+    if k < len(want):
+        assert k >= 2 and margins[k - 2] <= 2 * f_tol, (k, margins[k - 2])
+    for i in range(k):
+        assert abs(got[i][1] - want[i][1]) <= f_tol, (i, got[i][1], want[i][1])
+    return k
+
+
 def make_case(n_fam, m, seed=1, missing=0.0, keep_frac=1.0):
     """Synthetic .bed rows plus the oracle's decoded counts of the kept individuals."""
     from oracle import slemm_np as orc

@@ -12,7 +12,8 @@ oracle/_ref exist; the fixtures are committed and the tests read only them).
                      by tests/golden/pgenlib_shim, which reads PLINK1 .bed files).
   gwa_case/          the same kind of case for the reference's bin/slemm_gwa.py (windowed
                      MLMA on chromosome 1), with step-1 files from the oracle.
-Usage: python tests/golden/make_golden.py [/path/to/reference] [gwa]
+Usage: python tests/golden/make_golden.py /path/to/reference/checkout [gwa]
+(or with the checkout in the SLEMM_REFERENCE environment variable)
 """
 import ctypes
 import json
@@ -25,7 +26,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "gwa" else os.environ.get("SLEMM_REFERENCE", "")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("give the reference checkout as the first argument or in SLEMM_REFERENCE")
 
 
 def hwe():

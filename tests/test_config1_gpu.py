@@ -18,6 +18,7 @@ test_oracle.test_fp32_reference_gss_spread_at_config1 records on the CPU; so the
 import numpy as np
 import pytest
 
+from conftest import check_gss_branches
 from oracle import slemm_np as orc
 from slemm_gb300 import _lib, api, synth
 
@@ -44,24 +45,6 @@ def case1():
     return out
 
 
-def gss_margins(trace):
-    """|fc − fd| at each golden-section iteration, from the evaluations in order (c₀, d₀, then one
-    new point per iteration), with the reference's bookkeeping (src/reml.cpp:526-541)."""
-    pts = [p for p, _ in trace]
-    f = [v for _, v in trace]
-    c, fc, d, fd = pts[0], f[0], pts[1], f[1]
-    out = []
-    for i in range(2, len(pts)):
-        out.append(abs(fc - fd))
-        if fc > fd:
-            d, fd = c, fc
-            c, fc = pts[i], f[i]
-        else:
-            c, fc = d, fd
-            d, fd = pts[i], f[i]
-    return out
-
-
 @pytest.mark.parametrize("prec", PRECS)
 def test_sldf_config1(gpu, case1, prec):
     r64, r32 = case1["sldf64"], case1["sldf32"]
@@ -70,15 +53,8 @@ def test_sldf_config1(gpu, case1, prec):
         r = g.SLDF_REML(None, case1["X"], case1["y"], case1["persnp"], seed=SEED, n_V=N_V)
         gebv = g.gebv(r["snp_blup"].astype(np.float64))
     assert r["n_criterion"] == len(r64["gss"]) == len(r["trace"])
-    want = [(float(p), float(v)) for p, v in r64["gss"]]
-    got = r["trace"]
     # identical points until the first branch the FP64 oracle took by a margin ≤ 2·F_TOL
-    margins = gss_margins(want)
-    k = next((i for i, (a, b) in enumerate(zip(got, want)) if a[0] != b[0]), len(want))
-    if k < len(want):
-        assert k >= 2 and margins[k - 2] <= 2 * F_TOL, (k, margins[k - 2])
-    for i in range(k):
-        assert abs(got[i][1] - want[i][1]) <= F_TOL, (i, got[i][1], want[i][1])
+    check_gss_branches(r["trace"], r64["gss"], F_TOL)
     assert abs(r["h2"] - r64["h2"]) <= 1e-4
     assert abs(r["h2"] - r32["h2"]) <= abs(r32["h2"] - r64["h2"]) + 1e-4
     assert np.corrcoef(r["snp_blup"], r64["snp_blup"])[0, 1] >= 0.99999
