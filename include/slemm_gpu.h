@@ -331,6 +331,15 @@ int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t ldv, int k,
 int slemm_gpu_profile(slemm_geno* g, int enable, int max_rows, int* rows, int32_t* info,
                       int64_t* launches, double* ms);
 
+/* ---- failure-path test support -------------------------------------------------------------- */
+/* No counterpart in the reference.  Every wait inside the tensor-core product is bounded (2 s);
+ * a wait that runs out sets the handle's device error word, makes the CTA drain its copies in
+ * flight and free its tensor memory, and the call returns SLEMM_ERR_CUDA.  This makes the next
+ * tensor-core launch (any handle, this process) skip the dense-operand copy of stage `stage` in
+ * its first CTA, so that CTA's waits run out exactly as they would if a copy never arrived;
+ * stage < 0 clears a pending request.  One-shot: the launch that uses it resets it. */
+int slemm_gpu_test_withhold_b_stage(int stage);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,7 @@ _SIGS = {
     "slemm_gpu_gebv": (I32, [P, P, P, P]),
     "slemm_gpu_score_terms": (I32, [P, P, I32, P, P]),
     "slemm_gpu_profile": (I32, [P, I32, I32, ctypes.POINTER(I32), P, P, P]),
+    "slemm_gpu_test_withhold_b_stage": (I32, [I32]),
     "slemm_gpu_rademacher": (I32, [I32, I64, I32, P, I64, I32]),
 }
 

@@ -257,7 +257,7 @@ template <int PK, int S, int SB, int KT, bool F16>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
                float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
-               int kp, int pieces, int* __restrict__ err)
+               int kp, int pieces, int* __restrict__ err, int withhold)
 {
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment of the shared-window address (SWIZZLE_128B tiles need it)
@@ -350,6 +350,10 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
         uint64_t* full = (SB > 0) ? &b_full[s] : &st_full[s];
         if (i >= BS && !mbar_wait(&done[s], (round - 1) & 1, err, 16, abort_flag, 128)) break;
         if (*abort_flag) break;
+        if (i == withhold && blockIdx.x == 0 && blockIdx.y == 0) {   // test support: the stage never fills
+          ++issued;
+          continue;
+        }
         mbar_arrive_expect_tx(full, (uint32_t)KT * bytes);
         for (int kk = 0; kk < KT; ++kk)
           tma_load_2d(sB + ((size_t)s * KT + kk) * N * 128, &tmapB, (kt0 + i * KT + kk) * kTileK, 0, full);
@@ -490,6 +494,10 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
 }
 
 // ---- host side ------------------------------------------------------------------------------
+// Test support (slemm_gpu_test_withhold_b_stage): the B stage the next tensor-core launch leaves
+// unfilled in its first CTA, or −1.  Read and reset by that launch.
+static std::atomic<int> g_withhold_b{-1};
+
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                     const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                     const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -559,7 +567,8 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
   const size_t smem = std::max<size_t>(P.total, 120 * 1024);
   dim3 grid((unsigned)Mc, (unsigned)a.splits);
   gemm_tc_kernel<PK, S, SB, KT, F16><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N,
-                                                                       P.sub, a.kp, a.pieces, a.err);
+                                                                       P.sub, a.kp, a.pieces, a.err,
+                                                                       g_withhold_b.exchange(-1));
   LAUNCH_CHECK();
 }
 
@@ -576,3 +585,9 @@ void gemm_tc(const GemmArgs& a, cudaStream_t st)
 }
 
 }  // namespace slemm
+
+extern "C" int slemm_gpu_test_withhold_b_stage(int stage)
+{
+  slemm::g_withhold_b.store(stage < 0 ? -1 : stage);
+  return SLEMM_OK;
+}
