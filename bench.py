@@ -249,8 +249,10 @@ SUBSET = 1000   # the reference's SNP subset size (--subset_size default, src/op
 # the reference's arithmetic) on each workload, as the GPU arm's `fp32_*.counts` reports them: the
 # reference arm multiplies its measured per-application times by these.
 REF_STEPS = {
-    2: None,
-    3: None,
+    2: dict(iters_y=14, iters_Q=1, iters_V=14, c=1,
+            source="FP32 per-vector GPU fit of the n=100000 m=50000 workload (fp32_per_vector.counts)"),
+    3: dict(iters_y=297, iters_Q=2, iters_V=303, c=1, first_iters_V=15, first_n_criterion=4, n_mc=3,
+            source="FP32 per-vector GPU fit of the n=500000 m=60000 window-weighted workload (fp32_per_vector.counts)"),
 }
 
 

@@ -367,10 +367,10 @@ def L_Seed(ops: Operators, lnr, tau0, B, tol=5e-4, maxit=600, reorth=False):
             tmp = tmp - U[j - 1] * beta[:, j]
         delta[:, j] = (U[j] * tmp).sum(axis=0, dtype=dt)
         tmp = tmp - U[j] * delta[:, j]
-        if reorth:
-            Ub = np.stack(U)                                   # (j+1)×n×t
-            d = np.einsum("inc,nc->ic", Ub, tmp)               # U_i[:,c]ᵀ w[:,c]
-            tmp = tmp - np.einsum("ic,inc->nc", d, Ub)
+        if reorth:   # classical Gram–Schmidt: all coefficients from w before the pass
+            d = [(Ui * tmp).sum(axis=0, dtype=dt) for Ui in U]   # U_i[:,c]ᵀ w[:,c]
+            for Ui, di in zip(U, d):
+                tmp = tmp - Ui * di
         beta[:, j + 1] = np.sqrt((tmp * tmp).sum(axis=0, dtype=dt))
         U.append(tmp / beta[:, j + 1])
         if j == 0:
