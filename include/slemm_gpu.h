@@ -323,6 +323,21 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
 int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t ldv, int k, float* out,
                               int64_t ldo);
 
+/* ---- split-K autotuner (no counterpart in the reference, whose subset size is a flag,
+ * src/option.cpp:53-78) ------------------------------------------------------------------------- */
+/* on = 1: the handle's tensor-core passes pick their split-K count by timing, at the first pass of
+ * each shape (device, N, pieces, K-tiles, padded rows), the fixed rule's count and up to five
+ * counts near it that fill the last wave of CTAs well — one warm-up and two timed launches each,
+ * CUDA events on the handle's stream — and keep the fastest when it beats the rule's by ≥ 3 %.
+ * Decisions are cached for the process (shared by all handles); nothing is tuned while the stream
+ * is being captured.  Plans change the order of the split-K sums, so results of a tuned handle
+ * may differ from a default one's in the last bits.  on = 0 (the default): the fixed rule. */
+int slemm_gpu_set_autotune(slemm_geno* g, int on);
+/* The cached decisions: *rows = their number; for r < max_rows, info[6r …] = {device, N, pieces,
+ * rule's splits, chosen splits, candidates timed}, shape[2r …] = {K-tiles, padded rows},
+ * ms[2r …] = {rule's ms per launch, chosen ms per launch}.  Any of info, shape, ms may be NULL. */
+int slemm_gpu_autotune_table(int max_rows, int* rows, int32_t* info, int64_t* shape, double* ms);
+
 /* ---- measurement ---------------------------------------------------------------------------------- */
 /* Per-launch timing of the packed products with CUDA events on the handle's stream (no
  * counterpart in the reference, which only prints wall-clock times, src/option.cpp:21-34).

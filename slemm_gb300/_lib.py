@@ -70,6 +70,8 @@ _SIGS = {
     "slemm_gpu_set_precision": (I32, [P, I32]),
     "slemm_gpu_set_per_vector": (I32, [P, I32]),
     "slemm_gpu_set_lanczos": (I32, [P, I32]),
+    "slemm_gpu_set_autotune": (I32, [P, I32]),
+    "slemm_gpu_autotune_table": (I32, [I32, ctypes.POINTER(I32), P, P, P]),
     "slemm_gpu_op": (I32, [P, I32, F32, P, I64, I32, P, I64, I32]),
     "slemm_gpu_lanczos_seed": (I32, [P, I32, F32, P, I64, I32, F32, I32, I32, ctypes.POINTER(P),
                                      ctypes.POINTER(I32)]),

@@ -126,6 +126,10 @@ class Genotypes:
     def set_per_vector(self, flag: bool):
         check(self._lib.slemm_gpu_set_per_vector(self.h, 1 if flag else 0))
 
+    def set_autotune(self, on: bool = True):
+        """Split-K counts of this handle's tensor-core passes picked by timing at first use."""
+        check(self._lib.slemm_gpu_set_autotune(self.h, 1 if on else 0))
+
     def set_lanczos(self, reorth: bool = False):
         """Lanczos mode of the seeds run on this handle (default: the reference's recurrence)."""
         check(self._lib.slemm_gpu_set_lanczos(self.h, _lib.LANCZOS_REORTH if reorth else 0))
@@ -376,3 +380,19 @@ def tridiag_eig(delta, beta):
     W2 = np.zeros((t, nld), np.float64, order="F")
     check(_lib.load().slemm_gpu_tridiag_eig(_ptr(delta), _ptr(beta), t, nld, _ptr(D), _ptr(W2)))
     return D, W2
+
+
+def autotune_table():
+    """The tuner's cached decisions: one dict per shape."""
+    lib = _lib.load()
+    rows = ctypes.c_int(0)
+    check(lib.slemm_gpu_autotune_table(0, ctypes.byref(rows), None, None, None))
+    r = rows.value
+    info = np.zeros(6 * max(r, 1), np.int32)
+    shape = np.zeros(2 * max(r, 1), np.int64)
+    ms = np.zeros(2 * max(r, 1), np.float64)
+    check(lib.slemm_gpu_autotune_table(r, ctypes.byref(rows), _ptr(info), _ptr(shape), _ptr(ms)))
+    return [dict(device=int(info[6 * i]), N=int(info[6 * i + 1]), pieces=int(info[6 * i + 2]),
+                 rule_splits=int(info[6 * i + 3]), splits=int(info[6 * i + 4]), candidates=int(info[6 * i + 5]),
+                 K_tiles=int(shape[2 * i]), M_pad=int(shape[2 * i + 1]), ms_rule=float(ms[2 * i]),
+                 ms=float(ms[2 * i + 1])) for i in range(r)]

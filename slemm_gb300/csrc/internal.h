@@ -18,6 +18,7 @@ struct slemm_geno {
   int prec = SLEMM_PREC_BF16X2;
   int per_vector = 0;
   int lanczos_mode = 0;           // SLEMM_LANCZOS_* bits of the seeds run on this handle
+  bool autotune = false;          // tensor-core passes take their split-K count from the tuner
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // work buffers

@@ -21,6 +21,9 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <map>
+#include <mutex>
+
 namespace slemm {
 
 constexpr int kRedThreads = 256;
@@ -648,7 +651,86 @@ static int tc_min_splits(int64_t K_tiles, int N)
   return dense_bytes > 64.0 * 1024 * 1024 ? (int)ceil_div(K_tiles, 1536) : 1;
 }
 
-static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_pad)
+static cudaEvent_t take_event(slemm_geno* g);
+
+// ---- split-K autotuner ------------------------------------------------------------------------------
+// With a handle's autotune on, the first tensor-core pass of each shape (device, N, pieces, K-tiles,
+// padded rows) times a handful of split-K counts with CUDA events on the handle's stream — the
+// fixed rule's count, and counts near it whose CTAs fill the last wave to ≥ 80 % — each launched
+// once to warm up and twice timed over the real packed copy, and keeps the fastest if it beats the
+// rule's by ≥ 3 % (else the rule's, so close calls do not flip between processes).  Decisions are
+// cached for the life of the process; no tuning happens while the stream is being captured.
+struct TuneKey {
+  int dev, N, pieces;
+  int64_t K_tiles, M_pad;
+  bool operator<(const TuneKey& o) const
+  {
+    return std::tie(dev, N, pieces, K_tiles, M_pad) < std::tie(o.dev, o.N, o.pieces, o.K_tiles, o.M_pad);
+  }
+};
+struct TuneEntry {
+  int rule, best, candidates;
+  double ms_rule, ms_best;
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneEntry> g_tune;
+
+static int tune_splits(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t M_pad, int64_t K_pad, int rule)
+{
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return rule;
+  const int64_t K_tiles = K_pad / kTileK;
+  const TuneKey key{g->device, p.N, p.pieces, K_tiles, M_pad};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second.best;
+  }
+  // candidates: the rule's count, then counts near it with a well-filled last wave
+  const int64_t ctas = M_pad / gemm_tc_rows_per_cta(p.N);
+  const int sms = num_sms();
+  std::vector<int> cand{rule};
+  std::vector<std::pair<int, int>> near;   // (distance, s)
+  const int smax = (int)std::min<int64_t>(std::max(3 * rule + 2, 8), std::max<int64_t>(1, K_tiles / 16));
+  for (int s = std::max(1, rule / 3); s <= smax; ++s) {
+    if (s == rule) continue;
+    const double waves = (double)(ctas * s) / sms;
+    if (waves / std::ceil(waves) >= 0.8) near.push_back({std::abs(s - rule), s});
+  }
+  std::sort(near.begin(), near.end());
+  for (size_t i = 0; i < near.size() && cand.size() < 6; ++i) cand.push_back(near[i].second);
+  const int smost = *std::max_element(cand.begin(), cand.end());
+  DevBuf dD(g->stream);
+  float* D = (float*)dD.ensure((size_t)smost * p.kp * M_pad * sizeof(float));
+  const void* B = g->ws_B.ensure((size_t)p.N * K_pad * 2);   // timing only: the operand's values do not matter
+  cudaEvent_t e0 = take_event(g), e1 = take_event(g);
+  std::vector<double> ms(cand.size());
+  for (size_t i = 0; i < cand.size(); ++i) {
+    GemmArgs a{A, M_pad, K_pad, B, p.N, D, cand[i], g->err.as<int>(), p.kp, p.pieces, p.f16};
+    gemm_tc(a, g->stream);
+    CUDA_TRY(cudaEventRecord(e0, g->stream));
+    gemm_tc(a, g->stream);
+    gemm_tc(a, g->stream);
+    CUDA_TRY(cudaEventRecord(e1, g->stream));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+    ms[i] = t / 2.0;
+  }
+  g->event_pool.push_back(e0);
+  g->event_pool.push_back(e1);
+  CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));   // the timing launches' waits are not the caller's
+  size_t b = 0;
+  for (size_t i = 1; i < cand.size(); ++i)
+    if (ms[i] < ms[b]) b = i;
+  if (ms[b] > 0.97 * ms[0]) b = 0;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = {rule, cand[b], (int)cand.size(), ms[0], ms[b]};
+  return cand[b];
+}
+
+static PassPlan plan_pass(slemm_geno* g, int k, int64_t M_pad, int64_t K_pad, const uint8_t* A)
 {
   PassPlan p;
   p.tc = g->prec != SLEMM_PREC_FP32;
@@ -660,6 +742,7 @@ static PassPlan plan_pass(const slemm_geno* g, int k, int64_t M_pad, int64_t K_p
   p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(),
                                   tc_min_splits(K_tiles, p.N))
                   : choose_splits(M_tiles, K_tiles, 8, num_sms());
+  if (p.tc && g->autotune && A) p.splits = tune_splits(g, p, A, M_pad, K_pad, p.splits);
   return p;
 }
 
@@ -737,8 +820,9 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   cudaStream_t st = g->stream;
   const bool dir1 = kind != SLEMM_OP_MATVEC;                          // needs Zᵀ pass
   const bool dir2 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET || kind == SLEMM_OP_MATVEC;
-  const PassPlan p1 = plan_pass(g, k, g->m_pad, g->n_pad);             // M = SNPs, K = indiv
-  const PassPlan p2 = plan_pass(g, k, g->n_pad, g->m_pad);             // M = indiv, K = SNPs
+  // (the tuner times only the directions this operator runs)
+  const PassPlan p1 = plan_pass(g, k, g->m_pad, g->n_pad, dir1 ? g->G.as<uint8_t>() : nullptr);    // M = SNPs, K = indiv
+  const PassPlan p2 = plan_pass(g, k, g->n_pad, g->m_pad, dir2 ? g->GT.as<uint8_t>() : nullptr);   // M = indiv, K = SNPs
   const int np1 = p1.tc ? p1.pieces : 0, np2 = p2.tc ? p2.pieces : 0;
   const int pad1 = p1.tc ? p1.N - p1.pieces * k : 0;                   // padding rows of the operands
   const int pad2 = p2.tc ? p2.N - p2.pieces * k : 0;
@@ -1032,6 +1116,42 @@ void check_device_error(slemm_geno* g)
 }  // namespace slemm
 
 using namespace slemm;
+
+extern "C" int slemm_gpu_set_autotune(slemm_geno* g, int on)
+{
+  return guarded([&] {
+    CHECK_ARG(g != nullptr, "null handle");
+    CHECK_ARG(on == 0 || on == 1, "on must be 0 or 1");
+    g->autotune = on != 0;
+  });
+}
+
+extern "C" int slemm_gpu_autotune_table(int max_rows, int* rows, int32_t* info, int64_t* shape, double* ms)
+{
+  return guarded([&] {
+    CHECK_ARG(rows != nullptr && max_rows >= 0, "bad arguments");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    *rows = (int)g_tune.size();
+    int r = 0;
+    for (const auto& kv : g_tune) {
+      if (r >= max_rows) break;
+      if (info) {
+        const int32_t v[6] = {kv.first.dev, kv.first.N, kv.first.pieces, kv.second.rule, kv.second.best,
+                              kv.second.candidates};
+        std::copy(v, v + 6, info + 6 * r);
+      }
+      if (shape) {
+        shape[2 * r] = kv.first.K_tiles;
+        shape[2 * r + 1] = kv.first.M_pad;
+      }
+      if (ms) {
+        ms[2 * r] = kv.second.ms_rule;
+        ms[2 * r + 1] = kv.second.ms_best;
+      }
+      ++r;
+    }
+  });
+}
 
 extern "C" int slemm_gpu_op(slemm_geno* g, int op_kind, float tau0, const float* in, int64_t ld_in,
                             int k, float* out, int64_t ld_out, int mem)
