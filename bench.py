@@ -491,6 +491,7 @@ def run_gpu(args, cfg):
     g = api.Genotypes(rows_np, n)
     stream = torch.cuda.ExternalStream(g.stream())
     g.set_precision(prec)
+    g.set_autotune(not args.no_autotune)   # shapes are tuned during the warm-up fits
     # clock samplers start before the warm-up (their start-up stays out of the timed steps) and
     # keep only the samples of the timed window
     nvml = NvmlSampler(local).__enter__()
@@ -528,6 +529,7 @@ def run_gpu(args, cfg):
         t0 = time.perf_counter()
         with api.Genotypes(rows_pinned, n) as g2:
             g2.set_precision(prec)
+            g2.set_autotune(not args.no_autotune)
             fit(g2)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
@@ -608,6 +610,7 @@ def run_gpu(args, cfg):
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches / max(args.steps, 1)),
         "roofline": roof,
+        "autotune": None if args.no_autotune else api.autotune_table(),
         "cpu_baseline": cpu,
         "integer_stages": integer,
         "clocks": nvml.summary() or clocks.summary(),
@@ -1125,6 +1128,8 @@ def main():
     ap.add_argument("--fp32", default="per_vector", choices=["per_vector", "batched", "skip"],
                     help="the plain FP32 GPU fit the metric compares with")
     ap.add_argument("--skip-fp32", action="store_true", help="same as --fp32 skip")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="fixed split-K rule instead of the autotuner's timed choice")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-subsets", type=int, default=4)
     ap.add_argument("--ref-budget", type=float, default=120.0,
