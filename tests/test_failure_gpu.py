@@ -37,7 +37,7 @@ def test_withheld_copy_times_out_and_handle_recovers(gpu, k):
         with pytest.raises(_lib.SlemmError) as e:
             g.rmatvec(v)
         elapsed = time.perf_counter() - t0
-        assert e.value.args[0] == -2                     # SLEMM_ERR_CUDA
+        assert e.value.code == -2                        # SLEMM_ERR_CUDA
         assert "bounded wait" in str(e.value)
         assert 1.5 < elapsed < 30.0                      # the 2 s budget ran out, then the CTA drained
         # the request was one-shot and the error word was cleared: the next call is correct
