@@ -94,6 +94,17 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
                               int64_t row_stride, const int64_t* keep_idx, int64_t n,
                               int flags, slemm_geno** out);
 int slemm_gpu_genotype_destroy(slemm_geno* g);
+/* A trait view: a handle over the individuals keep_idx (n increasing indices into the parent's
+ * individuals) that shares the parent's packed copies instead of packing its own — for several
+ * traits with their own missing individuals over one .bed (the reference analyses each trait on its
+ * own individual set, src/input.cpp:287, src/option.cpp:320, and so does a view: its counts, allele
+ * frequencies, centring, weights and fits are those of its individuals).  The operators read
+ * inputs and write outputs through the view's individual map; the products stream the parent's
+ * copies.  The view has its own stream, weights, projection and precision; the parent must outlive
+ * it and must not be changed meanwhile.  Entry points that read the packed copies directly
+ * (gebv, score_terms, gwa_windows, lmm_quadforms, wls, rmatvec_noalloc) return
+ * SLEMM_ERR_UNSUPPORTED on a view.  Destroy with slemm_gpu_genotype_destroy. */
+int slemm_gpu_genotype_view(slemm_geno* parent, const int64_t* keep_idx, int64_t n, slemm_geno** out);
 int slemm_gpu_genotype_dims(const slemm_geno* g, int64_t* n, int64_t* m);
 /* Binds the handle's work to a caller stream (cudaStream_t passed as void*; NULL = own stream). */
 int slemm_gpu_set_stream(slemm_geno* g, void* stream);

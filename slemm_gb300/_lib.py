@@ -58,6 +58,7 @@ _SIGS = {
     "slemm_gpu_launch_count": (I64, []),
     "slemm_gpu_genotype_create": (I32, [P, I64, I64, I64, P, I64, I32, ctypes.POINTER(P)]),
     "slemm_gpu_genotype_destroy": (I32, [P]),
+    "slemm_gpu_genotype_view": (I32, [P, P, I64, ctypes.POINTER(P)]),
     "slemm_gpu_genotype_dims": (I32, [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "slemm_gpu_set_stream": (I32, [P, P]),
     "slemm_gpu_get_stream": (I32, [P, ctypes.POINTER(P)]),

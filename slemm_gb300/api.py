@@ -64,6 +64,20 @@ class Genotypes:
         self.h = h
         self.n, self.m = int(n), int(m)
 
+    @classmethod
+    def view(cls, parent: "Genotypes", keep_idx):
+        """A handle over the parent's individuals keep_idx that shares the parent's packed copies
+        (slemm_gpu_genotype_view); the parent must stay open while the view is used."""
+        keep = np.ascontiguousarray(keep_idx, dtype=np.int64)
+        self = cls.__new__(cls)
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.slemm_gpu_genotype_view(parent.h, _ptr(keep), keep.size, ctypes.byref(h)))
+        self.h = h
+        self.n, self.m = int(keep.size), parent.m
+        self._parent = parent   # keeps the parent alive as long as the view
+        return self
+
     def close(self):
         if getattr(self, "h", None):
             check(self._lib.slemm_gpu_genotype_destroy(self.h))

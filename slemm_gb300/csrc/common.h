@@ -89,6 +89,7 @@ struct DevBuf {
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   bool ordered = false;
+  bool owned = true;   // false: p aliases another buffer (a trait view's packed copies), never freed here
   DevBuf() = default;
   explicit DevBuf(cudaStream_t s) : stream(s), ordered(true) {}
   DevBuf(const DevBuf&) = delete;
@@ -96,12 +97,21 @@ struct DevBuf {
   ~DevBuf() { release(); }
   void release()
   {
-    if (p) {
+    if (p && owned) {
       if (ordered) cudaFreeAsync(p, stream);
       else cudaFree(p);
     }
     p = nullptr;
     bytes = 0;
+    owned = true;
+  }
+  // Points at `other`'s memory without owning it.
+  void alias(const DevBuf& other)
+  {
+    release();
+    p = other.p;
+    bytes = other.bytes;
+    owned = false;
   }
   // Grows (never shrinks); contents are not preserved.
   void* ensure(size_t nbytes)

@@ -180,6 +180,9 @@ int slemm_gpu_gebv(slemm_geno* g, const double* alpha, const uint8_t* flip, doub
 {
   return guarded([&] {
     CHECK_ARG(g && alpha && tgv, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_gebv reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     cudaStream_t st = g->stream;
     std::vector<double> a(g->m_pad, 0.0);
     double shift = 0.0;
@@ -225,6 +228,9 @@ int slemm_gpu_score_terms(slemm_geno* g, const float* y, int mac, float* xy, flo
 {
   return guarded([&] {
     CHECK_ARG(g && y && xy && xx, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_score_terms reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     CHECK_ARG(g->weights_set, "set_weights (rr) must be called first");
     const int c = g->c;
     CHECK_ARG(c <= 14, "score terms support up to 14 projection columns");

@@ -252,6 +252,35 @@ __global__ void row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int
   }
 }
 
+// The same counts over the kept positions of a trait view only: kmask holds, per K-tile word, the
+// low bit of every kept 2-bit field.
+__global__ void masked_row_counts_kernel(const uint32_t* __restrict__ G, int64_t m, int64_t K_tiles,
+                                         const uint32_t* __restrict__ kmask, int64_t* __restrict__ pc,
+                                         int32_t* __restrict__ c1, int32_t* __restrict__ c2)
+{
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= m) return;
+  const int64_t mt = warp / 128, r = warp % 128;
+  long long ones = 0, twos = 0;
+  for (int64_t wi = lane; wi < K_tiles * 4; wi += 32) {
+    const int64_t kt = wi / 4, wr = wi % 4;
+    const uint32_t w = G[((mt * K_tiles + kt) * 128 + r) * 4 + wr];
+    const uint32_t mk = kmask[wi];
+    ones += __popc(w & mk);
+    twos += __popc(w & (mk << 1));
+  }
+  for (int o = 16; o; o >>= 1) {
+    ones += __shfl_xor_sync(0xffffffffu, ones, o);
+    twos += __shfl_xor_sync(0xffffffffu, twos, o);
+  }
+  if (lane == 0) {
+    pc[warp] = ones + 2 * twos;
+    c1[warp] = (int32_t)ones;
+    c2[warp] = (int32_t)twos;
+  }
+}
+
 }  // namespace slemm
 
 namespace slemm {
@@ -269,7 +298,10 @@ __global__ void counts_from_classes_kernel(const int32_t* __restrict__ n1, const
 void row_counts_device(slemm_geno* g, int64_t* pc, int32_t* c1, int32_t* c2)
 {
   const int th = 256;
-  if (g->dcounts_valid) {   // summed by the pack kernel
+  if (g->is_view) {   // the view's own individuals
+    masked_row_counts_kernel<<<(unsigned)ceil_div(g->m * 32, th), th, 0, g->stream>>>(
+        g->G.as<uint32_t>(), g->m, g->n_pad / kTileK, g->kmask.as<uint32_t>(), pc, c1, c2);
+  } else if (g->dcounts_valid) {   // summed by the pack kernel
     const int32_t* n1 = g->dcounts.as<int32_t>();
     counts_from_classes_kernel<<<(unsigned)ceil_div(g->m, th), th, 0, g->stream>>>(n1, n1 + g->m_pad, g->m, pc, c1, c2);
   } else {
@@ -451,6 +483,66 @@ int slemm_gpu_genotype_destroy(slemm_geno* g)
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
+  });
+}
+
+int slemm_gpu_genotype_view(slemm_geno* parent, const int64_t* keep_idx, int64_t n, slemm_geno** out)
+{
+  return guarded([&] {
+    CHECK_ARG(out != nullptr, "out is null");
+    *out = nullptr;
+    CHECK_ARG(parent != nullptr && keep_idx != nullptr, "null argument");
+    CHECK_ARG(!parent->is_view, "a view of a view is not supported; take the view of the parent");
+    CHECK_ARG(n >= 1 && n <= parent->n, "n out of [1, parent's individuals]");
+    for (int64_t r = 0; r < n; ++r)
+      CHECK_ARG(keep_idx[r] >= 0 && keep_idx[r] < parent->n && (r == 0 || keep_idx[r] > keep_idx[r - 1]),
+                "keep_idx must be increasing indices of the parent's individuals");
+    CUDA_TRY(cudaSetDevice(parent->device));
+    auto* g = new slemm_geno;
+    try {
+      g->device = parent->device;
+      CUDA_TRY(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      g->own_stream = true;
+      g->bind_stream();
+      g->is_view = true;
+      g->n = n;
+      g->m = parent->m;
+      g->n_pad = parent->n_pad;
+      g->m_pad = parent->m_pad;
+      g->prec = parent->prec;
+      g->G.alias(parent->G);
+      g->GT.alias(parent->GT);
+      // the parent's packed copies are complete once its queued work is
+      CUDA_TRY(cudaStreamSynchronize(parent->stream));
+      const int64_t K_tiles = g->n_pad / kTileK;
+      std::vector<int32_t> map(n), inv(g->n_pad, -1);
+      std::vector<uint32_t> mask((size_t)K_tiles * 4, 0u);
+      for (int64_t r = 0; r < n; ++r) {
+        const int64_t i = keep_idx[r];
+        map[r] = (int32_t)i;
+        inv[i] = (int32_t)r;
+        const int64_t e = i % 64, q = e % 16;
+        const int sh = (q & 1) ? 16 + (int)(q & ~1) : (int)q;   // bit of the element's 2-bit field
+        mask[(size_t)(i / 64) * 4 + e / 16] |= 1u << sh;
+      }
+      g->ind_map.ensure((size_t)n * sizeof(int32_t));
+      g->ind_inv.ensure((size_t)g->n_pad * sizeof(int32_t));
+      g->kmask.ensure(mask.size() * sizeof(uint32_t));
+      g->err.ensure(sizeof(int));
+      CUDA_TRY(cudaMemsetAsync(g->err.p, 0, sizeof(int), g->stream));
+      CUDA_TRY(cudaMemcpyAsync(g->ind_map.p, map.data(), map.size() * sizeof(int32_t), cudaMemcpyHostToDevice, g->stream));
+      CUDA_TRY(cudaMemcpyAsync(g->ind_inv.p, inv.data(), inv.size() * sizeof(int32_t), cudaMemcpyHostToDevice, g->stream));
+      CUDA_TRY(cudaMemcpyAsync(g->kmask.p, mask.data(), mask.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               g->stream));
+      CUDA_TRY(cudaStreamSynchronize(g->stream));   // the host vectors go out of scope
+    } catch (...) {
+      g->for_each_buf([](DevBuf& b) { b.release(); });
+      if (g->stream) cudaStreamSynchronize(g->stream);
+      if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+      delete g;
+      throw;
+    }
+    *out = g;
   });
 }
 

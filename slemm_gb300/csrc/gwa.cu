@@ -160,6 +160,9 @@ extern "C" int slemm_gpu_gwa_windows(slemm_geno* g, const float* y, const float*
 {
   return guarded([&] {
     CHECK_ARG(g && y && covar && model_idx && beta && se && chisq && pval, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_gwa_windows reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     const int64_t n = g->n, m = g->m;
     CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES && ldc >= n, "bad covariate matrix");
     CHECK_ARG(n_model >= 2 && test_begin >= 0 && test_end < m && test_begin <= test_end, "bad SNP ranges");

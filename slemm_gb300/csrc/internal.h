@@ -35,6 +35,13 @@ struct slemm_geno {
   // with a constant vector, set with the weights; the operators remove each input column's mean
   // and add it back through this term (see ops.cu)
   slemm::DevBuf gcorr;
+  // A trait view (slemm_gpu_genotype_view) aliases its parent's packed copies (G, GT, n_pad, m_pad
+  // are the parent's) and analyses a subset of the parent's individuals: ind_map[r] is the packed
+  // individual position of view row r (n entries), ind_inv[i] the view row of position i or −1
+  // (n_pad entries), kmask the field masks of the kept positions per K-tile (4 words each, the low
+  // bit of each kept 2-bit field) for its own integer counts.
+  bool is_view = false;
+  slemm::DevBuf ind_map, ind_inv, kmask;
   // per-SNP popcount and class counts of the packed copy (immutable): host copies on first request
   std::vector<int64_t> counts_pc;
   std::vector<int32_t> counts_c1, counts_c2;
@@ -58,7 +65,7 @@ struct slemm_geno {
   void for_each_buf(F&& f)
   {
     for (slemm::DevBuf* b : {&G, &GT, &gm, &w, &rr, &Q, &ws_B, &ws_D, &ws_red, &ws_small, &ws_T, &ws_in, &ws_out, &err,
-                             &dcounts, &gcorr})
+                             &dcounts, &gcorr, &ind_map, &ind_inv, &kmask})
       f(*b);
   }
   void bind_stream()

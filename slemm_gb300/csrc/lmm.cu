@@ -163,6 +163,9 @@ extern "C" int slemm_gpu_lmm_quadforms(slemm_geno* g, const float* Py, float tau
 {
   return guarded([&] {
     CHECK_ARG(g && Py && variants && xPy && xPx && xBx && xSx && count, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_lmm_quadforms reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     CHECK_ARG(g->weights_set, "set_weights must be called first");
     CHECK_ARG(num_qf >= 1 && num_qf <= 300, "num_qf_markers out of [1, 300]");
     CHECK_ARG(tau1 > 0.f && std::isfinite(tau1), "tau1 must be positive");

@@ -166,6 +166,9 @@ extern "C" int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t 
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr && v != nullptr && out != nullptr, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_rmatvec_noalloc reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     CHECK_ARG(k >= 1, "k must be >= 1");
     CHECK_ARG(ldv >= g->n && ldo >= g->m, "leading dimension too small");
     if (!g->weights_set) SLEMM_THROW(SLEMM_ERR_STATE, "set_weights must be called before operators");

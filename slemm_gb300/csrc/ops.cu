@@ -351,7 +351,7 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
                       const float* __restrict__ Q, int64_t ldq, int cq, const double* __restrict__ qparts,
                       int nblkq, int nq, const float* __restrict__ rr, int npieces, void* B,
                       double* __restrict__ red, int nblk, const double* __restrict__ mparts,
-                      double* __restrict__ xmax)
+                      double* __restrict__ xmax, const int32_t* __restrict__ inv)
 {
   __shared__ double sh[32];
   __shared__ float shf[32];
@@ -383,29 +383,47 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
   const float one[V] = {};
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
     float x[V] = {};
-    if (i < n) {
-      ldv<V>(in + (int64_t)c * ld + i, x);
-      if (proj) {
+    bool ok[V];
+    if (inv != nullptr) {
+      // trait view: packed position i + u holds view row inv[i + u], or no individual of the view
 #pragma unroll
-        for (int u = 0; u < V; ++u) x[u] = __fsub_rn(x[u], proj_dot(Q, ldq, cq, i + u, qt));
+      for (int u = 0; u < V; ++u) {
+        const int64_t rv = inv[i + u];
+        ok[u] = rv >= 0;
+        if (ok[u]) {
+          x[u] = in[(int64_t)c * ld + rv];
+          if (proj) x[u] = __fsub_rn(x[u], proj_dot(Q, ldq, cq, rv, qt));
+          if (rr) x[u] = __fmul_rn(x[u], rr[rv]);
+          if (!MEASURE) x[u] = __fsub_rn(x[u], mu);
+        }
       }
-      if (rr) {
-        float r[V];
-        ldv<V>(rr + i, r);
+    } else {
 #pragma unroll
-        for (int u = 0; u < V; ++u) x[u] = __fmul_rn(x[u], r[u]);
-      }
-      if (!MEASURE) {
+      for (int u = 0; u < V; ++u) ok[u] = i + u < n;
+      if (i < n) {
+        ldv<V>(in + (int64_t)c * ld + i, x);
+        if (proj) {
 #pragma unroll
-        for (int u = 0; u < V; ++u)
-          if (i + u < n) x[u] = __fsub_rn(x[u], mu);
+          for (int u = 0; u < V; ++u) x[u] = __fsub_rn(x[u], proj_dot(Q, ldq, cq, i + u, qt));
+        }
+        if (rr) {
+          float r[V];
+          ldv<V>(rr + i, r);
+#pragma unroll
+          for (int u = 0; u < V; ++u) x[u] = __fmul_rn(x[u], r[u]);
+        }
+        if (!MEASURE) {
+#pragma unroll
+          for (int u = 0; u < V; ++u)
+            if (ok[u]) x[u] = __fsub_rn(x[u], mu);
+        }
       }
     }
     if (MEASURE) {
 #pragma unroll
       for (int u = 0; u < V; ++u) {
         df_add(acc, x[u]);
-        if (i + u < n) {
+        if (ok[u]) {
           xhi = fmaxf(xhi, x[u]);
           nxlo = fmaxf(nxlo, -x[u]);
         }
@@ -602,7 +620,7 @@ __global__ void __launch_bounds__(kRedThreads)
 finalize_indiv_kernel(const float* __restrict__ D, int splits, int kp2, int64_t n_pad, int k,
                       int64_t n, const double* __restrict__ tparts, int nblkt, const float* __restrict__ rr,
                       const float* __restrict__ Vin, int64_t ld_v, float tau0, int nq, float* __restrict__ out,
-                      int64_t ldo, const double* __restrict__ xmax2)
+                      int64_t ldo, const double* __restrict__ xmax2, const int32_t* __restrict__ map)
 {
   __shared__ float sb[2];
   __shared__ float sisc;
@@ -615,7 +633,16 @@ finalize_indiv_kernel(const float* __restrict__ D, int splits, int kp2, int64_t 
   const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;
   if (i >= n) return;
   float val[V];
-  gather_D<V>(D, splits, kp2, n_pad, c, i, isc, val);
+  if (map != nullptr) {   // trait view: view row i + u is packed row map[i + u]
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      float t[1];
+      gather_D<1>(D, splits, kp2, n_pad, c, map[i + u], isc, t);
+      val[u] = t[0];
+    }
+  } else {
+    gather_D<V>(D, splits, kp2, n_pad, c, i, isc, val);
+  }
   float r[V], v[V];
   if (rr) ldv<V>(rr + i, r);
   const bool addv = Vin != nullptr && c >= nq;
@@ -860,6 +887,9 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   // H0 operators: the first nq columns are projected (H0_quadform_mv), the rest are not (H0_ldet_mv)
   const bool h0 = kind == SLEMM_OP_QUADFORM || kind == SLEMM_OP_LDET;
   const bool vin = vec4_ok(g->n, ld_in, in);
+  // a trait view reads its inputs and writes its outputs through its individual map
+  const int32_t* inv_ind = g->is_view ? g->ind_inv.as<int32_t>() : nullptr;
+  const int32_t* map_ind = g->is_view ? g->ind_map.as<int32_t>() : nullptr;
 
   if (dir1) {
     // ---- prologue 1: v_adj = rr∘(v − QQᵀv) (quadform), rr∘v (ldet), v (rmatvec) ----
@@ -875,31 +905,31 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
       if (vin)
         prologue_indiv_kernel<4, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, mu, nblk_n, nullptr,
-            x_max1);
+            x_max1, inv_ind);
       else
         prologue_indiv_kernel<1, true><<<dim3(nblk_n, k), kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, mu, nblk_n, nullptr,
-            x_max1);
+            x_max1, inv_ind);
       LAUNCH_CHECK();
     }
     if (f16) {
       if (vin)
         prologue_indiv_kernel<4, false, true><<<grid, kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
-            x_max1);
+            x_max1, inv_ind);
       else
         prologue_indiv_kernel<1, false, true><<<grid, kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
-            x_max1);
+            x_max1, inv_ind);
     } else {
       if (vin)
         prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
-            nullptr);
+            nullptr, inv_ind);
       else
         prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(
             in, ld_in, g->n, g->n_pad, k, p1.kp, Qp, g->n_pad, cq, qp, nblk_q, nq, rr, np1, B1, r_col, nblk_n, mu,
-            nullptr);
+            nullptr, inv_ind);
     }
     LAUNCH_CHECK();
     // ---- pass 1: Cntᵀ over individuals ----
@@ -968,11 +998,11 @@ static void op_group(slemm_geno* g, int kind, float tau0, const float* in, int64
   if (vec4_ok(g->n, ld_out, out) && (!v2 || vin)) {
     dim3 grid((unsigned)ceil_div(g->n, 4 * kRedThreads), k);
     finalize_indiv_kernel<4><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.kp, g->n_pad, k, g->n, r_t, nblk_m, rr2,
-                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2);
+                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2, map_ind);
   } else {
     dim3 grid((unsigned)ceil_div(g->n, kRedThreads), k);
     finalize_indiv_kernel<1><<<grid, kRedThreads, 0, st>>>(D, p2.splits, p2.kp, g->n_pad, k, g->n, r_t, nblk_m, rr2,
-                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2);
+                                                           v2, ld_in, tau0, nq2, out, ld_out, x_max2, map_ind);
   }
   LAUNCH_CHECK();
   // quadform columns 0 … nq−1: out = T + τ0 v − QQᵀT
@@ -1028,11 +1058,11 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
       if (v4)
         prologue_indiv_kernel<4, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, mu, nblk_n,
-            nullptr, x_rng);
+            nullptr, x_rng, nullptr);
       else
         prologue_indiv_kernel<1, true><<<dim3(nblk_n, kc), kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, mu, nblk_n,
-            nullptr, x_rng);
+            nullptr, x_rng, nullptr);
       LAUNCH_CHECK();
     }
     const dim3 grid(nblk_n, kc + pad);
@@ -1040,20 +1070,20 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
       if (v4)
         prologue_indiv_kernel<4, false, true><<<grid, kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-            x_rng);
+            x_rng, nullptr);
       else
         prologue_indiv_kernel<1, false, true><<<grid, kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-            x_rng);
+            x_rng, nullptr);
     } else {
       if (v4)
         prologue_indiv_kernel<4, false><<<grid, kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-            nullptr);
+            nullptr, nullptr);
       else
         prologue_indiv_kernel<1, false><<<grid, kRedThreads, 0, st>>>(
             in, ldu, g->n, g->n_pad, kc, p.kp, nullptr, 0, 0, nullptr, 1, 0, nullptr, pieces, B1, r_col, nblk_n, mu,
-            nullptr);
+            nullptr, nullptr);
     }
     LAUNCH_CHECK();
     run_gemm(g, p, A, rows, K_pad, B1, D, g->err.as<int>(), kc, 1);

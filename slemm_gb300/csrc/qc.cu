@@ -84,19 +84,21 @@ __global__ void marker_qc_kernel(const int64_t* __restrict__ pc, const int32_t* 
   hwep[j] = (float)hwe_exact_p(n1, n0, n2, midp);
 }
 
-// out[c·ld + i] = count of SNP rows[c] for kept individual i (i < n), from the G copy.
+// out[c·ld + i] = count of SNP rows[c] for kept individual i (i < n), from the G copy (at packed
+// position map[i] for a trait view, else i).
 __global__ void genotype_rows_kernel(const uint32_t* __restrict__ G, int64_t K_tiles, const int64_t* __restrict__ rows,
-                                     int64_t n, float* __restrict__ out, int64_t ld)
+                                     int64_t n, const int32_t* __restrict__ map, float* __restrict__ out, int64_t ld)
 {
   const int c = blockIdx.y;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int64_t iv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (iv >= n) return;
+  const int64_t i = map ? (int64_t)map[iv] : iv;
   const int64_t j = rows[c];
   const int64_t mt = j / 128, r = j % 128, kt = i / 64, e = i % 64;
   const uint32_t w = G[((mt * K_tiles + kt) * 128 + r) * 4 + e / 16];
   const int q = (int)(e % 16);
   const int sh = (q & 1) ? 16 + (q & ~1) : q;   // even element 2p at bits 2p, odd 2p+1 at 16+2p
-  out[(int64_t)c * ld + i] = (float)((w >> sh) & 3u);
+  out[(int64_t)c * ld + iv] = (float)((w >> sh) & 3u);
 }
 
 }  // namespace slemm
@@ -164,7 +166,8 @@ int slemm_gpu_genotype_rows(slemm_geno* g, const int64_t* rows, int cnt, float* 
       ldd = g->n;
     }
     genotype_rows_kernel<<<dim3((unsigned)ceil_div(g->n, 256), cnt), 256, 0, g->stream>>>(
-        g->G.as<uint32_t>(), g->n_pad / kTileK, d_rows.as<int64_t>(), g->n, dst, ldd);
+        g->G.as<uint32_t>(), g->n_pad / kTileK, d_rows.as<int64_t>(), g->n,
+        g->is_view ? g->ind_map.as<int32_t>() : nullptr, dst, ldd);
     LAUNCH_CHECK();
     if (mem == SLEMM_MEM_HOST)
       CUDA_TRY(cudaMemcpy2DAsync(out, ld * sizeof(float), dst, g->n * sizeof(float), g->n * sizeof(float), cnt,

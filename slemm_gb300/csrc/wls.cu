@@ -179,6 +179,9 @@ extern "C" int slemm_gpu_wls(slemm_geno* g, const float* rvec, const float* X, i
 {
   return guarded([&] {
     CHECK_ARG(g && X && y && snp_blup, "null argument");
+    if (g->is_view)
+      SLEMM_THROW(SLEMM_ERR_UNSUPPORTED, "slemm_gpu_wls reads the packed copies directly and is not available on a "
+                                         "trait view; create a handle with the keep list instead");
     const int64_t n = g->n, m = g->m;
     CHECK_ARG(c >= 1 && c <= SLEMM_MAX_COVARIATES && ldx >= n, "bad covariate matrix");
     cudaStream_t st = g->stream;
