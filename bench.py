@@ -56,9 +56,10 @@ CONFIGS = {
                  "SNP weights in (0, 2] (windows of 50 SNPs), 64 Rademacher probes"),
     5: dict(n=1000000, m=50000, probes=64, h2=0.4, missing=0.0, traits=16, miss_lo=0.05, miss_hi=0.40,
             gwas_m=200000,
-            name="n=1000000 m=50000, 16 traits with 5-40% of individuals missing per trait (one handle per trait "
-                 "packed from the .bed rows held in HBM), DF-REML + BLUP with 64 probes each; GWAS score terms "
-                 "over a 1000000 x 200000 .bed for the first trait's individuals"),
+            name="n=1000000 m=50000, 16 traits with 5-40% of individuals missing per trait (the .bed rows held "
+                 "in HBM packed once per step, each trait a view of its individuals over the shared packed copies), "
+                 "DF-REML + BLUP with 64 probes each; GWAS score terms over a 1000000 x 200000 .bed for the first "
+                 "trait's individuals"),
 }
 
 
@@ -841,10 +842,10 @@ def _mem_available_gb():
 
 def run_multi(args, cfg):
     """Multi-trait workload: one step = DF-REML + BLUP for every trait on its own individuals —
-    each trait's handle packed (both tiled copies, per-SNP counts of its individuals) from the
-    .bed rows held in HBM, as the reference analyses each trait on its own individual set — then
-    the GWAS score terms of the first trait over a 10⁶-row, 2·10⁵-SNP .bed (resident handle of
-    that trait's individuals)."""
+    the .bed rows held in HBM packed once (both tiled copies), every trait a view of its
+    individuals over those copies (its own counts, frequencies, centring and fit, as the reference
+    analyses each trait on its own individual set) — then the GWAS score terms of the first trait
+    over a 10⁶-row, 2·10⁵-SNP .bed (resident handle of that trait's individuals)."""
     import torch
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -883,11 +884,14 @@ def run_multi(args, cfg):
         return gh.score_terms(Py, mac=20)
 
     def step(rows, gwas_handle=None, gwas_rows=None):
+        """One pack of the .bed rows for all individuals, then every trait's fit on a view of it."""
         res = []
-        for t in range(T):
-            with api.Genotypes(rows, n, keep_idx=keeps[t]) as gt:
-                gt.set_precision(prec_code(args.prec))
-                res.append(gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes))
+        with api.Genotypes(rows, n) as parent:
+            for t in range(T):
+                with api.Genotypes.view(parent, keeps[t]) as gt:
+                    gt.set_precision(prec_code(args.prec))
+                    gt.set_autotune(not args.no_autotune)
+                    res.append(gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes))
         if gwas_handle is not None:
             sc = gwas(gwas_handle, res[0]["Py"])
         else:
@@ -925,24 +929,31 @@ def run_multi(args, cfg):
     mean_step = max_over_ranks(statistics.mean(times), dist)
     # per-phase split of one step: trait handles (pack), fits, GWAS score pass
     # (the first trait's fit also gives the packed-product launch shapes for the roofline)
-    ph = {"pack_s": 0.0, "fit_s": 0.0}
+    ph = {"pack_s": 0.0, "views_s": 0.0, "fit_s": 0.0}
     prof = None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    parent = api.Genotypes(rows_dev, n)
+    torch.cuda.synchronize()
+    ph["pack_s"] = time.perf_counter() - t0
     for t in range(T):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        gt = api.Genotypes(rows_dev, n, keep_idx=keeps[t])
+        gt = api.Genotypes.view(parent, keeps[t])
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         gt.set_precision(prec_code(args.prec))
+        gt.set_autotune(not args.no_autotune)
         if t == 0:
             _prof(gt, 1)
         gt.SLDF_REML(None, Xs[t], ys[t], persnp, seed=0, n_V=probes)
         torch.cuda.synchronize()
         if t == 0:
             prof = _prof(gt, 0)
-        ph["pack_s"] += t1 - t0
+        ph["views_s"] += t1 - t0
         ph["fit_s"] += time.perf_counter() - t1
         gt.close()
+    parent.close()
     roof, matvec_gbs = roofline(prof, int(keeps[0].size), m)
     t0 = time.perf_counter()
     gwas(gw, res[0]["Py"])
@@ -967,11 +978,11 @@ def run_multi(args, cfg):
         h2d = rows_host.numel() + sum(y.nbytes + x.nbytes for y, x in zip(ys, Xs)) + T * persnp.nbytes
         if keep_gw_host is not None:
             h2d += keep_gw_host.nbytes
-            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, every trait's handle "
-                        "packed from them in HBM; the GWAS .bed uploaded from host memory through genotype_create")
+            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, packed once in HBM, every trait "
+                        "a view of its individuals; the GWAS .bed uploaded from host memory through genotype_create")
         else:
-            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, every trait's handle "
-                        "packed from them in HBM; the GWAS handle stays resident (too little free host memory "
+            e2e_note = ("the REML .bed rows uploaded from pinned host memory once per step, packed once in HBM, every trait "
+                        "a view of its individuals; the GWAS handle stays resident (too little free host memory "
                         "for a host copy of its 50 GB of rows)")
         del rows_host
     d2h = sum((k.size + m + 1 + 1) * 4 for k in keeps) + 2 * 4 * m2
