@@ -1,8 +1,9 @@
-"""Builds libslemm_gb300.so in-tree for sm_103a.
+"""Builds libslemm_gb300.so in-tree for sm_103a, and the `slemm` command line over it.
 
 Every translation unit under csrc/ is compiled by nvcc in parallel into _build/, then linked
-into lib/libslemm_gb300.so.  Incremental: a unit is rebuilt only when it or a header is newer
-than its object.
+into lib/libslemm_gb300.so.  cli/slemm.cpp (host C++ only) is compiled by the host C++ compiler
+into bin/slemm, linked against the library with an rpath to it.  Incremental: a unit is rebuilt
+only when it or a header is newer than its output.
 """
 from __future__ import annotations
 
@@ -18,6 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libslemm_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "slemm.cpp")
+CLI = os.path.join(HERE, "bin", "slemm")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -72,7 +75,23 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """bin/slemm from cli/slemm.cpp, linked against lib/libslemm_gb300.so (rpath $ORIGIN/../lib)."""
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    if _stale(CLI, [CLI_SRC, LIB] + _headers()):
+        cxx = shutil.which("g++") or shutil.which("c++")
+        if not cxx:
+            raise RuntimeError("no host C++ compiler for the slemm command line")
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), CLI_SRC, "-o", CLI,
+               "-L" + os.path.dirname(LIB), "-lslemm_gb300", "-Wl,-rpath,$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"slemm command line failed to build:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":
