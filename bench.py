@@ -967,6 +967,7 @@ def run_multi(args, cfg):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             rows_up = rows_host.to("cuda", non_blocking=True)   # the .bed rows cross the link once
+            torch.cuda.current_stream().synchronize()           # landed before the library's stream reads them
             if keep_gw_host is not None:
                 step(rows_up, gwas_rows=keep_gw_host)
             else:
