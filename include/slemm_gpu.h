@@ -182,9 +182,9 @@ int slemm_gpu_rademacher(int seed, int64_t n, int n_V, float* V, int64_t ldv, in
 /* ---- batched tridiagonal eigensolve + SLQ (src/reml.cpp:440-451, 638-646) -------------- */
 /* For t Jacobi matrices (diag delta t×nld, off-diag beta t×(nld+1) with beta[:,1:nld] used),
  * returns eigenvalues D (t×nld, ascending per probe) and squared first eigenvector components W2
- * (t×nld), FP64, computed on the GPU (one thread per probe runs an FP64 implicit QL; the DF-REML
- * driver keeps them on the device and sums the SLQ log-determinant there for every criterion
- * evaluation).  Host pointers, column-major. */
+ * (t×nld), FP64, computed on the host: an implicit QL per probe, the probes spread over the host's
+ * threads (a serial chain of FP64 rotations, which GB300's low FP64 rate makes ~100× slower on the
+ * GPU).  Host pointers, column-major. */
 int slemm_gpu_tridiag_eig(const double* delta, const double* beta, int t, int nld, double* D,
                           double* W2);
 

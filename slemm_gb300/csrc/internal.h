@@ -111,13 +111,9 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
                                  int p_freq, int nq = 0);
 // Solve for the columns of group `grp`; X has that group's columns (ld = ldx) on device.
 int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, int64_t ldx, int grp);
-// Batched tridiagonal eigensolve on the device (one thread per probe, FP64 implicit QL): delta
-// nld×t and beta (nld+1)×t in, D and W2 nld×t out, eigenvalues ascending per probe; synchronises.
-void tridiag_eig_device(const double* d_delta, const double* d_beta, int t, int nld, double* d_D, double* d_W2,
-                        cudaStream_t st);
-// SLQ log-determinant scale·Σ W2·log(D + σ) over cnt nodes on the device; synchronises and returns it.
-double slq_ldet_device(const double* d_D, const double* d_W2, int cnt, double sigma, double scale, double* d_out,
-                       cudaStream_t st);
+// Batched tridiagonal eigensolve on the host (FP64 implicit QL per probe over host threads): delta
+// nld×t and beta (nld+1)×t in, D and W2 nld×t out, eigenvalues ascending per probe.
+void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2);
 // L_Solve coefficients of group grp at shift σ (X = Σ_i coef[i·tc+c]·V_i[:,c], V_0 = B, V_i = U_i).
 int solve_coeffs(const slemm_lseed* S, double sigma, double tol, int grp, std::vector<double>& coef);
 // Inner products B[:,a]ᵀV_i[:,b] for i = 0 … J and each (a, b) pair (V_0 = B), host result

@@ -22,6 +22,7 @@
 #include "reduce.cuh"
 
 #include <chrono>
+#include <thread>
 
 struct slemm_lseed {
   slemm_geno* g = nullptr;
@@ -661,7 +662,20 @@ int lanczos_solve_device(slemm_lseed* S, double sigma, double tol, float* dX, in
 // (diagonal d[0 … nld−1], off-diagonal e[0 … nld−2], both overwritten): implicit QL with
 // Wilkinson shifts in FP64, tracking only the first row z of the eigenvector matrix (all the
 // Gauss quadrature needs).  Returns false if a sweep limit is hit.
-__device__ bool tridiag_ql(double* d, double* e, double* z, int nld)
+//
+// It runs on the Grace host: the QL is a serial chain of FP64 rotations (a square root and a
+// division each), and GB300 executes FP64 at a small fraction of its FP32 rate — one thread per
+// probe on the GPU took 330 ms for 64 probes of 330 steps (9 % of the window-weighted fit in the
+// launch list), the host threads a few milliseconds.
+// √(a² + b²) without hypot's overflow handling (a tenth of its cost), falling back to it when the
+// squares leave the FP64 range.
+static inline double fast_hypot(double a, double b)
+{
+  const double r = std::sqrt(a * a + b * b);
+  return (std::isfinite(r) && (r > 0.0 || (a == 0.0 && b == 0.0))) ? r : std::hypot(a, b);
+}
+
+static bool tridiag_ql(double* d, double* e, double* z, int nld)
 {
   for (int i = 0; i < nld; ++i) z[i] = (i == 0) ? 1.0 : 0.0;
   if (nld > 0) e[nld - 1] = 0.0;
@@ -670,19 +684,19 @@ __device__ bool tridiag_ql(double* d, double* e, double* z, int nld)
     for (int iter = 0;; ++iter) {
       int mm = l;
       for (; mm < nld - 1; ++mm) {
-        const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
-        if (fabs(e[mm]) <= eps * dd) break;
+        const double dd = std::fabs(d[mm]) + std::fabs(d[mm + 1]);
+        if (std::fabs(e[mm]) <= eps * dd) break;
       }
       if (mm == l) break;
       if (iter >= 64) return false;
       double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-      double r = hypot(g, 1.0);
+      double r = fast_hypot(g, 1.0);
       g = d[mm] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
       double s = 1.0, c = 1.0, pp = 0.0;
       bool deflated = false;
       for (int i = mm - 1; i >= l; --i) {
         const double f = s * e[i], b = c * e[i];
-        r = hypot(f, g);
+        r = fast_hypot(f, g);
         e[i + 1] = r;
         if (r == 0.0) {
           d[i + 1] -= pp;
@@ -710,85 +724,44 @@ __device__ bool tridiag_ql(double* d, double* e, double* z, int nld)
   return true;
 }
 
-// Batched tridiagonal eigensolve on the device, one thread per probe p < t: the Jacobi matrix of
-// probe p (delta[i·t + p], off-diagonal beta[(i+1)·t + p]) is solved in its own slice of `work`
-// (3·nld doubles), then its eigenvalues are sorted ascending (insertion sort, carrying z²) into
-// D[i·t + p], W2[i·t + p].  A QL that hits its sweep limit sets *status.
-__global__ void tridiag_eig_kernel(const double* __restrict__ delta, const double* __restrict__ beta, int t, int nld,
-                                   double* __restrict__ work, double* __restrict__ D, double* __restrict__ W2,
-                                   int* __restrict__ status)
-{
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= t) return;
-  double* d = work + (size_t)p * 3 * nld;
-  double* e = d + nld;
-  double* z = e + nld;
-  for (int i = 0; i < nld; ++i) {
-    d[i] = delta[(size_t)i * t + p];
-    e[i] = (i + 1 < nld) ? beta[(size_t)(i + 1) * t + p] : 0.0;
-  }
-  if (!tridiag_ql(d, e, z, nld)) {
-    atomicOr(status, 1);
-    return;
-  }
-  for (int i = 0; i < nld; ++i) z[i] *= z[i];
-  for (int i = 1; i < nld; ++i) {   // ascending by eigenvalue
-    const double dv = d[i], zv = z[i];
-    int j = i - 1;
-    while (j >= 0 && d[j] > dv) {
-      d[j + 1] = d[j];
-      z[j + 1] = z[j];
-      --j;
-    }
-    d[j + 1] = dv;
-    z[j + 1] = zv;
-  }
-  for (int i = 0; i < nld; ++i) {
-    D[(size_t)i * t + p] = d[i];
-    W2[(size_t)i * t + p] = z[i];
-  }
-}
-
-// SLQ log-determinant (src/reml.cpp:440-451): out = scale·Σ_q W2_q·log(D_q + σ) over cnt nodes,
-// one block, per-thread strided sums then a fixed-order block sum (bit-reproducible).
-__global__ void __launch_bounds__(256)
-slq_ldet_kernel(const double* __restrict__ D, const double* __restrict__ W2, int cnt, double sigma, double scale,
-                double* __restrict__ out)
-{
-  __shared__ double sh[32];
-  double a = 0.0;
-  for (int q = threadIdx.x; q < cnt; q += blockDim.x) a += W2[q] * log(D[q] + sigma);
-  a = block_sum_d(a, sh);
-  if (threadIdx.x == 0) *out = a * scale;
-}
-
-void tridiag_eig_device(const double* d_delta, const double* d_beta, int t, int nld, double* d_D, double* d_W2,
-                        cudaStream_t st)
+// Batched tridiagonal eigensolve (host in/out, FP64).  delta is nld×t (row i = step i), beta
+// (nld+1)×t; D and W2 are nld×t with eigenvalues ascending per probe.  The probes are independent
+// and are spread over the host's hardware threads; each probe's result does not depend on which
+// thread solves it.
+void tridiag_eig_host(const double* delta, const double* beta, int t, int nld, double* D, double* W2)
 {
   if (t <= 0 || nld <= 0) return;
-  DevBuf work(st), stat(st);
-  work.ensure((size_t)t * 3 * nld * sizeof(double));
-  int* d_stat = (int*)stat.ensure(sizeof(int));
-  CUDA_TRY(cudaMemsetAsync(d_stat, 0, sizeof(int), st));
-  tridiag_eig_kernel<<<(unsigned)ceil_div(t, 64), 64, 0, st>>>(d_delta, d_beta, t, nld, work.as<double>(), d_D, d_W2,
-                                                                 d_stat);
-  LAUNCH_CHECK();
-  int h = 0;
-  CUDA_TRY(cudaMemcpyAsync(&h, d_stat, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaStreamSynchronize(st));
-  if (h) SLEMM_THROW(SLEMM_ERR_NUMERIC, "tridiagonal QL did not converge in 64 sweeps");
+  std::atomic<int> next{0}, failed{0};
+  auto worker = [&] {
+    std::vector<double> d(nld), e(nld), z(nld);
+    std::vector<int> idx(nld);
+    for (int p = next.fetch_add(1); p < t; p = next.fetch_add(1)) {
+      for (int i = 0; i < nld; ++i) {
+        d[i] = delta[(size_t)i * t + p];
+        e[i] = (i + 1 < nld) ? beta[(size_t)(i + 1) * t + p] : 0.0;
+      }
+      if (!tridiag_ql(d.data(), e.data(), z.data(), nld)) {
+        failed = 1;
+        continue;
+      }
+      for (int i = 0; i < nld; ++i) idx[i] = i;
+      std::sort(idx.begin(), idx.end(), [&](int a, int b) { return d[a] < d[b]; });
+      for (int i = 0; i < nld; ++i) {
+        D[(size_t)i * t + p] = d[idx[i]];
+        W2[(size_t)i * t + p] = z[idx[i]] * z[idx[i]];
+      }
+    }
+  };
+  // a few hundred thousand rotations per probe at a few hundred steps: threads pay off there
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nth = (nld >= 64) ? std::min(t, hw) : 1;
+  std::vector<std::thread> pool;
+  for (int q = 1; q < nth; ++q) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+  if (failed) SLEMM_THROW(SLEMM_ERR_NUMERIC, "tridiagonal QL did not converge in 64 sweeps");
 }
 
-double slq_ldet_device(const double* d_D, const double* d_W2, int cnt, double sigma, double scale, double* d_out,
-                       cudaStream_t st)
-{
-  slq_ldet_kernel<<<1, 256, 0, st>>>(d_D, d_W2, cnt, sigma, scale, d_out);
-  LAUNCH_CHECK();
-  double h = 0.0;
-  CUDA_TRY(cudaMemcpyAsync(&h, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaStreamSynchronize(st));
-  return h;
-}
 
 }  // namespace slemm
 
@@ -863,16 +836,7 @@ int slemm_gpu_tridiag_eig(const double* delta, const double* beta, int t, int nl
   return guarded([&] {
     CHECK_ARG(delta && beta && D && W2, "null argument");
     CHECK_ARG(t >= 1 && nld >= 1, "empty problem");
-    cudaStream_t st = nullptr;
-    DevBuf buf(st);
-    double* p = (double*)buf.ensure((size_t)t * (4 * nld + 1) * sizeof(double));
-    double *d_delta = p, *d_beta = p + (size_t)t * nld, *d_D = d_beta + (size_t)t * (nld + 1), *d_W2 = d_D + (size_t)t * nld;
-    CUDA_TRY(cudaMemcpyAsync(d_delta, delta, (size_t)t * nld * sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_beta, beta, (size_t)t * (nld + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-    tridiag_eig_device(d_delta, d_beta, t, nld, d_D, d_W2, st);
-    CUDA_TRY(cudaMemcpyAsync(D, d_D, (size_t)t * nld * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(W2, d_W2, (size_t)t * nld * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    tridiag_eig_host(delta, beta, t, nld, D, W2);
   });
 }
 

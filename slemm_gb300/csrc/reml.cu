@@ -372,14 +372,9 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     for (int j = 0; j <= nld; ++j)
       for (int p = 0; p < n_V; ++p) bt[(size_t)j * n_V + p] = B[(size_t)j * tQV + 1 + c + p];
   }
-  // Eigenvalues and quadrature weights on the device in FP64; they stay there for the SLQ sums.
-  DevBuf d_slq(g->stream);
-  double* slq = (double*)d_slq.ensure(((size_t)n_V * (4 * nld + 1) + 1) * sizeof(double));
-  double *d_dl = slq, *d_bt = slq + (size_t)n_V * nld, *d_DV = d_bt + (size_t)n_V * (nld + 1);
-  double *d_W2 = d_DV + (size_t)n_V * nld, *d_ldet = d_W2 + (size_t)n_V * nld;
-  CUDA_TRY(cudaMemcpyAsync(d_dl, dl.data(), dl.size() * sizeof(double), cudaMemcpyHostToDevice, g->stream));
-  CUDA_TRY(cudaMemcpyAsync(d_bt, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice, g->stream));
-  tridiag_eig_device(d_dl, d_bt, n_V, nld, d_DV, d_W2, g->stream);
+  // Gauss quadrature nodes and weights of every probe (FP64, host threads)
+  std::vector<double> DV((size_t)n_V * nld), W2((size_t)n_V * nld);
+  tridiag_eig_host(dl.data(), bt.data(), n_V, nld, DV.data(), W2.data());
 
   // Moments of the stored basis: every shifted solve the criterion needs is a combination
   // X = Σ_i coef_i·V_i of the seed vectors (V_0 = the right-hand side), so yᵀX and QᵀX follow
@@ -408,8 +403,9 @@ void reml_sldf(slemm_geno* g, const float* rvec, const float* X, int64_t ldx, in
     Criterion r;
     r.vg = yPy / (double)(n - c);
     r.ve = r.vg * tau;
-    const double ldet_H = slq_ldet_device(d_DV, d_W2, n_V * nld, (double)sigma, (double)n / (double)n_V, d_ldet,
-                                          g->stream);   // SLQ_LDet (src/reml.cpp:440-451)
+    double ldet_H = 0.0;   // SLQ_LDet (src/reml.cpp:440-451)
+    for (size_t q = 0; q < DV.size(); ++q) ldet_H += W2[q] * std::log(DV[q] + sigma);
+    ldet_H = ldet_H * (double)n / (double)n_V;
     r.lrt = (double)n * std::log(ySy / yPy) - ldet_H;
     const int sq = solve_coeffs(seed, (double)sigma, 1e-6, GQ, cq);
     std::vector<double> M((size_t)c * c, 0.0);   // M[k][l] = Q_kᵀ X_l, row-major
