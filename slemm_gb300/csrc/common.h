@@ -82,14 +82,17 @@ __host__ __device__ inline int64_t ceil_div(int64_t x, int64_t a) { return (x + 
 // Plain buffers use cudaMalloc/cudaFree.  A buffer bound to a stream (DevBuf(stream)) is
 // allocated and freed stream-ordered from the device's default memory pool, whose release
 // threshold configure_pool raises so that freed blocks stay cached for the next fit: such
-// allocations cost no device synchronisation.  A stream-bound buffer must be released before its
-// stream is destroyed.
+// allocations cost no device synchronisation.  Buffers that set `pool` draw from that pool
+// instead (the packed copies and the Lanczos basis have their own, so that each reuses its own
+// freed blocks instead of competing with every other allocation for the default pool's).  A
+// stream-bound buffer must be released before its stream is destroyed.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   bool ordered = false;
   bool owned = true;   // false: p aliases another buffer (a trait view's packed copies), never freed here
+  cudaMemPool_t pool = nullptr;   // stream-ordered from this pool instead of the default one
   DevBuf() = default;
   explicit DevBuf(cudaStream_t s) : stream(s), ordered(true) {}
   DevBuf(const DevBuf&) = delete;
@@ -119,7 +122,9 @@ struct DevBuf {
     if (nbytes <= bytes) return p;
     release();
     if (nbytes == 0) return nullptr;
-    cudaError_t e = ordered ? cudaMallocAsync(&p, nbytes, stream) : cudaMalloc(&p, nbytes);
+    cudaError_t e = !ordered ? cudaMalloc(&p, nbytes)
+                    : pool ? cudaMallocFromPoolAsync(&p, nbytes, pool, stream)
+                           : cudaMallocAsync(&p, nbytes, stream);
     if (e != cudaSuccess) {
       p = nullptr;
       throw Error{SLEMM_ERR_NOMEM, std::string(ordered ? "cudaMallocAsync(" : "cudaMalloc(") +
@@ -164,6 +169,10 @@ struct HostScal {
 
 // Keeps freed stream-ordered blocks of the device's default pool cached (idempotent).
 void configure_pool(int device);
+// The device's pools for the packed genotype copies and for the Lanczos basis (created on first
+// use, freed blocks kept cached like the default pool's).
+enum class Pool { Packed = 0, Basis = 1 };
+cudaMemPool_t own_pool(int device, Pool which);
 
 // ---- packed product plan ------------------------------------------------------------------------
 // D[M_pad × N] = Cnt[M_pad × K_pad] · B where the count matrix is a tiled 2-bit packed array

@@ -15,6 +15,8 @@
 // bulk copy per tile.  Padding rows/columns hold count 0.
 #include "internal.h"
 
+#include <map>
+
 #include <cstring>
 #include <mutex>
 
@@ -35,6 +37,26 @@ void configure_pool(int device)
   uint64_t keep = UINT64_MAX;   // this process's pool only: freed blocks stay cached for reuse
   CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
   done.push_back(device);
+}
+
+cudaMemPool_t own_pool(int device, Pool which)
+{
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(device, (int)which);
+  auto it = pools.find(key);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool;
+  CUDA_TRY(cudaMemPoolCreate(&pool, &props));
+  uint64_t keep = UINT64_MAX;   // freed blocks stay cached for the next handle or fit
+  CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  pools[key] = pool;
+  return pool;
 }
 
 int num_sms()
@@ -397,6 +419,7 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
       const int64_t Kt_G = g->n_pad / kTileK, Kt_GT = g->m_pad / kTileK;
       const size_t bytes_G = (size_t)(g->m_pad / kTileM) * Kt_G * kTileBytes;
       const size_t bytes_GT = (size_t)(g->n_pad / kTileM) * Kt_GT * kTileBytes;
+      g->G.pool = g->GT.pool = own_pool(g->device, Pool::Packed);
       g->G.ensure(bytes_G);
       g->GT.ensure(bytes_GT);
       g->err.ensure(sizeof(int));

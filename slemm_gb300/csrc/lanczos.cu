@@ -57,6 +57,7 @@ struct slemm_lseed {
     const int c = j / kChunk;
     while ((int)chunks.size() <= c) {
       auto* b = new slemm::DevBuf(st);
+      b->pool = slemm::own_pool(g->device, slemm::Pool::Basis);
       b->ensure((size_t)kChunk * n * t * sizeof(float));
       chunks.push_back(b);
     }
@@ -99,7 +100,7 @@ lz_dot_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur, const flo
   __shared__ float sb[2];
   const int c = blockIdx.y;
   float bh = 0.f, bl = 0.f;
-  if (Uprev) block_scalar([&] { return sqrt(sum_partials(nrm_prev + (int64_t)c * nblk, nblk)); }, sb, bh, bl);
+  if (Uprev) block_scalar([&] { return sqrt(warp_sum_partials(nrm_prev + (int64_t)c * nblk, nblk)); }, sb, bh, bl);
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
   DF acc;
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
@@ -131,7 +132,7 @@ lz_orth_kernel(float* __restrict__ tmp, const float* __restrict__ Ucur, const do
   __shared__ float sb[2];
   const int c = blockIdx.y;
   float dh, dlo;
-  block_scalar([&] { return sum_partials(dot + (int64_t)c * nblk, nblk); }, sb, dh, dlo);
+  block_scalar([&] { return warp_sum_partials(dot + (int64_t)c * nblk, nblk); }, sb, dh, dlo);
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
   DF acc;
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {
@@ -160,7 +161,7 @@ lz_scale_kernel(float* __restrict__ Unext, const float* __restrict__ src, const 
   __shared__ float sb[2];
   const int c = blockIdx.y;
   float ih, il;
-  block_scalar([&] { return 1.0 / sqrt(sum_partials(nrm + (int64_t)c * nblk, nblk)); }, sb, ih, il);
+  block_scalar([&] { return 1.0 / sqrt(warp_sum_partials(nrm + (int64_t)c * nblk, nblk)); }, sb, ih, il);
   const int64_t i0 = (int64_t)blockIdx.x * kLzRows, i1 = min64(n, i0 + kLzRows);
   DF acc;
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kLzThreads * V) {

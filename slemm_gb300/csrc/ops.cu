@@ -73,14 +73,18 @@ proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __res
   if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.x] = s;
 }
 
-// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ SLEMM_MAX_COVARIATES
-// (≤ the block's threads), as hi+lo FP32 pairs
+// qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ SLEMM_MAX_COVARIATES,
+// as hi+lo FP32 pairs; warp w of the block reduces the covariates l ≡ w (mod warps).
 __device__ __forceinline__ void load_qt(const double* __restrict__ parts, int nblk, int cq, int k, int c, float2* qt)
 {
-  if ((int)threadIdx.x < cq) {
-    float h, l;
-    split_double(sum_partials(parts + (int64_t)(threadIdx.x * k + c) * nblk, nblk), h, l);
-    qt[threadIdx.x] = make_float2(h, l);
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int l = warp; l < cq; l += nw) {
+    const double v = warp_sum_partials(parts + (int64_t)(l * k + c) * nblk, nblk);
+    if ((threadIdx.x & 31) == 0) {
+      float h, lo;
+      split_double(v, h, lo);
+      qt[l] = make_float2(h, lo);
+    }
   }
   __syncthreads();
 }
@@ -223,12 +227,10 @@ __device__ __forceinline__ int f16_exp(double bound)
   return max(-120, min(120, 11 - E));     // bound·2^e ∈ [2^10, 2^11)
 }
 
-// max_b parts[c·nblk + b]
+// max_b parts[c·nblk + b] by the 32 lanes of the calling warp (0 for no partials)
 __device__ __forceinline__ double max_partials(const double* __restrict__ parts, int nblk, int c)
 {
-  double v = 0.0;
-  for (int b = 0; b < nblk; ++b) v = fmax(v, parts[(int64_t)c * nblk + b]);
-  return v;
+  return warp_max_partials(parts + (int64_t)c * nblk, nblk);
 }
 
 // Block maximum of one float per thread (valid in thread 0; −∞ when every thread holds −∞);
@@ -252,11 +254,9 @@ __device__ __forceinline__ float block_max_f(float v, float* sh)
 // the resolution of its spread.  The prologue and the finalize take the same e from this.
 __device__ __forceinline__ int f16_col_exp(const double* __restrict__ range, int nblk, int c, float mu)
 {
-  double hi = -INFINITY, nlo = -INFINITY;
-  for (int b = 0; b < nblk; ++b) {
-    hi = fmax(hi, range[((int64_t)c * nblk + b) * 2]);
-    nlo = fmax(nlo, range[((int64_t)c * nblk + b) * 2 + 1]);
-  }
+  // by the 32 lanes of the calling warp
+  const double hi = warp_max_partials(range + (int64_t)c * nblk * 2, nblk, 2, -INFINITY);
+  const double nlo = warp_max_partials(range + (int64_t)c * nblk * 2 + 1, nblk, 2, -INFINITY);
   return f16_exp(fmax(hi - (double)mu, nlo + (double)mu));
 }
 
@@ -339,7 +339,7 @@ __device__ __forceinline__ void zero_pad_row(void* Bv, int64_t K_pad, int row, i
 // Otherwise, with mparts (those sums), x − μ_c is stored, μ_c = (float)(Σ/n) as in column_mean.
 __device__ __forceinline__ float column_mean(const double* __restrict__ mparts, int nblk, int c, double inv_n)
 {
-  return (float)(sum_partials(mparts + (int64_t)c * nblk, nblk) * inv_n);
+  return (float)(warp_sum_partials(mparts + (int64_t)c * nblk, nblk) * inv_n);   // by a whole warp
 }
 
 // F16: the operand is stored as FP16 pieces of (x − μ)·2^e, e from the MEASURE pass's signed
@@ -366,10 +366,11 @@ prologue_indiv_kernel(const float* __restrict__ in, int64_t ld, int64_t n, int64
   const bool proj = qparts != nullptr && c < nq;
   if (proj) load_qt(qparts, nblkq, cq, nq, c, qt);
   if (!MEASURE && (mparts != nullptr || F16)) {
-    if (threadIdx.x == 0) {
-      smu = mparts != nullptr ? column_mean(mparts, nblk, c, 1.0 / (double)n) : 0.f;
-      if (F16) {
-        const int e = f16_col_exp(xmax, nblk, c, smu);
+    if (threadIdx.x < 32) {   // warp 0 reduces the column's partials
+      const float mu_ = mparts != nullptr ? column_mean(mparts, nblk, c, 1.0 / (double)n) : 0.f;
+      const int e = F16 ? f16_col_exp(xmax, nblk, c, mu_) : 0;
+      if (threadIdx.x == 0) {
+        smu = mu_;
         ssc[0] = ldexpf(1.f, e);
         ssc[1] = ldexpf(1.f, -e);
       }
@@ -488,10 +489,14 @@ finalize_snp_kernel(const float* __restrict__ D, int splits, int kp1, int64_t m_
     return;
   }
   float ch, cl;
-  block_scalar([&] { return sum_partials(cparts + (int64_t)c * nblkc, nblkc); }, sb, ch, cl);
-  if (threadIdx.x == 0) {   // the mean the prologue removed, added back as μ·(pc_j − n·gm_j)
-    smu = mparts != nullptr ? column_mean(mparts, nblkc, c, 1.0 / (double)n_rows) : 0.f;
-    sisc = xmax1 != nullptr ? ldexpf(1.f, -f16_col_exp(xmax1, nblkc, c, smu)) : 1.f;
+  block_scalar([&] { return warp_sum_partials(cparts + (int64_t)c * nblkc, nblkc); }, sb, ch, cl);
+  if (threadIdx.x < 32) {   // the mean the prologue removed, added back as μ·(pc_j − n·gm_j)
+    const float mu_ = mparts != nullptr ? column_mean(mparts, nblkc, c, 1.0 / (double)n_rows) : 0.f;
+    const float isc_ = xmax1 != nullptr ? ldexpf(1.f, -f16_col_exp(xmax1, nblkc, c, mu_)) : 1.f;
+    if (threadIdx.x == 0) {
+      smu = mu_;
+      sisc = isc_;
+    }
   }
   __syncthreads();
   const float mu = mparts != nullptr ? smu : 0.f;
@@ -546,10 +551,12 @@ convert_snp_kernel(const float* __restrict__ V2, int64_t m_pad, int k, int kp2, 
   __shared__ float ssc[2];
   const int c = blockIdx.y;
   const int64_t j0 = (int64_t)blockIdx.x * kRowsPerBlock, j1 = min64(m_pad, j0 + kRowsPerBlock);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
     const int e = f16_exp(max_partials(xmax2, nblk, c));
-    ssc[0] = ldexpf(1.f, e);
-    ssc[1] = ldexpf(1.f, -e);
+    if (threadIdx.x == 0) {
+      ssc[0] = ldexpf(1.f, e);
+      ssc[1] = ldexpf(1.f, -e);
+    }
   }
   __syncthreads();
   DF acc;
@@ -582,10 +589,12 @@ prologue_snp_kernel(const float* __restrict__ in, int64_t ld, int64_t m, int64_t
     return;
   }
   if (F16 && !MEASURE) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
       const int e = f16_exp(max_partials(xmax, nblk, c));
-      ssc[0] = ldexpf(1.f, e);
-      ssc[1] = ldexpf(1.f, -e);
+      if (threadIdx.x == 0) {
+        ssc[0] = ldexpf(1.f, e);
+        ssc[1] = ldexpf(1.f, -e);
+      }
     }
     __syncthreads();
   }
@@ -626,8 +635,11 @@ finalize_indiv_kernel(const float* __restrict__ D, int splits, int kp2, int64_t 
   __shared__ float sisc;
   const int c = blockIdx.y;
   float th, tl;
-  block_scalar([&] { return sum_partials(tparts + (int64_t)c * nblkt, nblkt); }, sb, th, tl);
-  if (threadIdx.x == 0) sisc = xmax2 != nullptr ? ldexpf(1.f, -f16_exp(max_partials(xmax2, nblkt, c))) : 1.f;
+  block_scalar([&] { return warp_sum_partials(tparts + (int64_t)c * nblkt, nblkt); }, sb, th, tl);
+  if (threadIdx.x < 32) {
+    const float isc_ = xmax2 != nullptr ? ldexpf(1.f, -f16_exp(max_partials(xmax2, nblkt, c))) : 1.f;
+    if (threadIdx.x == 0) sisc = isc_;
+  }
   __syncthreads();
   const float isc = sisc;
   const int64_t i = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * V;

@@ -7,8 +7,9 @@
 // accumulator — while FP64 is used only once per thread and per block.  The explicit _rn
 // intrinsics keep the compiler from contracting the error-free transformations into FMAs.
 //
-// Partials are written per block and summed in a fixed order (sum_partials), by the consumer
-// kernels and by the final reduce alike, so every reader sees the same bits run to run.
+// Partials are written per block and summed in one fixed order — by a warp in the consumer
+// kernels' preambles (warp_sum_partials) and by one thread in the final reductions
+// (sum_partials), with the same arithmetic — so every reader sees the same bits run to run.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -61,12 +62,46 @@ __device__ __forceinline__ double block_sum_d(double v, double* sh)
   return r;
 }
 
-// Σ_b part[b] for b = 0 … nblk−1, in that order.
+// The fixed order of a sum of block partials: lane l of a warp adds part[b] for b ≡ l (mod 32) in
+// increasing b, then the 32 lane sums combine by a butterfly (v_l ← v_l + v_(l xor o) for
+// o = 16, 8, 4, 2, 1; floating-point addition is commutative, so every lane ends with the same
+// value).  A block's preamble reads its column's scalars this way with 32 lanes instead of one
+// thread walking a hundred partials.  All 32 lanes of the warp must call it.
+__device__ __forceinline__ double warp_sum_partials(const double* __restrict__ part, int nblk)
+{
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int b = lane; b < nblk; b += 32) s += part[b];
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// The same sum, the same bits, in one thread (the final reductions).
 __device__ __forceinline__ double sum_partials(const double* __restrict__ part, int nblk)
 {
-  double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += part[b];
-  return s;
+  double v[32];
+  for (int l = 0; l < 32; ++l) {
+    double s = 0.0;
+    for (int b = l; b < nblk; b += 32) s += part[b];
+    v[l] = s;
+  }
+  for (int o = 16; o; o >>= 1) {
+    double w[32];
+    for (int l = 0; l < 32; ++l) w[l] = v[l] + v[l ^ o];
+    for (int l = 0; l < 32; ++l) v[l] = w[l];
+  }
+  return v[0];
+}
+
+// max_b part[b·stride] over b < nblk (0 when nblk = 0), by the 32 lanes of a warp.
+__device__ __forceinline__ double warp_max_partials(const double* __restrict__ part, int nblk, int stride = 1,
+                                                    double init = 0.0)
+{
+  const int lane = threadIdx.x & 31;
+  double v = init;
+  for (int b = lane; b < nblk; b += 32) v = fmax(v, part[(int64_t)b * stride]);
+  for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
 }
 
 // V consecutive rows per thread and iteration (V = 4 needs 16-byte aligned addresses).
@@ -87,11 +122,15 @@ __device__ __forceinline__ void stv(float* p, const float (&v)[V])
   else *p = v[0];
 }
 
-// Thread 0 evaluates f() once per block and shares its double-float split.
+// Warp 0 evaluates f() once per block (f may use the warp-collective helpers above) and shares
+// its double-float split.
 template <class F>
 __device__ __forceinline__ void block_scalar(F&& f, float* sb, float& hi, float& lo)
 {
-  if (threadIdx.x == 0) split_double(f(), sb[0], sb[1]);
+  if (threadIdx.x < 32) {
+    const double v = f();
+    if (threadIdx.x == 0) split_double(v, sb[0], sb[1]);
+  }
   __syncthreads();
   hi = sb[0];
   lo = sb[1];
