@@ -577,7 +577,7 @@ def run_gpu(args, cfg):
         if fp32:
             reorth["dh2_vs_fp32"] = abs(rr_["h2"] - fp32["h2"])
     # ---- roofline of the dominant packed-product launch shape ----
-    roof, matvec_gbs = roofline(prof, n, m, sustained=min(times) > 1.0)
+    roof, matvec_gbs = roofline(prof, n, m, args.prec, sustained=min(times) > 1.0)
     # ---- CPU baseline (oracle port, this fit's step counts), rank 0, N = 1 only ----
     cpu = None
     counts = fit_counts(cfg, res)
@@ -647,7 +647,7 @@ def run_gpu(args, cfg):
         dist.destroy_process_group()
 
 
-def roofline(prof, n, m, sustained=False):
+def roofline(prof, n, m, prec, sustained=False):
     """Roofline object of the dominant packed-product launch shape (most device time in the
     timed region) and the packed bytes per second it streamed.  sustained: the launches run
     inside a fit of seconds, so the measured sustained BF16 figure is the peak (else the burst)."""
@@ -680,7 +680,7 @@ def roofline(prof, n, m, sustained=False):
         # ceiling of this kernel is the 16-bit peak over P
         "tc_peak_eff": tc_peak / dom["pieces"] if dom["tc"] else None,
         "frac_eff": ach_tf / (tc_peak / dom["pieces"]) if dom["tc"] else None,
-        "traffic": _traffic(dom, n, m),
+        "traffic": _traffic(dom, n, m, prec),
         "kernel": "gemm_tc_kernel" if dom["tc"] else "gemm_simt_kernel",
         "launch": {"N": dom["N"], "k": k, "pieces": dom["pieces"],
                    "direction": "Z^T U (M=SNPs)" if dom["dir"] == 1 else "Z V (M=individuals)",
@@ -787,7 +787,7 @@ def run_grad(args, cfg):
                              "d_sigma_e2": abs(rf["d_sigma_e2"] - r["d_sigma_e2"]) / abs(rf["d_sigma_e2"]),
                              "d_w_max_over_max": float(dw)}}
         g.set_precision(prec_code(args.prec))
-    roof, matvec_gbs = roofline(prof, n, m)
+    roof, matvec_gbs = roofline(prof, n, m, args.prec)
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         s_ldet, _, info = cpu_operator_sample(rows_np, n, m, probes, subsets=args.cpu_subsets)
@@ -971,7 +971,7 @@ def run_multi(args, cfg):
         ph["fit_s"] += time.perf_counter() - t1
         gt.close()
     parent.close()
-    roof, matvec_gbs = roofline(prof, int(keeps[0].size), m)
+    roof, matvec_gbs = roofline(prof, int(keeps[0].size), m, args.prec)
     t0 = time.perf_counter()
     gwas(gw, res[0]["Py"])
     torch.cuda.synchronize()
@@ -1079,30 +1079,35 @@ def _prof(g, enable):
     from slemm_gb300 import _lib
     lib = _lib.load()
     rows = ctypes.c_int(0)
-    info = (ctypes.c_int32 * (5 * 64))()
+    info = (ctypes.c_int32 * (7 * 64))()
     la = (ctypes.c_int64 * 64)()
     ms = (ctypes.c_double * 64)()
     _lib.check(lib.slemm_gpu_profile(g.h, enable, 64, ctypes.byref(rows), info, la, ms))
     out = []
     for r in range(min(rows.value, 64)):
-        out.append({"tc": info[5 * r], "N": info[5 * r + 1], "k": info[5 * r + 2],
-                    "pieces": info[5 * r + 3], "dir": info[5 * r + 4], "launches": int(la[r]),
-                    "ms": float(ms[r])})
+        out.append({"tc": info[7 * r], "N": info[7 * r + 1], "k": info[7 * r + 2],
+                    "pieces": info[7 * r + 3], "dir": info[7 * r + 4], "splits": info[7 * r + 5],
+                    "plan": info[7 * r + 6], "launches": int(la[r]), "ms": float(ms[r])})
     return out
 
 
-def _traffic(dom, n, m):
+def _traffic(dom, n, m, prec):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary (captured on a
-    small case and scaled to n = 100,000, m = 50,000), rescaled by the packed bytes when the
-    workload has another size (DRAM traffic grows with them: packed matrix once plus partials)."""
+    small case, n = 40,000, m = 20,000), carried to this launch: the reads (packed matrix once plus
+    the dense operand) grow with the packed bytes, the writes with the split-K partial bytes
+    (splits x kp x M_pad x 4, kp = k rounded up to 8, M_pad = m or n rounded up to 256)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
             t = json.load(f)
-        key = f"tc{dom['tc']}_N{dom['N']}_dir{dom['dir']}"
-        v = t.get(key)
-        return None if v is None else v * (m * ((n + 3) // 4)) / (50000 * 25000)
-    except Exception:
+        c = t.get(f"{prec}_tc{dom['tc']}_N{dom['N']}_dir{dom['dir']}")
+        if c is None or not dom.get("splits"):
+            return None
+        M_pad = -(-(m if dom["dir"] == 1 else n) // 256) * 256
+        partials = dom["splits"] * (-(-dom["k"] // 8) * 8) * M_pad * 4
+        packed = m * ((n + 3) // 4)
+        return c["read"] * packed / c["packed"] + c["write"] * partials / c["partials"]
+    except (OSError, ValueError, KeyError):
         return None
 
 

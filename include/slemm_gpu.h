@@ -336,24 +336,29 @@ int slemm_gpu_rmatvec_noalloc(slemm_geno* g, const float* v, int64_t ldv, int k,
 
 /* ---- split-K autotuner (no counterpart in the reference, whose subset size is a flag,
  * src/option.cpp:53-78) ------------------------------------------------------------------------- */
-/* on = 1: the handle's tensor-core passes pick their split-K count by timing, at the first pass of
- * each shape (device, N, pieces, K-tiles, padded rows), the fixed rule's count and up to five
- * counts near it that fill the last wave of CTAs well — one warm-up and two timed launches each,
- * CUDA events on the handle's stream — and keep the fastest when it beats the rule's by ≥ 3 %.
+/* on = 1: the handle's tensor-core passes pick their split-K count and ring plan by timing, at the
+ * first pass of each shape (device, N, pieces, K-tiles, padded rows), the fixed rule's count and
+ * up to five counts near it that fill the last wave of CTAs well — and, for N ≤ 64, the plan with
+ * one 128-row tile per CTA and two CTAs per SM at up to three counts — one warm-up and two timed
+ * launches each, CUDA events on the handle's stream — and keep the fastest when it beats the
+ * rule's by ≥ 3 %.
  * Decisions are cached for the process (shared by all handles); nothing is tuned while the stream
  * is being captured.  Plans change the order of the split-K sums, so results of a tuned handle
  * may differ from a default one's in the last bits.  on = 0 (the default): the fixed rule. */
+/* on = 2: no timing; every tensor-core pass with N ≤ 64 takes the two-CTAs-per-SM plan at its own
+ * fixed-rule count. */
 int slemm_gpu_set_autotune(slemm_geno* g, int on);
-/* The cached decisions: *rows = their number; for r < max_rows, info[6r …] = {device, N, pieces,
- * rule's splits, chosen splits, candidates timed}, shape[2r …] = {K-tiles, padded rows},
+/* The cached decisions: *rows = their number; for r < max_rows, info[7r …] = {device, N, pieces,
+ * rule's splits, chosen splits, chosen plan (0: the default ring, 1: two CTAs per SM), candidates
+ * timed}, shape[2r …] = {K-tiles, padded rows},
  * ms[2r …] = {rule's ms per launch, chosen ms per launch}.  Any of info, shape, ms may be NULL. */
 int slemm_gpu_autotune_table(int max_rows, int* rows, int32_t* info, int64_t* shape, double* ms);
 
 /* ---- measurement ---------------------------------------------------------------------------------- */
 /* Per-launch timing of the packed products with CUDA events on the handle's stream (no
  * counterpart in the reference, which only prints wall-clock times, src/option.cpp:21-34).
- * Reads the statistics gathered so far (rows of info = {tc, N, k, pieces, dir}, launch count,
- * total ms), then: enable = 1 clears and starts recording, 0 clears and stops, −1 leaves the
+ * Reads the statistics gathered so far (rows of info, 7 per shape = {tc, N, k, pieces, dir,
+ * splits, plan}, launch count, total ms), then: enable = 1 clears and starts recording, 0 clears and stops, −1 leaves the
  * state as it is.  *rows receives the number of distinct launch shapes. */
 int slemm_gpu_profile(slemm_geno* g, int enable, int max_rows, int* rows, int32_t* info,
                       int64_t* launches, double* ms);

@@ -140,9 +140,12 @@ class Genotypes:
     def set_per_vector(self, flag: bool):
         check(self._lib.slemm_gpu_set_per_vector(self.h, 1 if flag else 0))
 
-    def set_autotune(self, on: bool = True):
-        """Split-K counts of this handle's tensor-core passes picked by timing at first use."""
-        check(self._lib.slemm_gpu_set_autotune(self.h, 1 if on else 0))
+    def set_autotune(self, on=True):
+        """Split-K counts and ring plans of this handle's tensor-core passes picked by timing at first
+        use (True), by the fixed rule (False), or by the fixed rule with the two-CTAs-per-SM plan for
+        every pass with N ≤ 64 ("two_cta")."""
+        mode = 2 if on == "two_cta" else (1 if on else 0)
+        check(self._lib.slemm_gpu_set_autotune(self.h, mode))
 
     def set_lanczos(self, reorth: bool = False):
         """Lanczos mode of the seeds run on this handle (default: the reference's recurrence)."""
@@ -402,11 +405,12 @@ def autotune_table():
     rows = ctypes.c_int(0)
     check(lib.slemm_gpu_autotune_table(0, ctypes.byref(rows), None, None, None))
     r = rows.value
-    info = np.zeros(6 * max(r, 1), np.int32)
+    info = np.zeros(7 * max(r, 1), np.int32)
     shape = np.zeros(2 * max(r, 1), np.int64)
     ms = np.zeros(2 * max(r, 1), np.float64)
     check(lib.slemm_gpu_autotune_table(r, ctypes.byref(rows), _ptr(info), _ptr(shape), _ptr(ms)))
-    return [dict(device=int(info[6 * i]), N=int(info[6 * i + 1]), pieces=int(info[6 * i + 2]),
-                 rule_splits=int(info[6 * i + 3]), splits=int(info[6 * i + 4]), candidates=int(info[6 * i + 5]),
+    return [dict(device=int(info[7 * i]), N=int(info[7 * i + 1]), pieces=int(info[7 * i + 2]),
+                 rule_splits=int(info[7 * i + 3]), splits=int(info[7 * i + 4]), plan=int(info[7 * i + 5]),
+                 candidates=int(info[7 * i + 6]),
                  K_tiles=int(shape[2 * i]), M_pad=int(shape[2 * i + 1]), ms_rule=float(ms[2 * i]),
                  ms=float(ms[2 * i + 1])) for i in range(r)]

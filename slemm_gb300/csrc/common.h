@@ -193,14 +193,16 @@ struct GemmArgs {
   int kp = 0;           // columns of D per split (TC: k rounded up to 8; SIMT: N)
   int pieces = 1;       // pieces per column (TC)
   bool f16 = false;     // TC operand type: FP16 (true) or BF16
+  int plan = 0;         // TC ring plan: 0 by N (N ≤ 64: two tiles per CTA, one CTA per SM), 1: N ≤ 64,
+                        // one tile per CTA and two CTAs per SM (256 TMEM columns each)
 };
 
 void gemm_simt(const GemmArgs& a, cudaStream_t st);
 // Tensor-core path (tcgen05); N must be a multiple of 16 in [16, 256].
 void gemm_tc(const GemmArgs& a, cudaStream_t st);
 int choose_splits(int64_t M_tiles, int64_t K_tiles, int ctas_per_sm, int num_sms, int min_splits = 1);
-// Rows one tensor-core CTA covers for this N (128 or 256).
-int gemm_tc_rows_per_cta(int N);
+// Rows one tensor-core CTA covers for this N and plan (128 or 256).
+int gemm_tc_rows_per_cta(int N, int plan);
 int num_sms();
 
 }  // namespace slemm

@@ -41,10 +41,37 @@ __device__ __forceinline__ uint32_t f16pair_of(uint32_t word, int q)
   return *reinterpret_cast<const uint32_t*>(&r);
 }
 
+// The pair as FP16 subnormals, by masking alone: an FP16 whose exponent field is zero is
+// mantissa·2^−24, so a count x whose 2-bit field sits at bits 2s, 2s+1 of a half-word (s ≤ 4,
+// inside the 10-bit mantissa) reads as x·2^(2s−24).  Pairs q = 0 … 4 are masked in place
+// (s = q); pairs 5 … 7 from the word shifted right by 10 (s = q − 5).  The product's other
+// operand carries the factor 2^−2s of its K position (f16sub_kscale) and the accumulator is
+// multiplied by 2^24, so count·operand is the same product, exactly: one LOP per pair and one
+// shift per word.
+__device__ __forceinline__ int f16sub_shift(int q) { return q < 5 ? q : q - 5; }
+__device__ __forceinline__ uint32_t f16sub_pair_of(uint32_t word, int q)
+{
+  const uint32_t src = (q < 5) ? word : (word >> 10);
+  return src & (0x00030003u << (2 * f16sub_shift(q)));
+}
+// 2^−2s for the element at K index kidx (K-tiles start at multiples of 64; element j of a
+// 16-element word is K index ≡ j mod 16, pair q = j / 2).
+__device__ __forceinline__ float f16sub_kscale(int64_t kidx)
+{
+  const int s = f16sub_shift((int)((kidx & 15) >> 1));
+  return __uint_as_float((uint32_t)(127 - 2 * s) << 23);
+}
+__device__ __forceinline__ float f16sub_kunscale(int64_t kidx)
+{
+  const int s = f16sub_shift((int)((kidx & 15) >> 1));
+  return __uint_as_float((uint32_t)(127 + 2 * s) << 23);
+}
+constexpr float kF16SubUnscale = 16777216.0f;   // 2^24
+
 template <bool F16>
 __device__ __forceinline__ uint32_t pair_of(uint32_t word, int q)
 {
-  if constexpr (F16) return f16pair_of(word, q);
+  if constexpr (F16) return f16sub_pair_of(word, q);
   else return bf16pair_of(word, q);
 }
 

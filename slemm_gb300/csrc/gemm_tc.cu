@@ -3,8 +3,10 @@
 // D[s][n][r] = Σ_{K in split s} count[r,K] · B[n][K].  One CTA owns SUB (1 or 2) tiles of 128
 // rows, each with its own TMEM accumulator (128 lanes × N FP32 columns); every B tile feeds all
 // of them.  The decoded counts (the MMA's A operand) never touch shared memory: decoder threads
-// turn their row's 16 packed bytes into 32 BF16 pairs in registers and write them into tensor
-// memory with tcgen05.st; the MMA reads A from TMEM and B from shared memory.
+// turn their row's 16 packed bytes into 32 16-bit pairs in registers and write them into tensor
+// memory with tcgen05.st; the MMA reads A from TMEM and B from shared memory.  BF16 pairs cost
+// one LOP and one HFMA2 each; FP16 pairs are the counts as FP16 subnormals, one LOP each, with
+// the matching power of two per K position in B and 2^24 in the epilogue (decode.cuh).
 //
 // What limits tcgen05 here is the issuing thread, not the tensor pipe.  Measured on GB300: one
 // thread issuing M=128, N=144, K=16 BF16 MMAs back to back keeps the pipe full (72 cycles per
@@ -55,6 +57,11 @@ namespace slemm {
 constexpr int kPkg = 4;                // K-tiles per packed slot
 constexpr int kNG = 3;                 // decoder groups (each keeps one stage in flight)
 constexpr int kMaxThreads = 64 + 2 * 32 + kNG * 2 * 128;   // SUB = 2
+// Threads of a one-tile CTA (the narrow plan that runs two CTAs per SM, 256 TMEM columns each).
+constexpr int kThreads1 = 64 + 32 + kNG * 128;
+// Launch bounds of a plan: TM = 512 TMEM columns per CTA, one CTA per SM; TM = 256, two.
+constexpr int tc_max_threads(int TM) { return TM == 512 ? kMaxThreads : kThreads1; }
+constexpr int tc_min_blocks(int TM) { return TM == 512 ? 1 : 2; }
 constexpr uint64_t kWaitBudgetNs = 2000000000ull;   // 2 s per wait
 constexpr size_t kSmemBudget = 227 * 1024;
 
@@ -76,11 +83,12 @@ struct TcPlan {
   __host__ __device__ uint32_t acol() const { return (uint32_t)(((sub * N + 31) / 32) * 32); }
 };
 
-// Two tiles when their accumulators and S A-stages of KT K-tiles fit the 512 TMEM columns, else one.
-template <int PK, int S, int SB, int KT>
+// Two tiles when their accumulators and S A-stages of KT K-tiles fit the 512 TMEM columns, else one;
+// a plan with TM = 256 (two CTAs per SM) always has one tile.
+template <int PK, int S, int SB, int KT, int TM = 512>
 static TcPlan<PK, S, SB, KT> plan_tc(int N)
 {
-  if ((((2 * N + 31) / 32) * 32) + 2 * 32 * KT * S <= 512) return TcPlan<PK, S, SB, KT>(N, 2);
+  if (TM == 512 && (((2 * N + 31) / 32) * 32) + 2 * 32 * KT * S <= 512) return TcPlan<PK, S, SB, KT>(N, 2);
   return TcPlan<PK, S, SB, KT>(N, 1);
 }
 constexpr int kNarrowN = 64;   // N ≤ 64 uses the deep ring
@@ -253,8 +261,8 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32
       : "memory");
 }
 
-template <int PK, int S, int SB, int KT, bool F16>
-__global__ void __launch_bounds__(kMaxThreads, 1)
+template <int PK, int S, int SB, int KT, bool F16, int TM>
+__global__ void __launch_bounds__(tc_max_threads(TM), tc_min_blocks(TM))
 gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMap tmapB,
                float* __restrict__ D, int64_t M_pad, int K_tiles, int tiles_per_split, int N, int sub,
                int kp, int pieces, int* __restrict__ err, int withhold)
@@ -305,7 +313,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
   if (warp == 2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(512)
+                 "r"(TM)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -475,6 +483,10 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
 #pragma unroll
             for (int j = 0; j < 8; ++j) acc[j] = 0.f;
           }
+          if constexpr (F16) {   // the FP16 counts were x·2^(2s−24), the operand ·2^−2s
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] = __fmul_rn(acc[j], kF16SubUnscale);
+          }
 #pragma unroll
           for (int j = 0; j < 8; ++j) Dbase[(size_t)(c0 + j) * M_pad] = acc[j];
         }
@@ -488,7 +500,7 @@ gemm_tc_kernel(const uint8_t* __restrict__ A, const __grid_constant__ CUtensorMa
     if (*abort_flag && lane == 0) mbar_wait_drain(accum, 0);   // MMAs finished before freeing TMEM
     __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TM)
                  : "memory");
   }
 }
@@ -517,8 +529,9 @@ static PFN_encodeTiled get_encode()
   return fn;
 }
 
-int gemm_tc_rows_per_cta(int N)
+int gemm_tc_rows_per_cta(int N, int plan)
 {
+  if (N <= kNarrowN && plan == 1) return kTileM;
   return (N <= kNarrowN ? plan_tc<6, 3, 0, 2>(N).sub : plan_tc<4, 3, 6, 1>(N).sub) * kTileM;
 }
 
@@ -536,13 +549,13 @@ static void configure_once()
   done.fetch_or(bit);
 }
 
-template <int PK, int S, int SB, int KT, bool F16>
+template <int PK, int S, int SB, int KT, bool F16, int TM = 512>
 static void launch_tc(const GemmArgs& a, cudaStream_t st)
 {
-  const TcPlan<PK, S, SB, KT> P = plan_tc<PK, S, SB, KT>(a.N);
+  const TcPlan<PK, S, SB, KT> P = plan_tc<PK, S, SB, KT, TM>(a.N);
   CHECK_ARG(a.M_pad % (P.sub * kTileM) == 0 && a.K_pad % 128 == 0, "unpadded operand");
   CHECK_ARG(((uintptr_t)a.A % 16) == 0 && ((uintptr_t)a.B % 16) == 0, "misaligned operand");
-  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * S * KT <= 512, "no TMEM/shared-memory plan for this N");
+  CHECK_ARG(P.total <= kSmemBudget && P.acol() + 32 * P.sub * S * KT <= TM, "no TMEM/shared-memory plan for this N");
   const int64_t Mc = a.M_pad / (P.sub * kTileM);
   const int K_tiles = (int)(a.K_pad / kTileK);
   CHECK_ARG(K_tiles % KT == 0, "K tiles not a multiple of the stage");
@@ -560,13 +573,13 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) SLEMM_THROW(SLEMM_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 
-  configure_once<gemm_tc_kernel<PK, S, SB, KT, F16>>();
+  configure_once<gemm_tc_kernel<PK, S, SB, KT, F16, TM>>();
   CHECK_ARG(a.kp % 8 == 0 && a.pieces >= 1 && a.pieces * a.kp <= a.N, "bad piece layout");
-  // Each CTA allocates all 512 TMEM columns: request enough shared memory that only one CTA is
-  // resident per SM, so no allocation ever has to wait for another CTA's release.
-  const size_t smem = std::max<size_t>(P.total, 120 * 1024);
+  // Each CTA allocates TM of the SM's 512 TMEM columns: request enough shared memory that at most
+  // 512 / TM CTAs are resident per SM, so no allocation ever has to wait for another CTA's release.
+  const size_t smem = std::max<size_t>(P.total, TM == 512 ? 120 * 1024 : 80 * 1024);
   dim3 grid((unsigned)Mc, (unsigned)a.splits);
-  gemm_tc_kernel<PK, S, SB, KT, F16><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N,
+  gemm_tc_kernel<PK, S, SB, KT, F16, TM><<<grid, P.threads(), smem, st>>>(a.A, map, a.D, a.M_pad, K_tiles, tps, a.N,
                                                                        P.sub, a.kp, a.pieces, a.err,
                                                                        g_withhold_b.exchange(-1));
   LAUNCH_CHECK();
@@ -575,12 +588,15 @@ static void launch_tc(const GemmArgs& a, cudaStream_t st)
 void gemm_tc(const GemmArgs& a, cudaStream_t st)
 {
   CHECK_ARG(a.N >= 16 && a.N <= 256 && a.N % 16 == 0, "TC path needs N in [16,256], N%16==0");
+  CHECK_ARG(a.plan == 0 || (a.plan == 1 && a.N <= kNarrowN), "unknown tensor-core plan");
   if (a.f16) {
-    if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2, true>(a, st);
-    else launch_tc<4, 3, 6, 1, true>(a, st);
+    if (a.N > kNarrowN) launch_tc<4, 3, 6, 1, true>(a, st);
+    else if (a.plan == 1) launch_tc<6, 3, 0, 2, true, 256>(a, st);
+    else launch_tc<6, 3, 0, 2, true>(a, st);
   } else {
-    if (a.N <= kNarrowN) launch_tc<6, 3, 0, 2, false>(a, st);
-    else launch_tc<4, 3, 6, 1, false>(a, st);
+    if (a.N > kNarrowN) launch_tc<4, 3, 6, 1, false>(a, st);
+    else if (a.plan == 1) launch_tc<6, 3, 0, 2, false, 256>(a, st);
+    else launch_tc<6, 3, 0, 2, false>(a, st);
   }
 }
 

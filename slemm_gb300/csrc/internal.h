@@ -18,7 +18,8 @@ struct slemm_geno {
   int prec = SLEMM_PREC_BF16X2;
   int per_vector = 0;
   int lanczos_mode = 0;           // SLEMM_LANCZOS_* bits of the seeds run on this handle
-  bool autotune = false;          // tensor-core passes take their split-K count from the tuner
+  int autotune = 0;               // tensor-core plans: 0 the fixed rule, 1 the tuner's, 2 the fixed rule
+                                  // with two CTAs per SM wherever N ≤ 64
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // work buffers
@@ -49,12 +50,13 @@ struct slemm_geno {
   struct GemmRecord {
     cudaEvent_t start, stop;
     int tc, N, k, pieces, splits, dir;   // dir 1: Zᵀ pass (M = SNPs), 2: Z pass (M = individuals)
+    int plan;                            // tensor-core ring plan (GemmArgs::plan)
   };
   bool profiling = false;
   std::vector<GemmRecord> prof_pending;
   std::vector<cudaEvent_t> event_pool;
   struct GemmStat {
-    int tc, N, k, pieces, dir;
+    int tc, N, k, pieces, dir, splits, plan;
     int64_t launches;
     double ms;
   };

@@ -17,6 +17,7 @@
 // are bit-reproducible run to run.
 #include "internal.h"
 #include "reduce.cuh"
+#include "decode.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -299,9 +300,12 @@ __device__ __forceinline__ void store_operand(const float (&x)[V], int npieces, 
     for (int u = 0; u < V; ++u) {
       float hf;
       if constexpr (F16) {
-        // piece 0: the integer part (|r| ≤ 2^11, exact in FP16); later pieces: FP16 rounding
-        const __half hh = __float2half_rn(p == 0 ? rintf(r[u]) : r[u]);
-        hf = __half2float(hh);
+        // Stored times the K position's 2^−2s (the decoded counts carry 2^2s, f16sub_pair_of).
+        // piece 0: the integer part (|r| ≤ 2^11: exact in FP16 after the ≥ 2^−8 factor); later
+        // pieces: FP16 rounding of the scaled residual, subnormal below 2^−14 (absolute step
+        // 2^−24·2^2s ≤ 2^−16 in units of r, against pieces of up to 2^11)
+        const __half hh = __float2half_rn(__fmul_rn(p == 0 ? rintf(r[u]) : r[u], f16sub_kscale(kidx + u)));
+        hf = __fmul_rn(__half2float(hh), f16sub_kunscale(kidx + u));   // exact
         h[u] = __half_as_ushort(hh);
       } else {
         const __nv_bfloat16 hb = __float2bfloat16_rn(r[u]);
@@ -677,6 +681,7 @@ struct PassPlan {
   int kp;       // rows between a column's pieces (k rounded up to 8) and columns of D per split
   int N;        // columns of the product
   int splits;
+  int plan = 0; // tensor-core ring plan (GemmArgs::plan)
 };
 
 // Fewest splits of a tensor-core pass.  Once the dense operand (K_pad·N BF16) is larger than half
@@ -694,11 +699,12 @@ static cudaEvent_t take_event(slemm_geno* g);
 
 // ---- split-K autotuner ------------------------------------------------------------------------------
 // With a handle's autotune on, the first tensor-core pass of each shape (device, N, pieces, K-tiles,
-// padded rows) times a handful of split-K counts with CUDA events on the handle's stream — the
-// fixed rule's count, and counts near it whose CTAs fill the last wave to ≥ 80 % — each launched
-// once to warm up and twice timed over the real packed copy, and keeps the fastest if it beats the
-// rule's by ≥ 3 % (else the rule's, so close calls do not flip between processes).  Decisions are
-// cached for the life of the process; no tuning happens while the stream is being captured.
+// padded rows) times a handful of (plan, split-K) choices with CUDA events on the handle's stream —
+// the fixed rule's count, and counts near it whose CTAs fill the last wave to ≥ 80 %; for N ≤ 64
+// also the two-CTAs-per-SM plan at its own rule's count and counts near it — each launched once to
+// warm up and twice timed over the real packed copy, and keeps the fastest if it beats the rule's by
+// ≥ 3 % (else the rule's, so close calls do not flip between processes).  Decisions are cached for
+// the life of the process; no tuning happens while the stream is being captured.
 struct TuneKey {
   int dev, N, pieces;
   int64_t K_tiles, M_pad;
@@ -708,28 +714,18 @@ struct TuneKey {
   }
 };
 struct TuneEntry {
-  int rule, best, candidates;
+  int rule, best, plan, candidates;
   double ms_rule, ms_best;
 };
 static std::mutex g_tune_mu;
 static std::map<TuneKey, TuneEntry> g_tune;
 
-static int tune_splits(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t M_pad, int64_t K_pad, int rule)
+// Up to `most` split counts near `rule` (rule first) whose CTAs fill the last wave to ≥ 80 %.
+static void near_splits(int rule, int64_t ctas, int per_sm, int64_t K_tiles, int plan, size_t most,
+                        std::vector<std::pair<int, int>>& cand)
 {
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  CUDA_TRY(cudaStreamIsCapturing(g->stream, &cs));
-  if (cs != cudaStreamCaptureStatusNone) return rule;
-  const int64_t K_tiles = K_pad / kTileK;
-  const TuneKey key{g->device, p.N, p.pieces, K_tiles, M_pad};
-  {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(key);
-    if (it != g_tune.end()) return it->second.best;
-  }
-  // candidates: the rule's count, then counts near it with a well-filled last wave
-  const int64_t ctas = M_pad / gemm_tc_rows_per_cta(p.N);
-  const int sms = num_sms();
-  std::vector<int> cand{rule};
+  const int sms = num_sms() * per_sm;
+  cand.push_back({plan, rule});
   std::vector<std::pair<int, int>> near;   // (distance, s)
   const int smax = (int)std::min<int64_t>(std::max(3 * rule + 2, 8), std::max<int64_t>(1, K_tiles / 16));
   for (int s = std::max(1, rule / 3); s <= smax; ++s) {
@@ -738,15 +734,44 @@ static int tune_splits(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64
     if (waves / std::ceil(waves) >= 0.8) near.push_back({std::abs(s - rule), s});
   }
   std::sort(near.begin(), near.end());
-  for (size_t i = 0; i < near.size() && cand.size() < 6; ++i) cand.push_back(near[i].second);
-  const int smost = *std::max_element(cand.begin(), cand.end());
+  for (size_t i = 0; i < near.size() && i + 1 < most; ++i) cand.push_back({plan, near[i].second});
+}
+
+// Tunes p.splits and p.plan in place.
+static void tune_pass(slemm_geno* g, PassPlan& p, const uint8_t* A, int64_t M_pad, int64_t K_pad)
+{
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return;
+  const int64_t K_tiles = K_pad / kTileK;
+  const TuneKey key{g->device, p.N, p.pieces, K_tiles, M_pad};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      p.splits = it->second.best;
+      p.plan = it->second.plan;
+      return;
+    }
+  }
+  // candidates: the rule's count, then counts near it with a well-filled last wave; for N ≤ 64 the
+  // same around the two-CTAs-per-SM plan's rule
+  std::vector<std::pair<int, int>> cand;   // (plan, splits)
+  near_splits(p.splits, M_pad / gemm_tc_rows_per_cta(p.N, 0), 1, K_tiles, 0, 6, cand);
+  if (p.N <= 64) {
+    const int64_t ctas1 = M_pad / gemm_tc_rows_per_cta(p.N, 1);
+    const int rule1 = choose_splits(ctas1, K_tiles, 2, num_sms(), tc_min_splits(K_tiles, p.N));
+    near_splits(rule1, ctas1, 2, K_tiles, 1, 3, cand);
+  }
+  int smost = 1;
+  for (const auto& c : cand) smost = std::max(smost, c.second);
   DevBuf dD(g->stream);
   float* D = (float*)dD.ensure((size_t)smost * p.kp * M_pad * sizeof(float));
   const void* B = g->ws_B.ensure((size_t)p.N * K_pad * 2);   // timing only: the operand's values do not matter
   cudaEvent_t e0 = take_event(g), e1 = take_event(g);
   std::vector<double> ms(cand.size());
   for (size_t i = 0; i < cand.size(); ++i) {
-    GemmArgs a{A, M_pad, K_pad, B, p.N, D, cand[i], g->err.as<int>(), p.kp, p.pieces, p.f16};
+    GemmArgs a{A, M_pad, K_pad, B, p.N, D, cand[i].second, g->err.as<int>(), p.kp, p.pieces, p.f16, cand[i].first};
     gemm_tc(a, g->stream);
     CUDA_TRY(cudaEventRecord(e0, g->stream));
     gemm_tc(a, g->stream);
@@ -765,8 +790,9 @@ static int tune_splits(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64
     if (ms[i] < ms[b]) b = i;
   if (ms[b] > 0.97 * ms[0]) b = 0;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = {rule, cand[b], (int)cand.size(), ms[0], ms[b]};
-  return cand[b];
+  g_tune[key] = {p.splits, cand[b].second, cand[b].first, (int)cand.size(), ms[0], ms[b]};
+  p.plan = cand[b].first;
+  p.splits = cand[b].second;
 }
 
 static PassPlan plan_pass(slemm_geno* g, int k, int64_t M_pad, int64_t K_pad, const uint8_t* A)
@@ -778,10 +804,15 @@ static PassPlan plan_pass(slemm_geno* g, int k, int64_t M_pad, int64_t K_pad, co
   p.kp = p.tc ? (int)round_up(k, 8) : k;
   p.N = p.tc ? (int)round_up((int64_t)p.pieces * p.kp, 16) : k;
   const int64_t M_tiles = M_pad / kTileM, K_tiles = K_pad / kTileK;
-  p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(),
+  p.splits = p.tc ? choose_splits(M_pad / gemm_tc_rows_per_cta(p.N, 0), K_tiles, 1, num_sms(),
                                   tc_min_splits(K_tiles, p.N))
                   : choose_splits(M_tiles, K_tiles, 8, num_sms());
-  if (p.tc && g->autotune && A) p.splits = tune_splits(g, p, A, M_pad, K_pad, p.splits);
+  if (p.tc && g->autotune == 2 && p.N <= 64) {
+    p.plan = 1;
+    p.splits = choose_splits(M_pad / gemm_tc_rows_per_cta(p.N, 1), K_tiles, 2, num_sms(),
+                             tc_min_splits(K_tiles, p.N));
+  }
+  if (p.tc && g->autotune == 1 && A) tune_pass(g, p, A, M_pad, K_pad);
   return p;
 }
 
@@ -814,13 +845,14 @@ void profile_collect(slemm_geno* g)
     CUDA_TRY(cudaEventElapsedTime(&ms, r.start, r.stop));
     bool found = false;
     for (auto& s : g->prof_stats)
-      if (s.tc == r.tc && s.N == r.N && s.k == r.k && s.dir == r.dir && s.pieces == r.pieces) {
+      if (s.tc == r.tc && s.N == r.N && s.k == r.k && s.dir == r.dir && s.pieces == r.pieces &&
+          s.splits == r.splits && s.plan == r.plan) {
         s.launches += 1;
         s.ms += ms;
         found = true;
         break;
       }
-    if (!found) g->prof_stats.push_back({r.tc, r.N, r.k, r.pieces, r.dir, 1, (double)ms});
+    if (!found) g->prof_stats.push_back({r.tc, r.N, r.k, r.pieces, r.dir, r.splits, r.plan, 1, (double)ms});
     g->event_pool.push_back(r.start);
     g->event_pool.push_back(r.stop);
   }
@@ -830,11 +862,11 @@ void profile_collect(slemm_geno* g)
 static void run_gemm(slemm_geno* g, const PassPlan& p, const uint8_t* A, int64_t M_pad,
                      int64_t K_pad, const void* B, float* D, int* err, int k, int dir)
 {
-  GemmArgs a{A, M_pad, K_pad, B, p.N, D, p.splits, err, p.kp, p.pieces, p.f16};
+  GemmArgs a{A, M_pad, K_pad, B, p.N, D, p.splits, err, p.kp, p.pieces, p.f16, p.plan};
   slemm_geno::GemmRecord rec{};
   if (g->profiling) {
     if (g->prof_pending.size() >= 512) profile_collect(g);
-    rec = {take_event(g), take_event(g), p.tc ? 1 : 0, p.N, k, p.pieces, p.splits, dir};
+    rec = {take_event(g), take_event(g), p.tc ? 1 : 0, p.N, k, p.pieces, p.splits, dir, p.plan};
     CUDA_TRY(cudaEventRecord(rec.start, g->stream));
   }
   if (p.tc) gemm_tc(a, g->stream);
@@ -1055,7 +1087,7 @@ void rows_product(slemm_geno* g, int64_t r0, int64_t rows, const float* U, int64
     p.pieces = pieces;
     p.kp = (int)round_up(kc, 8);
     p.N = (int)round_up((int64_t)pieces * p.kp, 16);
-    p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N), K_tiles, 1, num_sms(), tc_min_splits(K_tiles, p.N));
+    p.splits = choose_splits(rows / gemm_tc_rows_per_cta(p.N, 0), K_tiles, 1, num_sms(), tc_min_splits(K_tiles, p.N));
     const int pad = p.N - pieces * kc;
     void* B1 = g->ws_B.ensure((size_t)p.N * K_pad * 2);
     float* D = (float*)g->ws_D.ensure((size_t)p.splits * p.kp * rows * sizeof(float));
@@ -1163,8 +1195,8 @@ extern "C" int slemm_gpu_set_autotune(slemm_geno* g, int on)
 {
   return guarded([&] {
     CHECK_ARG(g != nullptr, "null handle");
-    CHECK_ARG(on == 0 || on == 1, "on must be 0 or 1");
-    g->autotune = on != 0;
+    CHECK_ARG(on >= 0 && on <= 2, "on must be 0, 1 or 2");
+    g->autotune = on;
   });
 }
 
@@ -1178,9 +1210,9 @@ extern "C" int slemm_gpu_autotune_table(int max_rows, int* rows, int32_t* info, 
     for (const auto& kv : g_tune) {
       if (r >= max_rows) break;
       if (info) {
-        const int32_t v[6] = {kv.first.dev, kv.first.N, kv.first.pieces, kv.second.rule, kv.second.best,
-                              kv.second.candidates};
-        std::copy(v, v + 6, info + 6 * r);
+        const int32_t v[7] = {kv.first.dev, kv.first.N, kv.first.pieces, kv.second.rule, kv.second.best,
+                              kv.second.plan, kv.second.candidates};
+        std::copy(v, v + 7, info + 7 * r);
       }
       if (shape) {
         shape[2 * r] = kv.first.K_tiles;
@@ -1230,11 +1262,8 @@ extern "C" int slemm_gpu_profile(slemm_geno* g, int enable, int max_rows, int* r
     int r = 0;
     for (const auto& s : g->prof_stats) {
       if (r < max_rows && info && launches && ms) {
-        info[5 * r + 0] = s.tc;
-        info[5 * r + 1] = s.N;
-        info[5 * r + 2] = s.k;
-        info[5 * r + 3] = s.pieces;
-        info[5 * r + 4] = s.dir;
+        const int32_t v[7] = {s.tc, s.N, s.k, s.pieces, s.dir, s.splits, s.plan};
+        std::copy(v, v + 7, info + 7 * r);
         launches[r] = s.launches;
         ms[r] = s.ms;
       }

@@ -71,9 +71,9 @@ def test_roofline_object_arithmetic():
     launch over the measured launch time, against the measured BF16 peak (and the hi+lo ceiling,
     half of it), and the per-launch DRAM traffic scaled from the committed ncu summary."""
     n, m = 100000, 50000
-    prof = [{"tc": 1, "N": 144, "k": 66, "pieces": 2, "dir": 2, "launches": 10, "ms": 7.2},
-            {"tc": 1, "N": 16, "k": 1, "pieces": 2, "dir": 1, "launches": 1, "ms": 0.58}]
-    roof, gbs = bench.roofline(prof, n, m)
+    prof = [{"tc": 1, "N": 144, "k": 66, "pieces": 2, "dir": 2, "splits": 3, "plan": 0, "launches": 10, "ms": 7.2},
+            {"tc": 1, "N": 16, "k": 1, "pieces": 2, "dir": 1, "splits": 5, "plan": 0, "launches": 1, "ms": 0.58}]
+    roof, gbs = bench.roofline(prof, n, m, "fp16x2")
     pk = bench.peaks()
     t = 7.2e-3 / 10
     flops = 2.0 * n * m * 66
@@ -84,9 +84,12 @@ def test_roofline_object_arithmetic():
     assert roof["frac_eff"] == pytest.approx(2 * roof["frac"])
     assert roof["executed_tflops"] == pytest.approx(2.0 * n * m * 144 / t / 1e12)
     assert gbs == pytest.approx(m * ((n + 3) // 4) / t / 1e9)
-    # traffic: the committed per-launch figure of this shape at this size
+    # traffic: the committed capture's reads scaled by the packed bytes, its writes by the
+    # split-K partial bytes of this launch (3 splits x kp 72 x M_pad 100,096 x 4 B)
     import json
     with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-        tr = json.load(f)
-    assert roof["traffic"] == pytest.approx(tr["tc1_N144_dir2"])
-    assert bench.roofline([], n, m) == (None, None)
+        c = json.load(f)["fp16x2_tc1_N144_dir2"]
+    want = c["read"] * (m * 25000) / c["packed"] + c["write"] * (3 * 72 * 100096 * 4) / c["partials"]
+    assert roof["traffic"] == pytest.approx(want)
+    assert bench.roofline(prof, n, m, "bf16x2")[0]["traffic"] is None   # no capture of that kernel
+    assert bench.roofline([], n, m, "fp16x2") == (None, None)
