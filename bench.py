@@ -983,15 +983,13 @@ def run_multi(args, cfg):
         for _ in range(2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            rows_up = rows_host.to("cuda", non_blocking=True)   # the .bed rows cross the link once
-            torch.cuda.current_stream().synchronize()           # landed before the library's stream reads them
+            # the .bed rows cross the link once, through genotype_create's upload pipeline
             if keep_gw_host is not None:
-                step(rows_up, gwas_rows=keep_gw_host)
+                step(rows_host.numpy(), gwas_rows=keep_gw_host)
             else:
-                step(rows_up, gw)
+                step(rows_host.numpy(), gw)
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
-            del rows_up
         e2e = max_over_ranks(statistics.mean(e2e_times), dist)
         h2d = rows_host.numel() + sum(y.nbytes + x.nbytes for y, x in zip(ys, Xs)) + T * persnp.nbytes
         if keep_gw_host is not None:

@@ -52,14 +52,21 @@ class Genotypes:
             rows = bed_rows.contiguous()
             ptr = ctypes.c_void_p(rows.data_ptr())
             flags = _lib.ROWS_DEVICE
+            stride = rows.shape[1]
         else:
-            rows = np.ascontiguousarray(bed_rows, dtype=np.uint8)
+            rows = np.asarray(bed_rows)
+            if not (rows.dtype == np.uint8 and rows.ndim == 2 and rows.strides[1] == 1
+                    and rows.strides[0] >= rows.shape[1]):
+                rows = np.ascontiguousarray(rows, dtype=np.uint8)   # rows with a byte stride pass as they are
             ptr = _ptr(rows)
+            stride = rows.strides[0] if rows.shape[0] > 1 else rows.shape[1]
         m, rb = rows.shape
+        if rb < (n_fam + 3) // 4:
+            raise ValueError(f"rows of {rb} bytes hold fewer than the {n_fam} individuals' {(n_fam + 3) // 4} bytes")
         keep = None if keep_idx is None else np.ascontiguousarray(keep_idx, dtype=np.int64)
         n = n_fam if keep is None else keep.size
         h = ctypes.c_void_p()
-        check(self._lib.slemm_gpu_genotype_create(ptr, n_fam, m, rb, _ptr(keep), n, flags,
+        check(self._lib.slemm_gpu_genotype_create(ptr, n_fam, m, stride, _ptr(keep), n, flags,
                                                   ctypes.byref(h)))
         self.h = h
         self.n, self.m = int(n), int(m)

@@ -19,6 +19,7 @@
 
 #include <cstring>
 #include <mutex>
+#include <unistd.h>
 
 namespace slemm {
 
@@ -335,6 +336,36 @@ void row_counts_device(slemm_geno* g, int64_t* pc, int32_t* c1, int32_t* c2)
 
 // Ends the upload pipeline of genotype_create on every path out: waits for the copy stream
 // before the staging buffers (declared earlier, so released later) go back to the pool.
+// Reads one byte of every host page of [p, p + bytes) (p: the device view of pinned host memory).
+// A DMA from pinned memory whose pages the GPU has not translated recently — after a fit has
+// streamed tens of GB through the GPU's translation caches, or at first use — runs at ≈25 GB/s
+// while it waits on each page's translation in turn, against ≈210 GB/s warm (measured on GB300
+// over its C2C link: 7.5 GB of .bed rows took 0.27–0.50 s after a fit, 0.036 s warm).  Many
+// threads reading a byte each have all those translations in flight at once: 16 ms for the
+// 117,000 64-KB pages of 7.5 GB, after which the copies run warm (0.05 s in all).
+__device__ uint32_t g_touch_sink;
+__global__ void touch_host_pages_kernel(const uint8_t* __restrict__ p, int64_t bytes, int64_t page)
+{
+  uint32_t acc = 0;
+  for (int64_t o = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * page; o < bytes;
+       o += (int64_t)gridDim.x * blockDim.x * page)
+    acc += p[o];
+  if (acc == 0xFFFFFFFFu) g_touch_sink = acc;   // keeps the loads (a thread's sum stays below 2^32 − 1
+                                                // for fewer than 2^24 pages per thread)
+}
+
+// Device view of pinned host memory (cudaHostAlloc / cudaHostRegister), or null for any other
+// pointer (pageable host memory is not touched from the device).
+static const uint8_t* pinned_device_view(const void* host)
+{
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? static_cast<const uint8_t*>(at.devicePointer) : nullptr;
+}
+
 struct UploadPipe {
   cudaStream_t cs = nullptr;
   cudaEvent_t copied[2] = {nullptr, nullptr}, packed[2] = {nullptr, nullptr}, ready = nullptr;
@@ -468,7 +499,17 @@ int slemm_gpu_genotype_create(const uint8_t* bed_rows, int64_t n_fam, int64_t m,
         uint8_t* raw[2] = {raw0.as<uint8_t>(), raw1.as<uint8_t>()};
         UploadPipe pipe;   // destroyed before raw0/raw1: the copy stream is drained first
         pipe.open();
-        CUDA_TRY(cudaEventRecord(pipe.ready, g->stream));   // staging allocations, keep list, count zeroing
+        if (const uint8_t* dv = pinned_device_view(bed_rows)) {   // warm the translations of every page
+          const int64_t bytes = (m - 1) * row_stride + row_bytes;
+          const long hp = sysconf(_SC_PAGESIZE);
+          const int64_t page = std::min<int64_t>(65536, hp > 0 ? hp : 4096);
+          const int64_t pages = ceil_div(bytes, page);
+          const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(pages, 256), 8 * num_sms()));
+          touch_host_pages_kernel<<<blocks, 256, 0, g->stream>>>(dv, bytes, page);
+          CUDA_TRY(cudaGetLastError());
+        }
+        CUDA_TRY(cudaEventRecord(pipe.ready, g->stream));   // staging allocations, keep list, count zeroing,
+                                                             // page touches
         CUDA_TRY(cudaStreamWaitEvent(pipe.cs, pipe.ready, 0));
         const bool al = (row_bytes % 4 == 0);
         int c = 0;
