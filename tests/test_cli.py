@@ -148,3 +148,84 @@ def test_cli_reml_lrt_prediction_lmm_wls(cli, plink_case):
     ref = orc.WLS(ct, None, c["X"], c["y"])
     got = np.array([float(l.split(",")[9]) for l in w[1:]])
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-3
+
+
+# ---- GWAS step 2: slemm_gamma / slemm_gwa (bin/slemm_gamma.py, bin/slemm_gwa.py) ------------------
+import shutil
+import sys
+
+
+def run_py(module, *args, cwd=None):
+    env = dict(os.environ, PYTHONPATH=ROOT + os.pathsep + os.environ.get("PYTHONPATH", ""))
+    return subprocess.run([sys.executable, "-m", module, *args], capture_output=True, text=True, cwd=cwd,
+                          env=env, timeout=600)
+
+
+def test_gwas_commands_report_missing_files(tmp_path):
+    for mod in ("slemm_gb300.cli.slemm_gamma", "slemm_gb300.cli.slemm_gwa"):
+        extra = ["--chr", "1"] if mod.endswith("gwa") else []
+        r = run_py(mod, "--pfile", str(tmp_path / "nothing"), "--slemm", "s1", "--out", "o.txt", *extra)
+        assert r.returncode == 0 and "Files do not exit:" in r.stdout and "Searching for bed/bim/fam" in r.stdout
+        r = run_py(mod, "--slemm", "s1", "--out", "o.txt", *extra)
+        assert r.returncode == 0 and "Genotype files are not specified" in r.stdout
+    r = run_py("slemm_gb300.cli.slemm_gamma", "--slemm", "s1")
+    assert r.returncode == 2 and "--out" in r.stderr                      # argparse: required option
+
+
+def test_gwas_commands_reject_pgen(tmp_path):
+    """A PLINK 2 .pgen (magic 6c 1b, storage mode ≠ 01) is reported as unsupported before any GPU
+    work; the step-1 files and the sample/variant files are read first, as the scripts do."""
+    src = os.path.join(GOLD, "gamma_case")
+    for f in ("s1.gstat.txt", "s1.reml.py.txt", "s1.reml.vc.csv"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    shutil.copy(os.path.join(src, "geno.fam"), tmp_path / "geno.psam")
+    shutil.copy(os.path.join(src, "geno.bim"), tmp_path / "geno.pvar")
+    (tmp_path / "geno.pgen").write_bytes(bytes([0x6C, 0x1B, 0x10]) + bytes(64))
+    r = run_py("slemm_gb300.cli.slemm_gamma", "--pfile", "geno", "--slemm", "s1", "--out", "o.txt", cwd=tmp_path)
+    assert r.returncode == 1 and "PLINK 2 .pgen (storage mode 0x10)" in r.stderr, r.stderr
+    assert "Correction factor is" in r.stdout and not (tmp_path / "o.txt").exists()
+
+
+def _stats_file(path):
+    rows = [l.split("\t") for l in open(path).read().splitlines()]
+    return rows[0], [r[:-4] for r in rows[1:]], np.array([[float(v) for v in r[-4:]] for r in rows[1:]])
+
+
+def _compare_stats(got_path, want_path):
+    h1, v1, s1 = _stats_file(got_path)
+    h2, v2, s2 = _stats_file(want_path)
+    assert h1 == h2 and v1 == v2                                 # header and variant columns identical
+    ok = np.isfinite(s2[:, 3])
+    assert np.array_equal(ok, np.isfinite(s1[:, 3]))             # same filtered variants
+    assert np.allclose(s1[ok, 0], s2[ok, 0], rtol=1e-3, atol=1e-5)   # beta
+    assert np.allclose(s1[ok, 1], s2[ok, 1], rtol=1e-3)              # se
+    assert np.max(np.abs(np.log10(s1[ok, 3]) - np.log10(s2[ok, 3]))) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_gamma_command_matches_reference_script_output(tmp_path):
+    """slemm_gamma on the golden case against the output of the reference's own script."""
+    src = os.path.join(GOLD, "gamma_case")
+    r = run_py("slemm_gb300.cli.slemm_gamma", "--pfile", os.path.join(src, "geno"), "--slemm",
+               os.path.join(src, "s1"), "--out", str(tmp_path / "gamma.txt"))
+    assert r.returncode == 0, r.stderr
+    _compare_stats(tmp_path / "gamma.txt", os.path.join(src, "gamma.txt"))
+    # --begin/--end select a variant range: the same lines of the full output
+    r = run_py("slemm_gb300.cli.slemm_gamma", "--pfile", os.path.join(src, "geno"), "--slemm",
+               os.path.join(src, "s1"), "--out", str(tmp_path / "part.txt"), "--begin", "5", "--end", "20")
+    assert r.returncode == 0, r.stderr
+    full = open(tmp_path / "gamma.txt").read().splitlines()
+    part = open(tmp_path / "part.txt").read().splitlines()
+    assert part[0] == full[0] and len(part) == 17
+    assert [l.split("\t")[:6] for l in part[1:]] == [l.split("\t")[:6] for l in full[6:22]]
+
+
+@pytest.mark.gpu
+def test_gwa_command_matches_reference_script_output(tmp_path):
+    """slemm_gwa --chr 1 on the golden two-chromosome case against the reference script's output."""
+    src = os.path.join(GOLD, "gwa_case")
+    r = run_py("slemm_gb300.cli.slemm_gwa", "--pfile", os.path.join(src, "geno"), "--slemm", os.path.join(src, "s1"),
+               "--out", str(tmp_path / "gwa.txt"), "--chr", "1")
+    assert r.returncode == 0, r.stderr
+    assert "Completed building blocks:" in r.stdout
+    _compare_stats(tmp_path / "gwa.txt", os.path.join(src, "gwa.txt"))
