@@ -376,13 +376,14 @@ def l2_note(n, m):
             f"from HBM, 129 MB L2")
 
 
-def gpu_config(cfg, precision):
-    """The `config` object both arms print for the workload."""
+def gpu_config(cfg):
+    """The `config` object both arms print for the workload (the arithmetic each arm runs in is
+    its line's own `precision` key)."""
     n, m = cfg["n"], cfg["m"]
     out = {"workload": cfg["name"], "n": n, "m": m, "probes": cfg["probes"], "h2_sim": cfg["h2"]}
     if cfg.get("window"):
         out.update(ld_rho=cfg["ld_rho"], ld_block=cfg["ld_block"], window_size=cfg["window"])
-    out.update(precision=precision, l2=l2_note(n, m), parallelism="replicas")
+    out.update(l2=l2_note(n, m), parallelism="replicas")
     return out
 
 
@@ -424,7 +425,7 @@ def run_reference(args, cfg):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (random packed bytes of the workload's shape: the loop's time does not depend on the values)",
-        "config": gpu_config(cfg, "FP32 (the reference's float arithmetic)"),
+        "config": gpu_config(cfg), "precision": "FP32 (the reference's float arithmetic)",
         "steps_are": f"each timed step runs the reference's full-n subset loop on {S} of the {nsub} subsets "
                      f"({covered} subsets covered over the {args.steps} steps) and converts it to one whole fit; "
                      f"ms_per_step is that step's measured wall time",
@@ -612,7 +613,7 @@ def run_gpu(args, cfg):
         "warmup": args.warmup, "ms_per_step": mean_step * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded, generated on the GPU)",
-        "config": gpu_config(cfg, PRECISIONS[args.prec]),
+        "config": gpu_config(cfg), "precision": PRECISIONS[args.prec],
         "h2": res["h2"], "vg": res["vg"], "ve": res["ve"], "lrt": res["lrt"],
         "lanczos_steps": {"y": res["iters"][0], "Q": res["iters"][1], "V": res["iters"][2]},
         "counts": counts,
@@ -810,10 +811,9 @@ def run_grad(args, cfg):
         "scaling": "weak", "vs_baseline": None, "dtype": args.prec,
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "windows": int(wwin.size),
-                   "sigma_g2": sg2, "sigma_e2": se2,
-                   "precision": PRECISIONS[args.prec] + " in the Lanczos solves; column-scaled FP16 hi+lo in "
-                                "the closing Z^T pass; FP64 reductions",
-                   "l2": l2_note(n, m), "parallelism": "replicas"},
+                   "sigma_g2": sg2, "sigma_e2": se2, "l2": l2_note(n, m), "parallelism": "replicas"},
+        "precision": PRECISIONS[args.prec] + " in the Lanczos solves; column-scaled FP16 hi+lo in "
+                     "the closing Z^T pass; FP64 reductions",
         "gradient": h,
         "step_ms": [round(t * 1e3, 3) for t in times],
         "matvec_gbs": matvec_gbs,
@@ -1046,9 +1046,9 @@ def run_multi(args, cfg):
         "data": "synthetic (seeded, generated on the GPU)",
         "config": {"workload": cfg["name"], "n": n, "m": m, "probes": probes, "traits": T,
                    "missing_fraction": [round(float(f), 4) for f in frac], "gwas_m": m2,
-                   "precision": PRECISIONS[args.prec] + "; GWAS score pass at column-scaled FP16 hi+lo",
                    "l2": l2_note(n, m), "parallelism": "replicas",
                    "timing": "host clock around a device synchronisation (each trait handle has its own stream)"},
+        "precision": PRECISIONS[args.prec] + "; GWAS score pass at column-scaled FP16 hi+lo",
         "per_trait": [{"n": int(k.size), "h2": r["h2"], "iters": list(r["iters"])} for r, k in zip(res, keeps)],
         "phases_s": ph,
         "gwas": {"tested": int(np.isfinite(sc[0]).sum())},
