@@ -971,7 +971,7 @@ def run_multi(args, cfg):
         ph["fit_s"] += time.perf_counter() - t1
         gt.close()
     parent.close()
-    roof, matvec_gbs = roofline(prof, int(keeps[0].size), m, args.prec)
+    roof, matvec_gbs = roofline(prof, int(keeps[0].size), m, args.prec, sustained=mean_step > 1.0)
     t0 = time.perf_counter()
     gwas(gw, res[0]["Py"])
     torch.cuda.synchronize()
