@@ -291,17 +291,19 @@ lz_reorth_update_kernel(float* __restrict__ w, const float* const* __restrict__ 
 }
 
 // out[c] = Σ dot, out[t+c] = Σ nrm, out[2t+c] = Σ un (the consumers' order); out[3t] = error word.
-__global__ void lz_final_kernel(const double* __restrict__ dot, const double* __restrict__ nrm,
-                                const double* __restrict__ un, int t, int nblk, const int* __restrict__ err,
-                                double* __restrict__ out)
+// One block per column, one warp per quantity (dot, norm, unscaled norm), each summed over the
+// blocks' partials in warp_sum_partials' fixed order (the bits sum_partials gives in one thread);
+// a thread per column summing all three serially over strided partials took ≈57 µs per step.
+__global__ void __launch_bounds__(96) lz_final_kernel(const double* __restrict__ dot, const double* __restrict__ nrm,
+                                                      const double* __restrict__ un, int t, int nblk,
+                                                      const int* __restrict__ err, double* __restrict__ out)
 {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < t) {
-    out[c] = dot ? sum_partials(dot + (int64_t)c * nblk, nblk) : 0.0;
-    out[t + c] = sum_partials(nrm + (int64_t)c * nblk, nblk);
-    out[2 * t + c] = sum_partials(un + (int64_t)c * nblk, nblk);
-  }
-  if (c == 0) out[3 * t] = (double)*err;
+  const int c = blockIdx.x;
+  const int w = threadIdx.x >> 5;   // warp-uniform
+  const double* src = w == 0 ? dot : (w == 1 ? nrm : un);
+  const double s = src ? warp_sum_partials(src + (int64_t)c * nblk, nblk) : 0.0;
+  if ((threadIdx.x & 31) == 0) out[(int64_t)w * t + c] = s;
+  if (c == 0 && threadIdx.x == 0) out[3 * t] = (double)*err;
 }
 
 // X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]
@@ -399,7 +401,7 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     const int* err = g->err.as<int>();
     // Waits for the step's scalars in the mapped buffer and checks the kernels' error word.
     auto fetch = [&](const double* dot) {
-      lz_final_kernel<<<(unsigned)ceil_div(t, 128), 128, 0, st>>>(dot, r_nrm, r_un, t, nblk, err, d_out);
+      lz_final_kernel<<<(unsigned)t, 96, 0, st>>>(dot, r_nrm, r_un, t, nblk, err, d_out);
       LAUNCH_CHECK();
       CUDA_TRY(cudaStreamSynchronize(st));
       if (h[3 * t] != 0.0) {
