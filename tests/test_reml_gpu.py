@@ -94,6 +94,29 @@ def test_sldf_reml_vs_oracle(gpu, prec):
     assert abs(r["lrt"] - r64["lrt"]) <= 1e-2 * max(1.0, abs(r64["lrt"]))
 
 
+@pytest.mark.parametrize("c", [70, 256])
+def test_sldf_reml_many_covariates_vs_oracle(gpu, c):
+    """Covariate counts above the one-block limits of the reduction kernels (a warp per covariate
+    in the projection's coefficient loads): 70 and the maximum, SLEMM_MAX_COVARIATES = 256 —
+    --iter_weighting appends the fixed SNPs to the covariates, so a large c is ordinary input.
+    One more covariate is refused with an argument error."""
+    counts, rows, y, rvec, X, persnp = _problem(n=1500, m=1200, seed=37, c=c)
+    n = counts.shape[1]
+    r64 = orc.SLDF_REML(counts, rvec, X, y, persnp, seed=3, n_V=12, dtype=np.float64)
+    with api.Genotypes(rows, n) as g:
+        g.set_precision(_lib.PREC_FP16X2)
+        r = g.SLDF_REML(rvec, X, y, persnp, seed=3, n_V=12)
+        check_gss_branches(r["trace"], r64["gss"], 2e-3)
+        assert abs(r["h2"] - r64["h2"]) <= 1e-4
+        assert np.corrcoef(r["snp_blup"], r64["snp_blup"])[0, 1] >= 0.99999
+        assert np.allclose(r["blue"], r64["blue"], rtol=5e-3, atol=5e-3)
+        if c == 256:
+            X2 = np.column_stack([X, np.random.default_rng(2).standard_normal(n)]).astype(np.float32)
+            with pytest.raises(_lib.SlemmError) as e:
+                g.SLDF_REML(rvec, X2, y, persnp, seed=3, n_V=12)
+            assert e.value.code == -1
+
+
 def test_per_trait_individual_sets_vs_oracle(gpu):
     """Several traits with their own missing individuals (5 %, 20 %, 40 %) from one set of .bed
     rows held in device memory: each trait's handle is packed for its individuals (the reference
