@@ -294,16 +294,18 @@ lz_reorth_update_kernel(float* __restrict__ w, const float* const* __restrict__ 
 // One block per column, one warp per quantity (dot, norm, unscaled norm), each summed over the
 // blocks' partials in warp_sum_partials' fixed order (the bits sum_partials gives in one thread);
 // a thread per column summing all three serially over strided partials took ≈57 µs per step.
+// out[w·stride + c] for block c; err_out[0] = the kernels' error word.
 __global__ void __launch_bounds__(96) lz_final_kernel(const double* __restrict__ dot, const double* __restrict__ nrm,
-                                                      const double* __restrict__ un, int t, int nblk,
-                                                      const int* __restrict__ err, double* __restrict__ out)
+                                                      const double* __restrict__ un, int stride, int nblk,
+                                                      const int* __restrict__ err, double* __restrict__ out,
+                                                      double* __restrict__ err_out)
 {
   const int c = blockIdx.x;
   const int w = threadIdx.x >> 5;   // warp-uniform
   const double* src = w == 0 ? dot : (w == 1 ? nrm : un);
   const double s = src ? warp_sum_partials(src + (int64_t)c * nblk, nblk) : 0.0;
-  if ((threadIdx.x & 31) == 0) out[(int64_t)w * t + c] = s;
-  if (c == 0 && threadIdx.x == 0) out[3 * t] = (double)*err;
+  if ((threadIdx.x & 31) == 0) out[(int64_t)w * stride + c] = s;
+  if (c == 0 && threadIdx.x == 0) err_out[0] = (double)*err;
 }
 
 // X[i,c] = coefB[c]·B[i,c] + Σ_{j=1..J} coef[j·t + c]·U_j[i,c]
@@ -399,9 +401,12 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     const bool v4 = (n % 4) == 0;
     const dim3 gr(nblk, t);
     const int* err = g->err.as<int>();
-    // Waits for the step's scalars in the mapped buffer and checks the kernels' error word.
-    auto fetch = [&](const double* dot) {
-      lz_final_kernel<<<(unsigned)t, 96, 0, st>>>(dot, r_nrm, r_un, t, nblk, err, d_out);
+    // Waits for the step's scalars of columns lo … t−1 in the mapped buffer (h[c], h[t + c],
+    // h[2t + c]) and checks the kernels' error word (h[3t]).
+    auto fetch = [&](const double* dot, int lo) {
+      const size_t offr = (size_t)lo * nblk;
+      lz_final_kernel<<<(unsigned)(t - lo), 96, 0, st>>>(dot ? dot + offr : nullptr, r_nrm + offr, r_un + offr, t,
+                                                        nblk, err, d_out + lo, d_out + 3 * t);
       LAUNCH_CHECK();
       CUDA_TRY(cudaStreamSynchronize(st));
       if (h[3 * t] != 0.0) {
@@ -454,7 +459,7 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     if (v4) lz_scale_kernel<4><<<gr, kLzThreads, 0, st>>>(S->block(0), S->B.as<float>(), r_nrm, n, r_un, nblk);
     else lz_scale_kernel<1><<<gr, kLzThreads, 0, st>>>(S->block(0), S->B.as<float>(), r_nrm, n, r_un, nblk);
     LAUNCH_CHECK();
-    fetch(nullptr);
+    fetch(nullptr, 0);
     S->bnorm.resize(t);
     S->beta.assign(t, 0.0);
     S->unorm.assign(t, 0.0);
@@ -472,30 +477,47 @@ slemm_lseed* lanczos_seed_device(slemm_geno* g, int kind, float tau0, const floa
     const int ngroups = (int)groups.size();
     std::vector<double> col_res(t, 0.0);
     while (j < maxit - 1) {
-      float* Uj = S->block(j);
-      float* Uprev = j > 0 ? S->block(j - 1) : nullptr;
-      float* Un = S->block(j + 1);
-      op_device_mixed(g, kind, tau0, Uj, n, t, tmp, n, nq_eff);
+      // Leading column groups that have all met the tolerance leave the block: the remaining
+      // steps run on the columns from the first unconverged group on (a group's basis past its
+      // own step count is never read: solves and moments stop there).  Not with
+      // reorthogonalisation, whose passes run over every stored column.
+      int lo = 0;
+      if (!reorth)
+        for (int q = 0; q < ngroups && S->group_iters[q] >= 0; ++q) lo = S->group_start[q + 1];
+      const int ta = t - lo;   // ≥ 1: some group is still running
+      const size_t off = (size_t)lo * n, offr = (size_t)lo * nblk;
+      float* Uj = S->block(j) + off;
+      float* Uprev = j > 0 ? S->block(j - 1) + off : nullptr;
+      float* Un = S->block(j + 1) + off;
+      float* tmpa = tmp + off;
+      const dim3 gra(nblk, ta);
+      op_device_mixed(g, kind, tau0, Uj, n, ta, tmpa, n, std::max(0, nq_eff - lo));
       if (v4) {
-        lz_dot_kernel<4><<<gr, kLzThreads, 0, st>>>(tmp, Uj, Uprev, r_nrm, n, r_dot, nblk);
+        lz_dot_kernel<4><<<gra, kLzThreads, 0, st>>>(tmpa, Uj, Uprev, r_nrm + offr, n, r_dot + offr, nblk);
         LAUNCH_CHECK();
-        lz_orth_kernel<4><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
+        lz_orth_kernel<4><<<gra, kLzThreads, 0, st>>>(tmpa, Uj, r_dot + offr, n, r_nrm + offr, nblk);
         LAUNCH_CHECK();
         if (reorth) reorthogonalise(j);
-        lz_scale_kernel<4><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
+        lz_scale_kernel<4><<<gra, kLzThreads, 0, st>>>(Un, tmpa, r_nrm + offr, n, r_un + offr, nblk);
         LAUNCH_CHECK();
       } else {
-        lz_dot_kernel<1><<<gr, kLzThreads, 0, st>>>(tmp, Uj, Uprev, r_nrm, n, r_dot, nblk);
+        lz_dot_kernel<1><<<gra, kLzThreads, 0, st>>>(tmpa, Uj, Uprev, r_nrm + offr, n, r_dot + offr, nblk);
         LAUNCH_CHECK();
-        lz_orth_kernel<1><<<gr, kLzThreads, 0, st>>>(tmp, Uj, r_dot, n, r_nrm, nblk);
+        lz_orth_kernel<1><<<gra, kLzThreads, 0, st>>>(tmpa, Uj, r_dot + offr, n, r_nrm + offr, nblk);
         LAUNCH_CHECK();
         if (reorth) reorthogonalise(j);
-        lz_scale_kernel<1><<<gr, kLzThreads, 0, st>>>(Un, tmp, r_nrm, n, r_un, nblk);
+        lz_scale_kernel<1><<<gra, kLzThreads, 0, st>>>(Un, tmpa, r_nrm + offr, n, r_un + offr, nblk);
         LAUNCH_CHECK();
       }
-      fetch(r_dot);
+      fetch(r_dot, lo);
       double res = 0.0;
       for (int c = 0; c < t; ++c) {
+        if (c < lo) {   // a finished group: placeholders, never read
+          S->delta.push_back(0.0);
+          S->beta.push_back(0.0);
+          S->unorm.push_back(0.0);
+          continue;
+        }
         const double dl = h[c], bt = std::sqrt(h[t + c]), un = std::sqrt(h[2 * t + c]);
         S->delta.push_back(dl);
         S->beta.push_back(bt);

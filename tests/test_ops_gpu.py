@@ -61,7 +61,7 @@ CASES = [(1000, 700, 1.0), (1537, 1300, 0.9)]
 
 
 @pytest.mark.parametrize("prec", [_lib.PREC_FP16X2, _lib.PREC_BF16X2, _lib.PREC_BF16X3])
-@pytest.mark.parametrize("k", [1, 7, 66, 130])
+@pytest.mark.parametrize("k", [1, 7, 64, 66, 130])
 def test_column_scales_and_piece_layout(gpu, prec, k):
     """Columns of very different magnitudes (1e-30 … 1e30, a zero column, a column with a large
     mean) in one block: FP16 pieces are scaled per column by a power of two, so every column keeps
