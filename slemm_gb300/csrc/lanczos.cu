@@ -603,21 +603,22 @@ int solve_coeffs(const slemm_lseed* S, double sigma, double tol, int grp, std::v
 }
 
 // mom[i·npairs + p] = Σ_r B[r, a_p]·V_i[r, b_p] for i = 0 … J (V_0 = B, V_i = U_i); double-float
-// sums of the stored FP32 vectors, one pass over the basis.
+// sums of the stored FP32 vectors, one pass over the basis.  Grid (pairs, row blocks, J + 1): the
+// pairs (1 + c² for c covariates) exceed the 65,535 of a grid's y dimension at c = 256.
 __global__ void __launch_bounds__(kLzThreads)
-lz_moments_kernel(const float* __restrict__ B, const float* const* __restrict__ blocks,
+lz_moments_kernel(const float* __restrict__ B, const float* const* __restrict__ blocks, int i0,
                   const int2* __restrict__ pairs, int npairs, int64_t n, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
-  const int p = blockIdx.y, i = blockIdx.z;
+  const int p = blockIdx.x, i = i0 + blockIdx.z;   // red holds the steps i0 … of this launch
   const int2 ab = pairs[p];
   const float* Vi = (i == 0) ? B : blocks[i];
-  const int64_t r0 = (int64_t)blockIdx.x * kLzRows, r1 = min64(n, r0 + kLzRows);
+  const int64_t r0 = (int64_t)blockIdx.y * kLzRows, r1 = min64(n, r0 + kLzRows);
   DF acc;
   for (int64_t r = r0 + threadIdx.x; r < r1; r += kLzThreads)
     df_fma(acc, B[(int64_t)ab.x * n + r], Vi[(int64_t)ab.y * n + r]);
   const double s = block_sum_d(df_value(acc), sh);
-  if (threadIdx.x == 0) red[((int64_t)i * npairs + p) * nblk + blockIdx.x] = s;
+  if (threadIdx.x == 0) red[((int64_t)blockIdx.z * npairs + p) * nblk + blockIdx.y] = s;
 }
 
 // out[q] = Σ_b red[q][b] in block order, q < nq
@@ -641,15 +642,23 @@ void lanczos_moments(slemm_lseed* S, const std::vector<std::pair<int, int>>& pai
   dblk.ensure(hb.size() * sizeof(float*));
   dpairs.ensure(hp.size() * sizeof(int2));
   const int nq = (J + 1) * npairs;
-  dred.ensure((size_t)nq * nblk * sizeof(double));
+  // the block partials of at most 256 MB of steps at a time (c² pairs for c covariates)
+  const size_t per_step = (size_t)npairs * nblk * sizeof(double);
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)J + 1, ((size_t)256 << 20) / per_step));
+  dred.ensure(per_step * chunk);
   double* out = S->g->scal.ensure((size_t)nq);
   CUDA_TRY(cudaMemcpyAsync(dblk.p, hb.data(), hb.size() * sizeof(float*), cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(dpairs.p, hp.data(), hp.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-  lz_moments_kernel<<<dim3(nblk, npairs, J + 1), kLzThreads, 0, st>>>(
-      S->B.as<float>(), dblk.as<const float*>(), dpairs.as<int2>(), npairs, S->n, dred.as<double>(), nblk);
-  LAUNCH_CHECK();
-  lz_sum_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(dred.as<double>(), nblk, nq, out);
-  LAUNCH_CHECK();
+  for (int i0 = 0; i0 <= J; i0 += chunk) {
+    const int ni = std::min(chunk, J + 1 - i0);
+    lz_moments_kernel<<<dim3(npairs, nblk, ni), kLzThreads, 0, st>>>(
+        S->B.as<float>(), dblk.as<const float*>(), i0, dpairs.as<int2>(), npairs, S->n, dred.as<double>(), nblk);
+    LAUNCH_CHECK();
+    const int nqc = ni * npairs;
+    lz_sum_kernel<<<(unsigned)ceil_div(nqc, 128), 128, 0, st>>>(dred.as<double>(), nblk, nqc,
+                                                                 out + (size_t)i0 * npairs);
+    LAUNCH_CHECK();
+  }
   CUDA_TRY(cudaStreamSynchronize(st));
   mom.assign(S->g->scal.h, S->g->scal.h + nq);
 }

@@ -53,15 +53,16 @@ static void reduce_partials(const double* red, int nblk, int nq, double* out, cu
 }
 
 // ---- projections ---------------------------------------------------------------------------------
-// red[(l*k + c)][blk] = Σ_{i in block} Q[i,l]·X[i,c]
+// red[(l*k + c)][blk] = Σ_{i in block} Q[i,l]·X[i,c]; grid (c·k, row blocks): c·k reaches
+// 256 × 269 for the largest covariate count, beyond the 65,535 of a grid's y dimension.
 template <int V>
 __global__ void __launch_bounds__(kRedThreads)
 proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __restrict__ X, int64_t ldx,
                     int64_t n, int k, double* __restrict__ red, int nblk)
 {
   __shared__ double sh[32];
-  const int c = blockIdx.y % k, l = blockIdx.y / k;
-  const int64_t i0 = (int64_t)blockIdx.x * kRowsPerBlock, i1 = min64(n, i0 + kRowsPerBlock);
+  const int c = blockIdx.x % k, l = blockIdx.x / k;
+  const int64_t i0 = (int64_t)blockIdx.y * kRowsPerBlock, i1 = min64(n, i0 + kRowsPerBlock);
   DF acc;
   for (int64_t i = i0 + threadIdx.x * V; i < i1; i += kRedThreads * V) {
     float q[V], x[V];
@@ -71,7 +72,7 @@ proj_partial_kernel(const float* __restrict__ Q, int64_t ldq, const float* __res
     for (int u = 0; u < V; ++u) df_fma(acc, q[u], x[u]);
   }
   const double s = block_sum_d(df_value(acc), sh);
-  if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.x] = s;
+  if (threadIdx.x == 0) red[(int64_t)(l * k + c) * nblk + blockIdx.y] = s;
 }
 
 // qt[l] = QᵀX[l, c] from its partials (nblk = 1: final values), l < cq ≤ SLEMM_MAX_COVARIATES,
@@ -131,7 +132,7 @@ proj_apply_kernel(const float* __restrict__ Q, int64_t ldq, int cq, float* __res
 template <int V>
 static void launch_proj_partial(slemm_geno* g, const float* X, int64_t ldx, int k, double* red, int nblk)
 {
-  proj_partial_kernel<V><<<dim3(nblk, g->c * k), kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, X, ldx,
+  proj_partial_kernel<V><<<dim3(g->c * k, nblk), kRedThreads, 0, g->stream>>>(g->Q.as<float>(), g->n_pad, X, ldx,
                                                                                g->n, k, red, nblk);
   LAUNCH_CHECK();
 }
