@@ -137,6 +137,7 @@ int slemm_gpu_genotype_rows(slemm_geno* g, const int64_t* rows, int cnt, float* 
 int slemm_gpu_set_weights(slemm_geno* g, const float* gm, const float* w, const float* rr);
 /* Q: host n×c column-major orthonormal basis of R^{-1/2}X (src/reml.cpp:583-585). c may be 0. */
 int slemm_gpu_set_projection(slemm_geno* g, const float* Q, int64_t ldq, int c);
+/* prec: SLEMM_PREC_* (a new handle, or view, starts at SLEMM_PREC_FP16X2). */
 int slemm_gpu_set_precision(slemm_geno* g, int prec);
 /* per_vector != 0 makes every operator run one column at a time (the plain per-vector path). */
 int slemm_gpu_set_per_vector(slemm_geno* g, int per_vector);

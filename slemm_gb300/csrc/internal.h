@@ -15,7 +15,7 @@ struct slemm_geno {
   slemm::DevBuf Q;                // n_pad × c column-major, zero padded rows
   int c = 0;
   bool weights_set = false;
-  int prec = SLEMM_PREC_BF16X2;
+  int prec = SLEMM_PREC_FP16X2;
   int per_vector = 0;
   int lanczos_mode = 0;           // SLEMM_LANCZOS_* bits of the seeds run on this handle
   int autotune = 0;               // tensor-core plans: 0 the fixed rule, 1 the tuner's, 2 the fixed rule
