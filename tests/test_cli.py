@@ -229,3 +229,58 @@ def test_gwa_command_matches_reference_script_output(tmp_path):
     assert r.returncode == 0, r.stderr
     assert "Completed building blocks:" in r.stdout
     _compare_stats(tmp_path / "gwa.txt", os.path.join(src, "gwa.txt"))
+
+
+def test_gwas_io_helpers(tmp_path):
+    """The step-2 commands' readers and writers, as bin/slemm_gamma.py / slemm_gwa.py parse and
+    print: .psam IID column ('#IID' header → first column, .fam → second), the SLEMM sample
+    subset in .psam order, output headers, NumPy-style value printing, --maf raising --mac."""
+    from slemm_gb300.cli import _gwas_io as io
+    pheno = {"b": "1.5", "d": "-2"}
+    covar = {"b": ["1", "0.5"], "d": ["1", "-0.25"]}
+    diagr = {"b": "1", "d": "2"}
+    (tmp_path / "x.psam").write_text("#IID\tSEX\na\t1\nb\t2\nc\t1\nd\t2\n")
+    raw, subset, y, cov, R = io.read_samples(str(tmp_path / "x.psam"), pheno, covar, diagr, 2)
+    assert raw == 4 and list(subset) == [1, 3] and list(y) == [1.5, -2.0]
+    assert cov.tolist() == [[1.0, 0.5], [1.0, -0.25]] and list(R) == [1.0, 2.0]
+    (tmp_path / "x.fam").write_text("F b 0 0 1 -9\nF d 0 0 2 -9\n")
+    raw, subset, y, _, _ = io.read_samples(str(tmp_path / "x.fam"), pheno, covar, diagr, 2)
+    assert raw == 2 and subset is None and list(y) == [1.5, -2.0]
+    with pytest.raises(SystemExit):   # a SLEMM sample missing from the sample file
+        io.read_samples(str(tmp_path / "x.fam"), dict(pheno, e="0"), dict(covar, e=["1", "0"]),
+                        dict(diagr, e="1"), 2)
+    assert io.output_header("#CHROM\tPOS\tID\tREF\tALT\n", "1\t5\ts\tA\tG") == \
+        "#CHROM\tPOS\tID\tREF\tALT\tBETA\tSE\tCHISQ\tP\n"
+    assert io.output_header(None, "1 s 0 5 A G").startswith("CHR\tSNP\tCM\tBP\tA1\tA2\t")
+    assert io.output_header(None, "1 s 5 A G").startswith("CHR\tSNP\tBP\tA1\tA2\t")
+    io.write_stats(str(tmp_path / "o.txt"), None, ["1 s1 0 5 A G\n", "1 s2 0 9 A G\n"], 1,
+                   np.array([0.25], np.float32), np.array([0.1], np.float32), np.array([6.25], np.float32),
+                   np.array([0.0124193], np.float64))
+    assert open(tmp_path / "o.txt").read().splitlines() == [
+        "CHR\tSNP\tCM\tBP\tA1\tA2\tBETA\tSE\tCHISQ\tP", "1 s2 0 9 A G\t0.25\t0.1\t6.25\t0.0124193"]
+    assert io.mac_threshold(20, 0.0, 1000) == 20 and io.mac_threshold(20, 0.05, 1000) == 100
+    (tmp_path / "p.bed").write_bytes(bytes([0x6C, 0x1B, 0x01, 0xFF, 0x00]))
+    assert io.bed_rows(str(tmp_path / "p.bed"), 4, 2).tolist() == [[0xFF], [0x00]]
+    with pytest.raises(SystemExit):
+        io.bed_rows(str(tmp_path / "p.bed"), 4, 3)                       # fewer rows than variants
+    (tmp_path / "q.bed").write_bytes(bytes([0x6C, 0x1B, 0x00, 0x00]))  # individual-major PLINK 1
+    with pytest.raises(SystemExit):
+        io.bed_rows(str(tmp_path / "q.bed"), 4, 1)
+
+
+def test_gamma_statistics_and_correction_factor():
+    """beta = xy/xx·cf, se = √(Vg·cf/xx), χ² = (beta/se)², p = χ²₁ survival in the script's dtypes
+    (FP32 statistics, FP64 p), NaN where filtered; the correction factor is the mean inside
+    Tukey's fences (bin/slemm_gamma.py:88-104, 321-325)."""
+    from scipy.stats import chi2
+    from slemm_gb300.cli import slemm_gamma as sg
+    xy = np.array([2.0, np.nan, -1.0], np.float32)
+    xx = np.array([4.0, np.nan, 8.0], np.float32)
+    beta, se, chisq, p = sg.stats(xy, xx, 1.1, 0.3)
+    assert beta.dtype == np.float32 and se.dtype == np.float32 and p.dtype == np.float64
+    assert np.isnan(beta[1]) and np.isnan(p[1])
+    assert beta[0] == np.float32(2.0) / np.float32(4.0) * np.float32(1.1)
+    assert np.isclose(se[2], np.sqrt(0.3 * 1.1 / 8.0), rtol=1e-6)
+    assert np.isclose(p[0], chi2.sf(float(chisq[0]), 1), rtol=1e-12)
+    x = [1.0, 1.1, 0.9, 1.05, 0.95, 10.0]                 # 10 is outside the fences
+    assert np.isclose(sg.mean_wo_outliers(x), np.mean(x[:5]))
