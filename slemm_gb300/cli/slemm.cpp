@@ -13,8 +13,10 @@
 // Error behaviour follows the reference: problems found while reading input files print a message
 // and exit with status 1; errors of the analysis print to stderr and the run ends normally.
 //
-// Options beyond the reference's: --gpu_device N (default 0) and --gpu_precision
-// fp16x2|bf16x2|bf16x3|fp32 (default fp16x2, the column-scaled FP16 hi+lo products).
+// Options beyond the reference's: --gpu_device N (default 0), --gpu_precision
+// fp16x2|bf16x2|bf16x3|fp32 (default fp16x2, the column-scaled FP16 hi+lo products),
+// --gpu_autotune (split-K counts and ring plans of the packed products timed at first use) and
+// --gpu_lanczos_reorth (reorthogonalised Lanczos seeds instead of the reference's recurrence).
 #include "slemm_gpu.h"
 
 #include <getopt.h>
@@ -447,6 +449,7 @@ void run(int argc, char** argv)
   bool using_nr = false, using_ws = false;
   float sig_chisq = 1e6f, indep_r2 = 0.5f, max_h2 = 0.7f, min_maf = 0.f, rel_tol = 5e-4f, min_hwep = 0.f;
   int seed = 0, num_rand = 30, window_size = 1000, num_qf = 30, num_threads = 1, hwe_midp = 0, device = 0;
+  bool gpu_autotune = false, gpu_reorth = false;
   unsigned subset_size = 1000;
   std::pair<float, float> beta_params{1.f, 1.f};
   std::string est_file, phen_file, trait, err_weight, covar_file, covar_names_str, snp_info, snp_group, snp_weight,
@@ -469,9 +472,10 @@ void run(int argc, char** argv)
       {"wls", no_argument, 0, 'S'},                   {"lrt", no_argument, 0, 'T'},
       {"iter_weighting", no_argument, 0, 'I'},        {"sig_chisq", required_argument, 0, 's'},
       {"indep_r2", required_argument, 0, 'n'},        {"gpu_device", required_argument, 0, 'D'},
-      {"gpu_precision", required_argument, 0, 'G'},   {0, 0, 0, 0}};
+      {"gpu_precision", required_argument, 0, 'G'},   {"gpu_autotune", no_argument, 0, 'A'},
+      {"gpu_lanczos_reorth", no_argument, 0, 'O'},    {0, 0, 0, 0}};
   int idx = 0, opt;
-  while ((opt = getopt_long(argc, argv, "HPRLFSTIi:a:w:j:p:t:e:c:v:m:x:y:g:b:u:o:z:r:k:f:q:h:d:s:n:D:G:", opts,
+  while ((opt = getopt_long(argc, argv, "HPRLFSTIAOi:a:w:j:p:t:e:c:v:m:x:y:g:b:u:o:z:r:k:f:q:h:d:s:n:D:G:", opts,
                             &idx)) != -1) {
     if (opt == '?' || opt == ':') {
       print_help();
@@ -527,6 +531,8 @@ void run(int argc, char** argv)
       case 'n': indep_r2 = std::stof(optarg); break;
       case 'D': device = std::stoi(optarg); break;
       case 'G': precision = optarg; break;
+      case 'A': gpu_autotune = true; break;
+      case 'O': gpu_reorth = true; break;
       default:
         print_help();
         std::exit(1);
@@ -678,6 +684,8 @@ void run(int argc, char** argv)
   rows.clear();
   rows.shrink_to_fit();
   check(slemm_gpu_set_precision(G, prec));
+  if (gpu_autotune) check(slemm_gpu_set_autotune(G, 1));
+  if (gpu_reorth) check(slemm_gpu_set_lanczos(G, SLEMM_LANCZOS_REORTH));
 
   std::vector<float> Py(n, 0.f), snp_blup(m, 0.f), blue(c, 0.f), var_blue;
   float vg = 0, ve = 0, llr = 0;

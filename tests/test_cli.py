@@ -61,6 +61,16 @@ def test_cli_reports_missing_required_options(cli):
     assert "--min_maf is out of [0, 0.5)" in r.stderr
 
 
+def test_cli_gpu_options_parse(cli):
+    """The options beyond the reference's are parsed (and echoed like the reference's own) before
+    the input checks: --gpu_device, --gpu_precision, --gpu_autotune, --gpu_lanczos_reorth."""
+    r = run(cli, "--reml", "--gpu_device", "0", "--gpu_precision", "bf16x2", "--gpu_autotune", "--gpu_lanczos_reorth",
+            "--bfile", "nothing")
+    assert "OPTION gpu_autotune initialized" in r.stdout and "OPTION gpu_lanczos_reorth initialized" in r.stdout
+    assert "OPTION gpu_precision with ARG bf16x2" in r.stdout
+    assert "--phenotype_file is required" in r.stderr
+
+
 def test_cli_input_file_errors_exit_1(cli, tmp_path):
     (tmp_path / "p.csv").write_text("IID,y,cov1\nI0,1.0,2\n")
     (tmp_path / "s.csv").write_text("SNP\nS0\n")
