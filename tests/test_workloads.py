@@ -93,3 +93,37 @@ def test_roofline_object_arithmetic():
     assert roof["traffic"] == pytest.approx(want)
     assert bench.roofline(prof, n, m, "bf16x2")[0]["traffic"] is None   # no capture of that kernel
     assert bench.roofline([], n, m, "fp16x2") == (None, None)
+
+
+def test_reference_arm_application_model():
+    """The reference arm's whole-fit model: every Lanczos step of a seed runs the reference's whole
+    subset loop on that seed's block (src/reml.cpp:293-322); the window-weighted workload adds the
+    MC-REML first stage.  Seconds = Σ count·(m/1000)·(a + passes·b·k)."""
+    cfg = bench.CONFIGS[3]
+    st = bench.REF_STEPS[3]
+    apps = bench.reference_applications(cfg, st)
+    by = {w: (p, k, c) for w, p, k, c in apps}
+    assert by["DF-REML L_Seed ldet V"] == (2, cfg["probes"], st["iters_V"])
+    assert by["DF-REML L_Seed quadform y"] == (2, 1, st["iters_y"])
+    assert by["MC-REML L_Seed quadform [y|Zu|e]"] == (2, 1 + 2 * st["n_mc"], st["first_iters_V"])
+    a, b = 0.07, 0.001
+    want = sum(c * (cfg["m"] / 1000) * (a + p * b * k) for _, p, k, c in apps)
+    assert bench.reference_seconds(a, b, cfg["m"], apps) == pytest.approx(want)
+    # DF-REML alone for the workload without windows
+    assert all(not w.startswith("MC-REML") for w, *_ in bench.reference_applications(bench.CONFIGS[2],
+                                                                                      bench.REF_STEPS[2]))
+    # the counts a GPU fit reports map onto the same model
+    res = {"iters": [287, 2, 331], "fixed": [], "first_stage": {"iters_V": 15, "n_criterion": 4}}
+    st2 = bench.fit_counts(cfg, res)
+    assert st2 == dict(iters_y=287, iters_Q=2, iters_V=331, c=1, first_iters_V=15, first_n_criterion=4,
+                       n_mc=bench.mc_samples(cfg["n"]))
+
+
+def test_both_arms_print_the_same_config():
+    """The GPU and reference arms share one config object per workload (their arithmetic is each
+    line's own precision key), and the L2 note states the packed bytes each pass streams."""
+    cfg = bench.CONFIGS[3]
+    c = bench.gpu_config(cfg)
+    assert c == bench.gpu_config(dict(cfg))
+    assert "precision" not in c and c["n"] == 500000 and c["m"] == 60000
+    assert "7.50 GB packed" in c["l2"]
